@@ -1,0 +1,271 @@
+"""Python binding of libcortrace.so through its C ABI (include/cor_trace.h).
+
+The structured numpy dtypes below have the exact C layouts of the header's
+structs, so arrays of jobs, parameter blocks, records and site results pass
+to the library as plain pointers.  Loading fails loudly when the library has
+not been built: there is no fallback implementation behind this module.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+from dataclasses import dataclass
+
+import numpy as np
+
+PKG = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(PKG, "libcortrace.so")
+
+COR_OK = 0
+ERRORS = {-1: "invalid", -2: "nomem", -3: "cuda", -4: "watchdog", -5: "nodev", -6: "unsupported", -7: "range"}
+
+INTERNAL_NONE, INTERNAL_SH = 0, 1
+EXTERNAL_NONE, EXTERNAL_T96, EXTERNAL_TS05 = 0, 1, 2
+CRUSTAL_NONE, CRUSTAL_CHAOS = 0, 1
+
+TRAJ_NONE, TRAJ_ALLOWED, TRAJ_REENTRY, TRAJ_SUPERLUM, TRAJ_STEP_LIMIT, TRAJ_WATCHDOG = range(6)
+
+# Physical constants of the reference (src/common.h:4-11).
+DEF_PI = 3.141592654
+DEF_RE = 6.3712e+06
+DEF_C = 2.99725e+08
+DEF_HM0_P = 1.6725e-27
+DEF_HM0_E = 9.1093826e-31
+
+SH = 105
+
+JOB_DTYPE = np.dtype([
+    ("r0", "f8"), ("the0", "f8"), ("fi0", "f8"), ("the1", "f8"), ("fi1", "f8"),
+    ("rig", "f8"), ("del", "f8"), ("rk", "f8"), ("zn", "f8"),
+    ("nk1", "i4"), ("param_index", "i4")], align=True)
+PARAMS_DTYPE = np.dtype([
+    ("parmod", "f8", (10,)), ("g", "f8", (SH,)), ("h", "f8", (SH,)), ("rec", "f8", (SH,)),
+    ("a1", "f8", (3,)), ("a2", "f8", (3,)), ("a3", "f8", (3,))], align=True)
+RECORD_DTYPE = np.dtype([
+    ("pos", "f8", (3,)), ("vel", "f8", (3,)), ("v", "f8"), ("time", "f8"), ("length", "f8"),
+    ("steps", "u4"), ("trials", "u4"), ("status", "i4"), ("reserved", "i4")], align=True)
+SITE_DTYPE = np.dtype([
+    ("r_lower", "f8"), ("r_upper", "f8"), ("r_cutoff", "f8"),
+    ("n_forbidden", "i4"), ("n_traj", "i4")], align=True)
+TRIG_DTYPE = np.dtype([(k, "f8") for k in ("st0", "ct0", "sp0", "cp0", "st1", "ct1", "sp1", "cp1")], align=True)
+
+assert JOB_DTYPE.itemsize == 80 and PARAMS_DTYPE.itemsize == 2672
+assert RECORD_DTYPE.itemsize == 88 and SITE_DTYPE.itemsize == 32
+
+
+class ModelSet(C.Structure):
+    _fields_ = [("internal_model", C.c_int32), ("external_model", C.c_int32),
+                ("crustal_model", C.c_int32), ("reserved", C.c_int32)]
+
+
+class Counters(C.Structure):
+    _fields_ = [("accepted_steps", C.c_uint64), ("trials", C.c_uint64), ("trajectories", C.c_uint64),
+                ("watchdog", C.c_uint64), ("turn_fallbacks", C.c_uint64)]
+
+    def as_dict(self) -> dict:
+        return {k: int(getattr(self, k)) for k, _ in self._fields_}
+
+
+class BatchReq(C.Structure):
+    _fields_ = [("jobs", C.c_void_p), ("n_jobs", C.c_int32), ("n_params", C.c_int32), ("params", C.c_void_p),
+                ("models", ModelSet), ("step_limit", C.c_uint64), ("tu_angle", C.c_double),
+                ("particle_mass", C.c_double)]
+
+
+class BatchResult(C.Structure):
+    _fields_ = [("sites", C.c_void_p), ("status", C.c_void_p), ("records", C.c_void_p), ("counters", Counters)]
+
+
+# Every symbol the header declares (checked by the CPU test suite).
+EXPORTS = [
+    "cor_ctx_create", "cor_ctx_destroy", "cor_last_error_string", "cor_abi_version", "cor_batch_count",
+    "cor_prepare_trig", "cor_trace_batch", "cor_trace_batch_device", "cor_field_batch",
+    "cor_internal_setup", "cor_gsm_setup",
+]
+
+_lib = None
+
+
+def load(path: str = LIB_PATH) -> C.CDLL:
+    """Load libcortrace.so; raises if it has not been built."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(path):
+        raise RuntimeError(f"libcortrace.so is not built ({path}); run __graft_entry__.build()")
+    lib = C.CDLL(path)
+    vp, i32, i64, u64, dbl = C.c_void_p, C.c_int32, C.c_int64, C.c_uint64, C.c_double
+    lib.cor_ctx_create.argtypes = [C.c_int, C.POINTER(vp)]
+    lib.cor_ctx_destroy.argtypes = [vp]
+    lib.cor_last_error_string.argtypes = [vp]
+    lib.cor_last_error_string.restype = C.c_char_p
+    lib.cor_abi_version.restype = C.c_int
+    lib.cor_batch_count.argtypes = [vp, i32, C.POINTER(u64), vp]
+    lib.cor_prepare_trig.argtypes = [vp, i32, vp]
+    lib.cor_trace_batch.argtypes = [vp, C.POINTER(BatchReq), C.POINTER(BatchResult)]
+    lib.cor_trace_batch_device.argtypes = [vp, vp, vp, i32, vp, u64, vp, i32, ModelSet, u64, dbl, dbl,
+                                           vp, vp, vp, vp, vp]
+    lib.cor_field_batch.argtypes = [vp, ModelSet, vp, i32, vp, vp, i64, vp]
+    lib.cor_internal_setup.argtypes = [C.c_char_p, vp, vp]
+    lib.cor_gsm_setup.argtypes = [vp, vp]
+    _lib = lib
+    return lib
+
+
+def _ptr(a: np.ndarray | None) -> int | None:
+    return None if a is None else a.ctypes.data
+
+
+class CorError(RuntimeError):
+    def __init__(self, code: int, msg: str):
+        super().__init__(f"cor error {code} ({ERRORS.get(code, '?')}): {msg}")
+        self.code = code
+
+
+def internal_setup(version: str, time7, parmod=None) -> np.ndarray:
+    """internal_recalc for model `version` at time {iy, mes, ide, id, ih, min, is}."""
+    lib = load()
+    p = np.zeros(1, PARAMS_DTYPE)
+    t = np.asarray(time7, dtype=np.int32)
+    rc = lib.cor_internal_setup(version.encode(), _ptr(t), _ptr(p))
+    if rc != COR_OK:
+        raise CorError(rc, f"internal set-up of {version} at {list(time7)}")
+    if parmod is not None:
+        p["parmod"][0, :len(parmod)] = parmod
+    return p
+
+
+def batch_offsets(jobs: np.ndarray) -> tuple[int, np.ndarray]:
+    lib = load()
+    off = np.zeros(len(jobs) + 1, np.uint64)
+    n = C.c_uint64(0)
+    rc = lib.cor_batch_count(_ptr(jobs), len(jobs), C.byref(n), _ptr(off))
+    if rc != COR_OK:
+        raise CorError(rc, "bad rigidity grid")
+    return int(n.value), off
+
+
+def prepare_trig(jobs: np.ndarray) -> np.ndarray:
+    lib = load()
+    out = np.zeros(len(jobs), TRIG_DTYPE)
+    rc = lib.cor_prepare_trig(_ptr(jobs), len(jobs), _ptr(out))
+    if rc != COR_OK:
+        raise CorError(rc, "trig")
+    return out
+
+
+@dataclass
+class ScanResult:
+    sites: np.ndarray
+    status: np.ndarray | None
+    records: np.ndarray | None
+    offsets: np.ndarray
+    counters: dict
+
+
+def model_set(internal=INTERNAL_SH, external=EXTERNAL_NONE, crustal=CRUSTAL_NONE) -> ModelSet:
+    return ModelSet(internal, external, crustal, 0)
+
+
+class Context:
+    """One libcortrace context bound to a CUDA device."""
+
+    def __init__(self, device: int = 0):
+        self.lib = load()
+        h = C.c_void_p()
+        rc = self.lib.cor_ctx_create(device, C.byref(h))
+        if rc != COR_OK:
+            raise CorError(rc, f"cannot create a context on device {device}")
+        self.h = h
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.lib.cor_ctx_destroy(self.h)
+            self.h = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def error(self) -> str:
+        s = self.lib.cor_last_error_string(self.h)
+        return s.decode() if s else ""
+
+    def _check(self, rc: int, what: str):
+        if rc != COR_OK:
+            raise CorError(rc, f"{what}: {self.error()}")
+
+    def trace_batch(self, jobs: np.ndarray, params: np.ndarray, models: ModelSet | None = None,
+                    step_limit: int = 25000, tu_angle: float = 0.01, particle_mass: float = DEF_HM0_P,
+                    want_status: bool = True, want_records: bool = False) -> ScanResult:
+        """cor_trace_batch: host buffers in, host buffers out."""
+        jobs = np.ascontiguousarray(jobs, JOB_DTYPE)
+        params = np.ascontiguousarray(params, PARAMS_DTYPE)
+        n, off = batch_offsets(jobs)
+        sites = np.zeros(len(jobs), SITE_DTYPE)
+        status = np.zeros(n, np.uint8) if want_status else None
+        records = np.zeros(n, RECORD_DTYPE) if want_records else None
+        req = BatchReq(_ptr(jobs), len(jobs), len(params), _ptr(params), models or model_set(),
+                       step_limit, tu_angle, particle_mass)
+        res = BatchResult(_ptr(sites), _ptr(status), _ptr(records), Counters())
+        self._check(self.lib.cor_trace_batch(self.h, C.byref(req), C.byref(res)), "trace_batch")
+        return ScanResult(sites, status, records, off, res.counters.as_dict())
+
+    def field_batch(self, gsm_pos_m: np.ndarray, params: np.ndarray, models: ModelSet | None = None,
+                    param_index: np.ndarray | None = None) -> np.ndarray:
+        """cor_field_batch: calculate_field at GSM positions [m] -> GEO field [nT]."""
+        pos = np.ascontiguousarray(gsm_pos_m, np.float64).reshape(-1, 3)
+        params = np.ascontiguousarray(params, PARAMS_DTYPE)
+        idx = None if param_index is None else np.ascontiguousarray(param_index, np.int32)
+        out = np.zeros_like(pos)
+        rc = self.lib.cor_field_batch(self.h, models or model_set(), _ptr(params), len(params), _ptr(idx),
+                                      _ptr(pos), len(pos), _ptr(out))
+        self._check(rc, "field_batch")
+        return out
+
+
+def make_job(lat, lon, rig=0.05, rk=20.0, dele=0.05, r0=1.0031391260673028, the1=None, fi1=None,
+             zn=1.0, nk1=100, param_index=0) -> np.ndarray:
+    """One scan (INFILE) as a JOB_DTYPE record; vertical incidence by default."""
+    j = np.zeros(1, JOB_DTYPE)
+    j["r0"], j["the0"], j["fi0"] = r0, lat, lon
+    j["the1"] = lat if the1 is None else the1
+    j["fi1"] = lon if fi1 is None else fi1
+    j["rig"], j["del"], j["rk"], j["zn"] = rig, dele, rk, zn
+    j["nk1"], j["param_index"] = nk1, param_index
+    return j
+
+
+class _ChaosTable(C.Structure):
+    _fields_ = [("version", C.c_char_p), ("name", C.c_char_p), ("nmax", C.c_int),
+                ("g", C.POINTER(C.c_double)), ("h", C.POINTER(C.c_double))]
+
+
+def chaos_table() -> tuple[np.ndarray, np.ndarray, int]:
+    """The CHAOS-7.16 lithospheric table compiled into the library, as the
+    packed lower triangles (index n*(n+1)/2 + m) of G and H."""
+    lib = load()
+    t = _ChaosTable.in_dll(lib, "cor_chaos716")
+    n = t.nmax * (t.nmax + 1) // 2
+    g = np.ctypeslib.as_array(t.g, shape=(n,)).copy()
+    h = np.ctypeslib.as_array(t.h, shape=(n,)).copy()
+    return g, h, int(t.nmax)
+
+
+def chaos_dense() -> tuple[np.ndarray, np.ndarray, int]:
+    """CHAOS G and H as dense nmax x nmax tables (zero above the diagonal)."""
+    g, h, nmax = chaos_table()
+    G = np.zeros((nmax, nmax))
+    H = np.zeros((nmax, nmax))
+    rows, cols = np.tril_indices(nmax)
+    G[rows, cols] = g
+    H[rows, cols] = h
+    return G, H, nmax

@@ -1,0 +1,201 @@
+// cor_device.cuh -- FP64 device building blocks of the rigidity scan.
+//
+// Every function here keeps the reference's expression order, and the
+// translation units that include it are compiled with --fmad=false (the
+// reference is built with -ffp-contract=off, CMakeLists.txt:17), so each
+// result is the correctly rounded IEEE value of the same expression tree:
+// bit-identical to the reference wherever only + - * / sqrt are involved.
+#pragma once
+
+#include <stdint.h>
+
+#include "../../include/cor_trace.h"
+
+namespace cor {
+
+// Legacy-truncated constants of src/common.h:4-11.
+constexpr double kPi = 3.141592654;
+constexpr double k2Pi = 6.28318531;
+constexpr double kRe = 6.3712e+06;
+constexpr double kToRad = kPi / 180.;
+constexpr double kQ = 1.6021e-19;
+constexpr double kC = 2.99725e+08;
+
+// Boundary refinement bound (the reference doubles nk0 without one,
+// src/trajectory.c:126-130).
+constexpr int kNk0Cap = 1 << 30;
+
+struct Vec3 {
+    double x, y, z;
+};
+
+// geo_to_gsm, src/utils.c:75-87 (rows of A).
+__device__ __forceinline__ Vec3 geo_to_gsm(const Vec3 g, const cor_model_params* __restrict__ p) {
+    Vec3 s;
+    s.x = __ldg(&p->a1[0]) * g.x + __ldg(&p->a1[1]) * g.y + __ldg(&p->a1[2]) * g.z;
+    s.y = __ldg(&p->a2[0]) * g.x + __ldg(&p->a2[1]) * g.y + __ldg(&p->a2[2]) * g.z;
+    s.z = __ldg(&p->a3[0]) * g.x + __ldg(&p->a3[1]) * g.y + __ldg(&p->a3[2]) * g.z;
+    return s;
+}
+
+// gsm_to_geo, src/utils.c:89-101 (columns of A).
+__device__ __forceinline__ Vec3 gsm_to_geo(const Vec3 s, const cor_model_params* __restrict__ p) {
+    Vec3 g;
+    g.x = __ldg(&p->a1[0]) * s.x + __ldg(&p->a2[0]) * s.y + __ldg(&p->a3[0]) * s.z;
+    g.y = __ldg(&p->a1[1]) * s.x + __ldg(&p->a2[1]) * s.y + __ldg(&p->a3[1]) * s.z;
+    g.z = __ldg(&p->a1[2]) * s.x + __ldg(&p->a2[2]) * s.y + __ldg(&p->a3[2]) * s.z;
+    return g;
+}
+
+// Spherical-harmonic internal field, internal_geo (lib/internal/internal.c:182-275).
+// Degree truncated by radius, NM = min(13, 3 + 30/((int)R + 2)) (:201-205).
+// The (m, n) double loop is unrolled with compile-time indices so the
+// powers of 1/R stay in registers; the loop exits at the lane's own degree.
+__device__ __forceinline__ Vec3 internal_geo(const Vec3 x, const cor_model_params* __restrict__ p) {
+    const double rho2 = x.x * x.x + x.y * x.y;
+    const double R = sqrt(rho2 + x.z * x.z);
+    const double C = x.z / R;
+    const double rho = sqrt(rho2);
+    const double S = rho / R;
+    const bool pole = S < 1.E-5;
+    double cf, sf;
+    if (pole) {
+        cf = 1.;
+        sf = 0.;
+    } else {
+        cf = x.x / rho;
+        sf = x.y / rho;
+    }
+    const double pp = 1. / R;
+    int nm = 3 + 30 / ((int)R + 2);
+    if (nm > 13) nm = 13;
+    const int K = nm + 1;
+
+    double pw[14], pwn[14];
+    {
+        double pr = pp;
+#pragma unroll
+        for (int n = 1; n <= 14; n++) {
+            pr = pr * pp;
+            pw[n - 1] = pr;
+            pwn[n - 1] = pr * n;
+        }
+    }
+
+    const double* __restrict__ G = p->g;
+    const double* __restrict__ H = p->h;
+    const double* __restrict__ REC = p->rec;
+    double pmm = 1., dmm = 0.;
+    double br = 0., bt = 0., bf = 0.;
+    double cm = 0., sm = 1.;
+#pragma unroll
+    for (int m = 1; m <= 14; m++) {
+        if (m > K) break;
+        if (m != 1) {
+            const double w = cm;
+            cm = w * cf + sm * sf;
+            sm = sm * cf - w * sf;
+        }
+        double q = pmm, zz = dmm, bi = 0., p2 = 0., d2 = 0.;
+#pragma unroll
+        for (int n = m; n <= 14; n++) {
+            if (n > K) break;
+            const double an = pw[n - 1];
+            const int mn = n * (n - 1) / 2 + m - 1;
+            const double e = __ldg(&G[mn]);
+            const double hh = __ldg(&H[mn]);
+            const double w = e * sm + hh * cm;
+            br = br + pwn[n - 1] * w * q;
+            bt = bt - an * w * zz;
+            if (m != 1) {
+                const double qq = pole ? zz : q;
+                bi = bi + an * (e * cm - hh * sm) * qq;
+            }
+            const double xk = __ldg(&REC[mn]);
+            const double dp = C * zz - S * q - xk * d2;
+            const double pm = C * q - xk * p2;
+            d2 = zz;
+            p2 = q;
+            zz = dp;
+            q = pm;
+        }
+        dmm = S * dmm + C * pmm;
+        pmm = S * pmm;
+        if (m != 1) {
+            bi = bi * (m - 1);
+            bf = bf + bi;
+        }
+    }
+    double bphi;
+    if (pole) {
+        if (C < 0.) bf = -bf;
+        bphi = bf;
+    } else {
+        bphi = bf / S;
+    }
+    const double he = br * S + bt * C;
+    Vec3 b;
+    b.x = he * cf - bphi * sf;
+    b.y = he * sf + bphi * cf;
+    b.z = br * C - bt * S;
+    return b;
+}
+
+// Velocity half of calculate_position_and_speed (src/trajectory.c:277-329,
+// :350-352): six stages of dv/dt = d (v x B) with B frozen.  Returns the
+// updated velocity; the position half is separate because a trial rejected
+// by the turn-angle test never uses it.
+__device__ __forceinline__ Vec3 rk_velocity(const double h, const double d, const Vec3 f, const Vec3 v) {
+#define CX(Y, Z) (h * (d * ((Y)*f.z - (Z)*f.y)))
+#define CY(X, Z) (h * (d * ((Z)*f.x - (X)*f.z)))
+#define CZ(X, Y) (h * (d * ((X)*f.y - (Y)*f.x)))
+    const double a1 = CX(v.y, v.z), b1 = CY(v.x, v.z), c1 = CZ(v.x, v.y);
+    const double sx2 = v.x + a1 / 3., sy2 = v.y + b1 / 3., sz2 = v.z + c1 / 3.;
+    const double a2 = CX(sy2, sz2), b2 = CY(sx2, sz2), c2 = CZ(sx2, sy2);
+    const double sx3 = v.x + (4. * a1 + 6. * a2) / 25.;
+    const double sy3 = v.y + (4. * b1 + 6. * b2) / 25.;
+    const double sz3 = v.z + (4. * c1 + 6. * c2) / 25.;
+    const double a3 = CX(sy3, sz3), b3 = CY(sx3, sz3), c3 = CZ(sx3, sy3);
+    const double sx4 = v.x + (a1 - 12. * a2 + 15. * a3) / 4.;
+    const double sy4 = v.y + (b1 - 12. * b2 + 15. * b3) / 4.;
+    const double sz4 = v.z + (c1 - 12. * c2 + 15. * c3) / 4.;
+    const double a4 = CX(sy4, sz4), b4 = CY(sx4, sz4), c4 = CZ(sx4, sy4);
+    const double sx5 = v.x + (6. * a1 + 90. * a2 - 50. * a3 + 8. * a4) / 81.;
+    const double sy5 = v.y + (6. * b1 + 90. * b2 - 50. * b3 + 8. * b4) / 81.;
+    const double sz5 = v.z + (6. * c1 + 90. * c2 - 50. * c3 + 8. * c4) / 81.;
+    const double a5 = CX(sy5, sz5), b5 = CY(sx5, sz5), c5 = CZ(sx5, sy5);
+    const double sx6 = v.x + (6. * a1 + 36. * a2 + 10. * a3 + 8. * a4) / 75.;
+    const double sy6 = v.y + (6. * b1 + 36. * b2 + 10. * b3 + 8. * b4) / 75.;
+    const double sz6 = v.z + (6. * c1 + 36. * c2 + 10. * c3 + 8. * c4) / 75.;
+    const double a6 = CX(sy6, sz6), b6 = CY(sx6, sz6), c6 = CZ(sx6, sy6);
+#undef CX
+#undef CY
+#undef CZ
+    Vec3 o;
+    o.x = v.x + (23. * a1 + 125. * a3 - 81. * a5 + 125. * a6) / 192.;
+    o.y = v.y + (23. * b1 + 125. * b3 - 81. * b5 + 125. * b6) / 192.;
+    o.z = v.z + (23. * c1 + 125. * c3 - 81. * c5 + 125. * c6) / 192.;
+    return o;
+}
+
+// Position half of calculate_position_and_speed (src/trajectory.c:331-348,
+// :353-355): the same tableau on h*v with the unrotated velocity.
+__device__ __forceinline__ double rk_position_1(const double h, const double vc, const double xc) {
+    const double k1 = h * vc;
+    const double k2 = h * (vc + k1 / 3.);
+    const double k3 = h * (vc + (4. * k1 + 6. * k2) / 25.);
+    const double k4 = h * (vc + (k1 - 12. * k2 + 15. * k3) / 4.);
+    const double k5 = h * (vc + (6. * k1 + 90. * k2 - 50. * k3 + 8. * k4) / 81.);
+    const double k6 = h * (vc + (6. * k1 + 36. * k2 + 10. * k3 + 8. * k4) / 75.);
+    return xc + (23. * k1 + 125. * k3 - 81. * k5 + 125. * k6) / 192.;
+}
+
+__device__ __forceinline__ Vec3 rk_position(const double h, const Vec3 v, const Vec3 x) {
+    Vec3 o;
+    o.x = rk_position_1(h, v.x, x.x);
+    o.y = rk_position_1(h, v.y, x.y);
+    o.z = rk_position_1(h, v.z, x.z);
+    return o;
+}
+
+}  // namespace cor

@@ -1,0 +1,69 @@
+// field.cuh -- field composition on the device, calculate_field
+// (src/models.c:194-207) with the model list fixed at compile time.
+#pragma once
+
+#include "cor_device.cuh"
+
+namespace cor {
+
+// Compile-time model set: internal (0/1), external (0 none, 1 T96, 2 TS05),
+// crustal (0/1).  The kernels are instantiated per set so the step loop
+// carries no model dispatch.
+template <int INTERNAL, int EXTERNAL, int CRUSTAL>
+struct ModelSet {
+    static constexpr int internal = INTERNAL;
+    static constexpr int external = EXTERNAL;
+    static constexpr int crustal = CRUSTAL;
+};
+
+// Device tables of the crustal model (packed lower triangle) and its
+// per-degree recursion factors; set by the context before a crustal launch.
+struct CrustalTables {
+    const double* g;
+    const double* h;
+    int nmax;
+};
+
+__device__ Vec3 t96_gsm(const double* __restrict__ parmod, const Vec3 x);
+__device__ Vec3 ts05_gsm(const double* __restrict__ parmod, const Vec3 x);
+__device__ Vec3 chaos_geo(const Vec3 x, const CrustalTables& t);
+
+// GSM position in metres -> GEO field in nT.
+template <class MS>
+__device__ __forceinline__ Vec3 calculate_field(const Vec3 gsm_pos, const cor_model_params* __restrict__ p,
+                                                const CrustalTables& crust) {
+    const Vec3 pos = {gsm_pos.x / kRe, gsm_pos.y / kRe, gsm_pos.z / kRe};
+    Vec3 tot = {0., 0., 0.};
+    if (MS::internal) {
+        // internal_calc, src/models.c:146-160
+        const Vec3 geo = gsm_to_geo(pos, p);
+        const Vec3 bg = internal_geo(geo, p);
+        const Vec3 bs = geo_to_gsm(bg, p);
+        tot.x += bs.x;
+        tot.y += bs.y;
+        tot.z += bs.z;
+    }
+    if (MS::external == COR_EXTERNAL_T96) {
+        const Vec3 b = t96_gsm(p->parmod, pos);  // t96_calc, src/models.c:171-177
+        tot.x += b.x;
+        tot.y += b.y;
+        tot.z += b.z;
+    } else if (MS::external == COR_EXTERNAL_TS05) {
+        const Vec3 b = ts05_gsm(p->parmod, pos);  // ts05_calc, src/models.c:162-169
+        tot.x += b.x;
+        tot.y += b.y;
+        tot.z += b.z;
+    }
+    if (MS::crustal) {
+        // chaos_7_16_calc, src/models.c:179-192
+        const Vec3 geo = gsm_to_geo(pos, p);
+        const Vec3 bg = chaos_geo(geo, crust);
+        const Vec3 bs = geo_to_gsm(bg, p);
+        tot.x += bs.x;
+        tot.y += bs.y;
+        tot.z += bs.z;
+    }
+    return gsm_to_geo(tot, p);
+}
+
+}  // namespace cor

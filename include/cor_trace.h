@@ -1,0 +1,229 @@
+/*
+ * cor_trace.h -- C ABI of the GB300 cutoff-rigidity tracer (libcortrace.so).
+ *
+ * The library replaces the rigidity scan of `cor -m cutoff`:
+ *   trajectory_simulation_cutoff()   src/trajectory.c:6-161   (scan, step control, RK, terminations)
+ *   calculate_field()                src/models.c:194-207     (field composition, GSM<->GEO)
+ *   internal_geo()                   lib/internal/internal.c:182-275 (spherical-harmonic field)
+ *   t96_gsm() / ts05_gsm()           lib/t96/t96.c:4, lib/ts05/ts05.c:7 (external fields)
+ *   chaos_geo()                      lib/chaos/chaos.c:120-226 (high-degree SH field)
+ * and the host-side set-up that feeds it:
+ *   internal_recalc()                lib/internal/internal.c:89-180
+ *
+ * Every entry point takes plain pointers and sizes; no C++ or framework types
+ * cross the boundary.  All functions return COR_OK (0) or a negative COR_ERR_*
+ * code; cor_last_error_string() gives a one-line reason for the last failure on
+ * a context.  Buffers are owned by the caller.  A context is bound to one CUDA
+ * device and is not safe for concurrent use from several host threads; use one
+ * context per thread.
+ */
+#ifndef COR_TRACE_H
+#define COR_TRACE_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define COR_TRACE_ABI_VERSION 1
+
+/* Number of Gauss coefficients of the degree-13 internal models
+ * (INTERNAL_COEFS_SIZE, lib/internal/coefs/coefs.h:6). */
+#define COR_SH_COEFS 105
+
+/* ---- error codes ------------------------------------------------------ */
+#define COR_OK               0
+#define COR_ERR_INVALID     -1  /* bad argument, bad size, unknown model     */
+#define COR_ERR_NOMEM       -2  /* device or host allocation failed          */
+#define COR_ERR_CUDA        -3  /* a CUDA runtime call failed                */
+#define COR_ERR_WATCHDOG    -4  /* a kernel gave up on a bounded wait        */
+#define COR_ERR_NODEV       -5  /* no CUDA device / library built without it */
+#define COR_ERR_UNSUPPORTED -6  /* combination of models not available       */
+#define COR_ERR_RANGE       -7  /* epoch outside the coefficient table       */
+
+/* ---- field models ----------------------------------------------------- */
+/* main() builds models[] in the order internal, external, crustal
+ * (src/main.c:269-299); calculate_field sums them in that order. */
+#define COR_INTERNAL_NONE 0
+#define COR_INTERNAL_SH   1   /* any of igrf9..igrf14, hist, cals10k.2 */
+#define COR_EXTERNAL_NONE 0
+#define COR_EXTERNAL_T96  1   /* -e t96  */
+#define COR_EXTERNAL_TS05 2   /* -e ts05 */
+#define COR_CRUSTAL_NONE  0
+#define COR_CRUSTAL_CHAOS 1   /* -c chaos7.16 */
+
+typedef struct {
+    int32_t internal_model;   /* COR_INTERNAL_* */
+    int32_t external_model;   /* COR_EXTERNAL_* */
+    int32_t crustal_model;    /* COR_CRUSTAL_*  */
+    int32_t reserved;         /* must be 0      */
+} cor_model_set;
+
+/* Per-condition parameter block: the ModelsParams struct of src/models.h:9-17
+ * with the same members and meaning.  g/h are the Schmidt-scaled Gauss
+ * coefficients at the epoch, rec the Legendre recursion factors, a1..a3 the
+ * rows of the GEO->GSM rotation, parmod the external-field parameters
+ * {Pdyn, Dst, ByIMF, BzIMF, W1..W6} (src/io.c:98-127). */
+typedef struct {
+    double parmod[10];
+    double g[COR_SH_COEFS];
+    double h[COR_SH_COEFS];
+    double rec[COR_SH_COEFS];
+    double a1[3];
+    double a2[3];
+    double a3[3];
+} cor_model_params;
+
+/* One rigidity scan = one INFILE of `cor -m cutoff` (InfileHeader,
+ * src/common.h:26-54; read by read_cutoff_infile_header, src/io.c:4-20).
+ * Rigidities are rig + i*del for i = 0 .. round((rk-rig)/del)
+ * (src/trajectory.c:7,14). */
+typedef struct {
+    double r0;     /* start radius [R_E]                              */
+    double the0;   /* start geographic latitude [deg]                 */
+    double fi0;    /* start geographic longitude [deg]                */
+    double the1;   /* latitude of the initial velocity vector [deg]   */
+    double fi1;    /* longitude of the initial velocity vector [deg]  */
+    double rig;    /* first rigidity [GV]                             */
+    double del;    /* rigidity step [GV], > 0                         */
+    double rk;     /* last rigidity [GV]                              */
+    double zn;     /* charge number                                   */
+    int32_t nk1;   /* steps per gyro period (initial)                 */
+    int32_t param_index; /* which cor_model_params block this scan uses */
+} cor_scan_job;
+
+/* Termination class of one trajectory (src/trajectory.c:48-145). */
+#define COR_TRAJ_NONE        0  /* not traced                                    */
+#define COR_TRAJ_ALLOWED     1  /* escaped at r = 25 R_E or the magnetopause      */
+#define COR_TRAJ_REENTRY     2  /* r < 1 R_E                  (forbidden, rmx1)   */
+#define COR_TRAJ_SUPERLUM    3  /* v/c > 1                    (forbidden, rmx1)   */
+#define COR_TRAJ_STEP_LIMIT  4  /* step > step_limit          (forbidden, rmx2)   */
+#define COR_TRAJ_WATCHDOG    5  /* boundary refinement ran past nk0 = 2^30;
+                                   the reference has no bound here (its int nk0
+                                   would overflow).  Counted as forbidden, rmx2. */
+
+/* Final state of one trajectory.  For allowed trajectories the host derives
+ * the printed row (eth, efi, ath, afi; src/trajectory.c:91-122) from pos/vel
+ * with the C library, so the text output matches the reference digit for digit. */
+typedef struct {
+    double pos[3];     /* final GEO position [m]                 */
+    double vel[3];     /* final GEO velocity [m/s]               */
+    double v;          /* |vel| as carried by the integrator     */
+    double time;       /* accumulated time [s]                   */
+    double length;     /* accumulated path length [m]            */
+    uint32_t steps;    /* accepted steps                         */
+    uint32_t trials;   /* RK trials, accepted and rejected       */
+    int32_t status;    /* COR_TRAJ_*                             */
+    int32_t reserved;
+} cor_traj_record;
+
+/* Per-scan reduction (src/trajectory.c:156-160): P(S)=r_lower, P(C)=r_upper,
+ * P(M)=r_cutoff, exactly as printed on the CUTOFF line. */
+typedef struct {
+    double r_lower;     /* rmi  */
+    double r_upper;     /* rmx  = max(rmx1, rmx2) + del */
+    double r_cutoff;    /* rms  = rmi + zan*del */
+    int32_t n_forbidden;  /* nza */
+    int32_t n_traj;
+} cor_site_result;
+
+typedef struct {
+    uint64_t accepted_steps;  /* = field evaluations after the initial one */
+    uint64_t trials;          /* RK trials (accepted + rejected)           */
+    uint64_t trajectories;
+    uint64_t watchdog;        /* trajectories that ended COR_TRAJ_WATCHDOG */
+    uint64_t turn_fallbacks;  /* turn-angle decisions that needed atan2    */
+} cor_counters;
+
+typedef struct {
+    const cor_scan_job *jobs;          /* n_jobs scans                        */
+    int32_t n_jobs;
+    int32_t n_params;
+    const cor_model_params *params;    /* n_params parameter blocks           */
+    cor_model_set models;
+    uint64_t step_limit;               /* -s, default 25000 (src/main.c:13)   */
+    double tu_angle;                   /* -u, default 0.01 (src/main.c:19)    */
+    double particle_mass;              /* -t, proton 1.6725e-27 kg            */
+} cor_batch_req;
+
+typedef struct {
+    cor_site_result *sites;     /* n_jobs, required                              */
+    uint8_t *status;            /* n_trajectories, optional (NULL = not written) */
+    cor_traj_record *records;   /* n_trajectories, optional                      */
+    cor_counters counters;      /* filled by the call                            */
+} cor_batch_result;
+
+typedef struct cor_ctx cor_ctx;
+
+/* ---- context ---------------------------------------------------------- */
+int cor_ctx_create(int device, cor_ctx **out);
+int cor_ctx_destroy(cor_ctx *ctx);
+const char *cor_last_error_string(const cor_ctx *ctx);
+int cor_abi_version(void);
+
+/* Number of trajectories of a batch and, optionally, the exclusive prefix
+ * offsets of each job's trajectories (offsets has n_jobs+1 entries). */
+int cor_batch_count(const cor_scan_job *jobs, int32_t n_jobs,
+                    uint64_t *n_trajectories, uint64_t *offsets);
+
+/* sin/cos of the start colatitude/longitude and of the velocity direction of
+ * each scan, (90-the0), fi0, (90-the1), fi1 in radians (src/trajectory.c:18-28).
+ * Taken from the host C library so the start vectors on the device equal the
+ * reference's; cor_trace_batch computes them itself. */
+typedef struct {
+    double st0, ct0, sp0, cp0;
+    double st1, ct1, sp1, cp1;
+} cor_job_trig;
+
+int cor_prepare_trig(const cor_scan_job *jobs, int32_t n_jobs, cor_job_trig *out);
+
+/* ---- scan ------------------------------------------------------------- */
+/* Replaces trajectory_simulation_cutoff (src/trajectory.c:6) for a batch of
+ * scans.  Host buffers in and out; copies are done inside the call.  Blocks
+ * until the results are on the host. */
+int cor_trace_batch(cor_ctx *ctx, const cor_batch_req *req, cor_batch_result *out);
+
+/* Same scan with every buffer already in device memory (jobs, trig from
+ * cor_prepare_trig, offsets from cor_batch_count, params, sites, status,
+ * records); `stream` is a
+ * cudaStream_t (NULL = the legacy default stream).  Returns after the
+ * launches are queued; counters are written to the device buffer
+ * `counters_dev` (a cor_counters) and read by the caller. */
+int cor_trace_batch_device(cor_ctx *ctx,
+                           const cor_scan_job *jobs_dev, const cor_job_trig *trig_dev,
+                           int32_t n_jobs, const uint64_t *offsets_dev, uint64_t n_trajectories,
+                           const cor_model_params *params_dev, int32_t n_params,
+                           cor_model_set models, uint64_t step_limit,
+                           double tu_angle, double particle_mass,
+                           cor_site_result *sites_dev, uint8_t *status_dev,
+                           cor_traj_record *records_dev, cor_counters *counters_dev,
+                           void *stream);
+
+/* ---- field ------------------------------------------------------------ */
+/* calculate_field (src/models.c:194-207) at n points: gsm_pos is n x 3 GSM
+ * positions in metres; geo_field gets n x 3 GEO field components in nT.
+ * param_index gives, per point, the parameter block (NULL = block 0). */
+int cor_field_batch(cor_ctx *ctx, cor_model_set models,
+                    const cor_model_params *params, int32_t n_params,
+                    const int32_t *param_index, const double *gsm_pos,
+                    int64_t n, double *geo_field);
+
+/* ---- host set-up ------------------------------------------------------ */
+/* internal_recalc (lib/internal/internal.c:89-180) for a named internal
+ * model ("igrf14", "igrf13", ..., "hist", "cals10k.2"; src/models.c:22-84).
+ * time = {iy, mes, ide, id, ih, min, is} as in the INFILE.  Fills g, h, rec,
+ * a1..a3 of *out and leaves parmod untouched.  Host only; needs no GPU. */
+int cor_internal_setup(const char *version, const int32_t time[7], cor_model_params *out);
+
+/* GEO->GSM rotation alone (a1..a3), for runs without an internal model.
+ * The reference leaves these uninitialised in that case (src/main.c:51);
+ * here they are computed from the date with the IGRF-14 dipole. */
+int cor_gsm_setup(const int32_t time[7], cor_model_params *out);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* COR_TRACE_H */

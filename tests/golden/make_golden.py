@@ -1,0 +1,269 @@
+"""Make the golden fixtures in tests/golden/ by running the reference itself.
+
+The reference is compiled from its own sources (oracle/build.py -> oracle/_ref)
+and driven two ways:
+  * through its library functions (internal_recalc, internal_geo, t96_gsm,
+    ts05_gsm, chaos_geo, calculate_field) via ctypes, giving field vectors and
+    set-up blocks as exact hex floats;
+  * through its `cor` binary (`cor -p -i igrf14 [-e t96|ts05] INFILE`),
+    giving the printed rows and the CUTOFF line of whole rigidity scans.
+
+Run here (where the reference tree exists):  python tests/golden/make_golden.py [section ...]
+Sections: setup field scan0 scan_t96 scan_ts05.  The fixtures are small JSON
+files; nothing on the GPU side reads the reference.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import json
+import os
+import sys
+from concurrent.futures import ThreadPoolExecutor
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(os.path.dirname(HERE))
+sys.path.insert(0, os.path.join(ROOT, "oracle"))
+sys.path.insert(0, os.path.join(ROOT, "cor-model_gb300"))
+
+import build as obuild  # noqa: E402
+import pyoracle  # noqa: E402
+import cortrace as ct  # noqa: E402
+
+
+def hx(a) -> list[str]:
+    return [float(v).hex() for v in np.asarray(a, np.float64).ravel()]
+
+
+class Vector(C.Structure):
+    _fields_ = [("x", C.c_double), ("y", C.c_double), ("z", C.c_double)]
+
+
+class RecalcTime(C.Structure):
+    _fields_ = [(k, C.c_int) for k in ("iy", "mes", "ide", "id", "ih", "min", "is_")]
+
+
+def ref_lib() -> C.CDLL:
+    obuild.build_ref()
+    lib = C.CDLL(os.path.join(obuild.REF_OUT, "libcorref.so"))
+    vp, dbl = C.c_void_p, C.c_double
+    lib.internal_recalc.argtypes = [vp, C.POINTER(RecalcTime), vp, vp, vp, vp, vp, vp]
+    lib.internal_geo.argtypes = [dbl, dbl, dbl, vp, vp, vp, vp, vp, vp]
+    lib.t96_gsm.argtypes = [vp, dbl, dbl, dbl, vp, vp, vp]
+    lib.ts05_gsm.argtypes = [vp, dbl, dbl, dbl, vp, vp, vp]
+    lib.chaos_geo.argtypes = [dbl, dbl, dbl, vp, vp, vp, vp]
+    lib.calculate_field.argtypes = [Vector, C.POINTER(Vector), vp, vp]
+    lib.get_model.argtypes = [vp, C.c_char_p]
+    lib.get_model.restype = vp
+    return lib
+
+
+def sym(lib, name: str) -> int:
+    return C.addressof(C.c_char.in_dll(lib, name))
+
+
+COEF_SYMS = {"igrf14": "IGRF_14_COEFS", "igrf13": "IGRF_13_COEFS", "igrf12": "IGRF_12_COEFS",
+             "igrf11": "IGRF_11_COEFS", "igrf10": "IGRF_10_COEFS", "igrf9": "IGRF_9_COEFS",
+             "hist": "HIST_COEFS", "cals10k.2": "CALS10K_2_COEFS"}
+
+SETUP_CASES = [
+    ("igrf14", [2020, 1, 1, 1, 0, 0, 0]),
+    ("igrf14", [2020, 6, 21, 173, 12, 0, 0]),
+    ("igrf14", [2027, 3, 5, 64, 7, 30, 15]),
+    ("igrf14", [1965, 11, 30, 334, 23, 59, 59]),
+    ("igrf13", [2010, 1, 1, 1, 0, 0, 0]),
+    ("igrf12", [2000, 7, 4, 185, 6, 0, 0]),
+    ("igrf11", [1980, 2, 1, 32, 1, 2, 3]),
+    ("igrf10", [2007, 12, 31, 365, 18, 0, 0]),
+    ("igrf9", [1990, 5, 5, 125, 0, 0, 0]),
+    ("hist", [1500, 1, 1, 1, 0, 0, 0]),
+    ("hist", [1925, 9, 1, 244, 0, 0, 0]),
+    ("cals10k.2", [1200, 1, 1, 1, 0, 0, 0]),
+    ("cals10k.2", [0, 1, 1, 1, 0, 0, 0]),
+]
+
+
+def ref_setup(lib, version: str, tm: list[int]) -> np.ndarray:
+    p = np.zeros(1, ct.PARAMS_DTYPE)
+    t = RecalcTime(*tm)
+    rc = lib.internal_recalc(sym(lib, COEF_SYMS[version]), C.byref(t), p["g"].ctypes.data, p["h"].ctypes.data,
+                             p["rec"].ctypes.data, p["a1"].ctypes.data, p["a2"].ctypes.data, p["a3"].ctypes.data)
+    if rc != 0:
+        raise RuntimeError(f"internal_recalc {version} {tm} -> {rc}")
+    return p
+
+
+def make_setup(lib) -> dict:
+    out = []
+    for version, tm in SETUP_CASES:
+        p = ref_setup(lib, version, tm)
+        out.append({"version": version, "time": tm, **{k: hx(p[k]) for k in ("g", "h", "rec", "a1", "a2", "a3")}})
+    return {"cases": out}
+
+
+T96_PARMOD = [2.0, -20.0, 0.0, -1.0]          # Pdyn, Dst, By, Bz (config-1 conditions)
+TS05_PARMOD = [2.0, -20.0, 0.0, -1.0, 1.0, 1.0, 1.0, 1.0, 1.0, 1.0]
+
+
+def field_points(rng, n, rmin, rmax):
+    u = rng.normal(size=(n, 3))
+    u /= np.linalg.norm(u, axis=1)[:, None]
+    r = rmin + (rmax - rmin) * rng.random(n)
+    return u * r[:, None]
+
+
+def make_field(lib) -> dict:
+    rng = np.random.default_rng(20240611)
+    out = {}
+    # internal_geo at GEO points [R_E], radius 1..25, plus poles and truncation edges
+    p = ref_setup(lib, "igrf14", [2020, 1, 1, 1, 0, 0, 0])
+    pts = field_points(rng, 400, 1.0, 25.0)
+    extra = np.array([[0, 0, 1.2], [0, 0, -3.0], [1e-6, 0, 1.5], [0, 2e-6, -1.1], [1.999999, 0, 0],
+                      [2.0, 0, 0], [0, 3.0, 0], [0, 0, 12.999], [7.0, 7.0, 7.0], [1.0, 0, 0]], np.float64)
+    pts = np.vstack([pts, extra])
+    b = np.zeros(3)
+    vals = []
+    for x, y, z in pts:
+        lib.internal_geo(x, y, z, p["g"].ctypes.data, p["h"].ctypes.data, p["rec"].ctypes.data,
+                         b[0:].ctypes.data, b[1:].ctypes.data, b[2:].ctypes.data)
+        vals.append(b.copy())
+    out["internal_geo"] = {"version": "igrf14", "time": [2020, 1, 1, 1, 0, 0, 0], "points": hx(pts), "b": hx(vals)}
+    # T96 and TS05 at GSM points [R_E] inside and around the magnetopause
+    for name, fn, pm in (("t96_gsm", lib.t96_gsm, T96_PARMOD), ("ts05_gsm", lib.ts05_gsm, TS05_PARMOD)):
+        pmod = np.zeros(10)
+        pmod[:len(pm)] = pm
+        pts = field_points(rng, 300, 1.0, 25.0)
+        pts = np.vstack([pts, [[-30.0, 2.0, 1.0], [-60.0, 0.0, 3.0], [10.0, 0.0, 0.0], [11.0, 1.0, -1.0],
+                               [0.0, 0.0, 1.0], [-5.0, 0.0, 0.0]]])
+        vals = []
+        for x, y, z in pts:
+            fn(pmod.ctypes.data, x, y, z, b[0:].ctypes.data, b[1:].ctypes.data, b[2:].ctypes.data)
+            vals.append(b.copy())
+        out[name] = {"parmod": hx(pmod), "points": hx(pts), "b": hx(vals)}
+    # chaos_geo at GEO points [R_E]
+    pts = field_points(rng, 40, 1.0, 5.0)
+    vals = []
+    for x, y, z in pts:
+        lib.chaos_geo(x, y, z, sym(lib, "CHAOS_7_16_COEFS"), b[0:].ctypes.data, b[1:].ctypes.data, b[2:].ctypes.data)
+        vals.append(b.copy())
+    out["chaos_geo"] = {"points": hx(pts), "b": hx(vals)}
+    # calculate_field (GSM metres -> GEO nT) with igrf14, igrf14+t96, igrf14+ts05
+    p1 = ref_setup(lib, "igrf14", [2020, 6, 21, 173, 12, 0, 0])
+    pts = field_points(rng, 200, 1.0, 25.0) * ct.DEF_RE
+    combos = {"igrf14": ("igrf14", None, None, None),
+              "igrf14+t96": ("igrf14", "t96", None, T96_PARMOD),
+              "igrf14+ts05": ("igrf14", "ts05", None, TS05_PARMOD)}
+    out["calculate_field"] = {"time": [2020, 6, 21, 173, 12, 0, 0], "points_m": hx(pts), "cases": {}}
+    for key, (imod, emod, cmod, pm) in combos.items():
+        pp = p1.copy()
+        if pm:
+            pp["parmod"][0, :len(pm)] = pm
+        models = (C.c_void_p * 4)()
+        k = 0
+        models[k] = lib.get_model(sym(lib, "internal_models"), imod.encode()); k += 1
+        if emod:
+            models[k] = lib.get_model(sym(lib, "external_models"), emod.encode()); k += 1
+        vals = []
+        o = Vector()
+        for x, y, z in pts:
+            lib.calculate_field(Vector(x, y, z), C.byref(o), C.addressof(models), pp.ctypes.data)
+            vals.append([o.x, o.y, o.z])
+        out["calculate_field"]["cases"][key] = {"parmod": hx(pp["parmod"][0]), "b": hx(vals)}
+    return out
+
+
+# ---- whole scans through the reference binary ------------------------------
+def infile(lat, lon, the1, fi1, rig, rk, dele, time7, nk1=100, r0=1.0031391260673028, ext_lines=()):
+    lines = [f"{rig!r} 1 {rk!r}", f"{r0!r} {lat!r} {lon!r}", f"{the1!r} {fi1!r}",
+             " ".join(str(v) for v in time7), f"{nk1} 0 0 {dele!r}", *ext_lines]
+    return "\n".join(lines) + "\n"
+
+
+def parse_cor_output(text: str, rig: float, dele: float):
+    """-> (allowed indices, [P(S), P(C), P(M)] strings, rows)"""
+    rows, cut = [], None
+    lines = text.splitlines()
+    for i, ln in enumerate(lines):
+        if ln.startswith("  CUTOFF"):
+            cut = lines[i + 1].split()
+            break
+    started = False
+    for ln in lines:
+        if ln.startswith(" rig : v"):
+            started = True
+            continue
+        if started and ln.strip() and not ln.startswith("  CUTOFF"):
+            if ln.startswith("  CUTOFF"):
+                break
+            parts = ln.split()
+            if len(parts) == 9:
+                rows.append(ln)
+        if ln.startswith("  CUTOFF"):
+            break
+    idx = [int(round((float(r.split()[0]) - rig) / dele)) for r in rows]
+    return idx, cut, rows
+
+
+def run_scan_set(sites, rig, rk, dele, time7, args, ext_lines=(), keep_text=(), workers=8):
+    def one(k):
+        lat, lon, the1, fi1 = sites[k]
+        txt = pyoracle.run_ref_cor(infile(lat, lon, the1, fi1, rig, rk, dele, time7, ext_lines=ext_lines), args,
+                                   parallel=False)
+        idx, cut, rows = parse_cor_output(txt, rig, dele)
+        rec = {"lat": lat, "lon": lon, "the1": the1, "fi1": fi1, "allowed": idx, "cutoff": cut}
+        if k in keep_text:
+            rec["text"] = txt
+        return rec
+    with ThreadPoolExecutor(max_workers=workers) as ex:
+        return list(ex.map(one, range(len(sites))))
+
+
+def make_scan0() -> dict:
+    sites = [(float(lat), float(lon), float(lat), float(lon)) for lat in range(-90, 91, 10) for lon in range(0, 331, 30)]
+    keep = {0, 57, 100, 131, 200}
+    recs = run_scan_set(sites, 0.05, 20.0, 0.05, [2020, 1, 1, 1, 0, 0, 0], ["-i", "igrf14"], keep_text=keep)
+    return {"config": "IGRF-14 at 2020-01-01, vertical, 20 km, 20 -> 0.05 GV by 0.05, nk1 100, tu 0.01, 25000 steps",
+            "rig": 0.05, "rk": 20.0, "del": 0.05, "time": [2020, 1, 1, 1, 0, 0, 0], "model": "igrf14",
+            "sites": recs}
+
+
+def make_scan_ext(kind: str) -> dict:
+    rng = np.random.default_rng(7 if kind == "t96" else 11)
+    lats = rng.choice(np.arange(-90, 91, 5), 10)
+    lons = rng.choice(np.arange(0, 360, 5), 10)
+    sites = [(float(a), float(o), float(a), float(o)) for a, o in zip(lats, lons)]
+    t7 = [2020, 6, 21, 173, 12, 0, 0]
+    if kind == "t96":
+        ext = ["-20 2 0 -1"]                              # Dst Pdyn By Bz (src/io.c:115-127)
+        args = ["-i", "igrf14", "-e", "t96"]
+        pm = [2.0, -20.0, 0.0, -1.0]
+    else:
+        ext = ["-20 2 0 -1", "1 1 1 1 1 1"]              # + W1..W6 (src/io.c:98-113)
+        args = ["-i", "igrf14", "-e", "ts05"]
+        pm = TS05_PARMOD
+    recs = run_scan_set(sites, 0.01, 20.0, 0.01, t7, args, ext_lines=ext, keep_text={0})
+    return {"config": f"IGRF-14 + {kind.upper()} at 2020-06-21 12 UT, vertical, 20 km, 20 -> 0.01 GV by 0.01",
+            "rig": 0.01, "rk": 20.0, "del": 0.01, "time": t7, "model": "igrf14", "external": kind,
+            "parmod": pm, "sites": recs}
+
+
+def main(sections):
+    lib = ref_lib()
+    todo = {
+        "setup": ("setup_params.json", lambda: make_setup(lib)),
+        "field": ("field_kats.json", lambda: make_field(lib)),
+        "scan0": ("scan_config0.json", make_scan0),
+        "scan_t96": ("scan_t96.json", lambda: make_scan_ext("t96")),
+        "scan_ts05": ("scan_ts05.json", lambda: make_scan_ext("ts05")),
+    }
+    for s in sections or list(todo):
+        fn, mk = todo[s]
+        data = mk()
+        with open(os.path.join(HERE, fn), "w") as f:
+            json.dump(data, f, separators=(",", ":"))
+        print(fn, os.path.getsize(os.path.join(HERE, fn)))
+
+
+if __name__ == "__main__":
+    main(sys.argv[1:])

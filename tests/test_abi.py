@@ -1,0 +1,68 @@
+"""CPU tests of the C ABI: the library loads, exports every function that
+include/cor_trace.h declares, and its host-only entry points behave."""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import re
+
+import numpy as np
+import pytest
+
+from conftest import ROOT
+import cortrace as ct
+
+
+def header_functions() -> list[str]:
+    names = []
+    for fn in sorted(os.listdir(os.path.join(ROOT, "include"))):
+        if fn.endswith(".h"):
+            txt = open(os.path.join(ROOT, "include", fn)).read()
+            txt = re.sub(r"/\*.*?\*/", "", txt, flags=re.S)
+            names += re.findall(r"^\s*(?:const\s+)?[\w\s\*]+?\b(cor_\w+)\s*\(", txt, flags=re.M)
+    return sorted(set(names))
+
+
+def test_library_exports_every_declared_function():
+    lib = ct.load()
+    declared = header_functions()
+    assert len(declared) >= 10
+    for name in declared:
+        assert hasattr(lib, name), name
+    assert set(ct.EXPORTS) <= set(declared)
+
+
+def test_abi_version():
+    assert ct.load().cor_abi_version() == 1
+
+
+def test_batch_count_matches_reference_grid():
+    # src/trajectory.c:7,12: i = 0 .. round((rk - rig)/del)
+    jobs = np.concatenate([ct.make_job(0, 0, rig=0.05, rk=20.0, dele=0.05),
+                           ct.make_job(0, 0, rig=0.01, rk=20.0, dele=0.01),
+                           ct.make_job(0, 0, rig=5.0, rk=5.0, dele=0.1)])
+    n, off = ct.batch_offsets(jobs)
+    assert off.tolist() == [0, 400, 2400, 2401] and n == 2401
+
+
+def test_batch_count_rejects_bad_grid():
+    with pytest.raises(ct.CorError):
+        ct.batch_offsets(ct.make_job(0, 0, dele=0.0))
+    with pytest.raises(ct.CorError):
+        ct.batch_offsets(ct.make_job(0, 0, rig=20.0, rk=0.05, dele=0.05))
+
+
+def test_prepare_trig_uses_host_libm():
+    j = ct.make_job(50.0, 15.0)
+    t = ct.prepare_trig(j)[0]
+    th = (90.0 - 50.0) * (ct.DEF_PI / 180.0)
+    assert t["st0"] == np.sin(th) and t["cp0"] == np.cos(15.0 * (ct.DEF_PI / 180.0))
+
+
+def test_context_without_gpu_reports_nodev():
+    import torch
+    if torch.cuda.is_available():
+        pytest.skip("a GPU is present")
+    lib = ct.load()
+    h = C.c_void_p()
+    assert lib.cor_ctx_create(0, C.byref(h)) == -5

@@ -1,0 +1,92 @@
+"""CPU tests: the oracle (CPU restatement) and the product's host set-up,
+pinned against golden fixtures made by the reference itself."""
+from __future__ import annotations
+
+import numpy as np
+import pytest
+
+from conftest import golden, unhex
+import cortrace as ct
+import pyoracle
+
+
+def test_setup_matches_reference_bit_for_bit():
+    """cor_internal_setup == internal_recalc for every model family and epoch kind."""
+    for case in golden("setup_params.json")["cases"]:
+        p = ct.internal_setup(case["version"], case["time"])
+        for k in ("g", "h", "rec", "a1", "a2", "a3"):
+            want = unhex(case[k])
+            got = p[k][0].ravel()
+            assert np.array_equal(got.view(np.uint64), want.view(np.uint64)), (case["version"], case["time"], k)
+
+
+def test_setup_rejects_out_of_range_and_unknown():
+    with pytest.raises(ct.CorError):
+        ct.internal_setup("igrf14", [2031, 1, 1, 1, 0, 0, 0])
+    with pytest.raises(ct.CorError):
+        ct.internal_setup("igrf99", [2020, 1, 1, 1, 0, 0, 0])
+    with pytest.raises(ct.CorError):
+        ct.internal_setup("hist", [2000, 1, 1, 1, 0, 0, 0])   # year >= max_year without extrapolation
+
+
+def test_oracle_internal_geo_bit_exact():
+    g = golden("field_kats.json")["internal_geo"]
+    p = ct.internal_setup(g["version"], g["time"])
+    pts = unhex(g["points"]).reshape(-1, 3)
+    want = unhex(g["b"]).reshape(-1, 3)
+    got = pyoracle.internal_geo(pts, p)
+    assert np.array_equal(got.view(np.uint64), want.view(np.uint64))
+
+
+def test_oracle_calculate_field_igrf_bit_exact():
+    g = golden("field_kats.json")["calculate_field"]
+    p = ct.internal_setup("igrf14", g["time"])
+    pts = unhex(g["points_m"]).reshape(-1, 3)
+    want = unhex(g["cases"]["igrf14"]["b"]).reshape(-1, 3)
+    got = pyoracle.calculate_field(pts, p)
+    assert np.array_equal(got.view(np.uint64), want.view(np.uint64))
+
+
+def test_oracle_chaos_bit_exact():
+    g = golden("field_kats.json")["chaos_geo"]
+    pts = unhex(g["points"]).reshape(-1, 3)
+    want = unhex(g["b"]).reshape(-1, 3)
+    G, H, nmax = ct.chaos_dense()
+    lib = pyoracle.load()
+    b = np.zeros(3)
+    for i, (x, y, z) in enumerate(pts):
+        lib.orc_chaos_geo(x, y, z, G.ctypes.data, H.ctypes.data, nmax, b[0:].ctypes.data, b[1:].ctypes.data,
+                          b[2:].ctypes.data)
+        assert np.array_equal(b.view(np.uint64), want[i].view(np.uint64)), i
+
+
+def config0_jobs(sites, rig=0.05, rk=20.0, dele=0.05):
+    jobs = np.concatenate([ct.make_job(s["lat"], s["lon"], rig=rig, rk=rk, dele=dele, the1=s["the1"], fi1=s["fi1"])
+                           for s in sites])
+    return jobs
+
+
+def fmt5(x: float) -> str:
+    return f"{x:12.5f}".strip()
+
+
+def test_oracle_scan_matches_reference_config0_subset():
+    """Allowed/forbidden flags and P(S)/P(C)/P(M) identical on 12 config-0 sites."""
+    g = golden("scan_config0.json")
+    sites = g["sites"][::19]
+    p = ct.internal_setup(g["model"], g["time"])
+    jobs = config0_jobs(sites, g["rig"], g["rk"], g["del"])
+    res = pyoracle.scan_batch(jobs, p, threads=8)
+    for j, s in enumerate(sites):
+        st = res.status[res.offsets[j]:res.offsets[j + 1]]
+        allowed = np.nonzero(st == ct.TRAJ_ALLOWED)[0].tolist()
+        assert allowed == s["allowed"], (s["lat"], s["lon"])
+        site = res.sites[j]
+        assert [fmt5(site["r_lower"]), fmt5(site["r_upper"]), fmt5(site["r_cutoff"])] == s["cutoff"]
+
+
+def test_oracle_flop_model():
+    """The op-count model of the SH field follows the degree truncation."""
+    assert pyoracle.internal_geo_flops(1.5) > pyoracle.internal_geo_flops(2.5) > pyoracle.internal_geo_flops(20.0)
+    # K = 14 at R < 2: 105 (n,m) terms, 14 of them with m = 1
+    assert pyoracle.internal_geo_flops(1.0) == 12 + 28 + 13 + 14 * 4 + 13 * 8 + 14 * 17 + (105 - 14) * 23
