@@ -79,7 +79,7 @@ class BatchResult(C.Structure):
 # Every symbol the header declares (checked by the CPU test suite).
 EXPORTS = [
     "cor_ctx_create", "cor_ctx_destroy", "cor_last_error_string", "cor_abi_version", "cor_batch_count",
-    "cor_prepare_trig", "cor_trace_batch", "cor_trace_batch_device", "cor_field_batch",
+    "cor_prepare_trig", "cor_trace_batch", "cor_trace_batch_device", "cor_upload_params", "cor_field_batch",
     "cor_internal_setup", "cor_gsm_setup",
 ]
 
@@ -103,8 +103,9 @@ def load(path: str = LIB_PATH) -> C.CDLL:
     lib.cor_batch_count.argtypes = [vp, i32, C.POINTER(u64), vp]
     lib.cor_prepare_trig.argtypes = [vp, i32, vp]
     lib.cor_trace_batch.argtypes = [vp, C.POINTER(BatchReq), C.POINTER(BatchResult)]
-    lib.cor_trace_batch_device.argtypes = [vp, vp, vp, i32, vp, u64, vp, i32, ModelSet, u64, dbl, dbl,
-                                           vp, vp, vp, vp, vp]
+    lib.cor_trace_batch_device.argtypes = [vp, vp, vp, i32, vp, u64, ModelSet, u64, dbl, dbl,
+                                           vp, vp, vp, vp, C.c_uint32, vp]
+    lib.cor_upload_params.argtypes = [vp, vp, i32]
     lib.cor_field_batch.argtypes = [vp, ModelSet, vp, i32, vp, vp, i64, vp]
     lib.cor_internal_setup.argtypes = [C.c_char_p, vp, vp]
     lib.cor_gsm_setup.argtypes = [vp, vp]

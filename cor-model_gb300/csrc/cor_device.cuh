@@ -29,6 +29,34 @@ struct Vec3 {
     double x, y, z;
 };
 
+// Correctly rounded x / c for a constant c, given rc = RN(1/c).  q0 = RN(x*rc)
+// is within one ulp of x/c, so r = x - q0*c is exact in one FMA, and
+// RN(q0 + r*rc) is the correctly rounded quotient (Markstein's theorem for
+// a correctly rounded reciprocal and a faithful first quotient).  Three FP64
+// operations instead of a full division; the result equals x / c bit for bit
+// (checked for every constant used here in the test suite).
+__device__ __forceinline__ double div_c(const double x, const double c, const double rc) {
+    const double q0 = __dmul_rn(x, rc);
+    const double r = __fma_rn(-q0, c, x);
+    return __fma_rn(r, rc, q0);
+}
+#define DIV3(x) ::cor::div_c((x), 3., 1. / 3.)
+#define DIV25(x) ::cor::div_c((x), 25., 1. / 25.)
+#define DIV81(x) ::cor::div_c((x), 81., 1. / 81.)
+#define DIV75(x) ::cor::div_c((x), 75., 1. / 75.)
+#define DIV192(x) ::cor::div_c((x), 192., 1. / 192.)
+#define DIV4(x) ((x)*0.25)  // exact: 0.25 is a power of two
+#define DIVRE(x) ::cor::div_c((x), ::cor::kRe, 1. / ::cor::kRe)
+
+// Correctly rounded x / b given the correctly rounded reciprocal rb = 1/b of
+// a run-time divisor (same theorem as div_c), for several quotients that
+// share one divisor.
+__device__ __forceinline__ double div_r(const double x, const double b, const double rb) {
+    const double q0 = __dmul_rn(x, rb);
+    const double r = __fma_rn(-q0, b, x);
+    return __fma_rn(r, rb, q0);
+}
+
 // geo_to_gsm, src/utils.c:75-87 (rows of A).
 __device__ __forceinline__ Vec3 geo_to_gsm(const Vec3 g, const cor_model_params* __restrict__ p) {
     Vec3 s;
@@ -54,9 +82,10 @@ __device__ __forceinline__ Vec3 gsm_to_geo(const Vec3 s, const cor_model_params*
 __device__ __forceinline__ Vec3 internal_geo(const Vec3 x, const cor_model_params* __restrict__ p) {
     const double rho2 = x.x * x.x + x.y * x.y;
     const double R = sqrt(rho2 + x.z * x.z);
-    const double C = x.z / R;
+    const double pp = 1. / R;
+    const double C = div_r(x.z, R, pp);
     const double rho = sqrt(rho2);
-    const double S = rho / R;
+    const double S = div_r(rho, R, pp);
     const bool pole = S < 1.E-5;
     double cf, sf;
     if (pole) {
@@ -66,7 +95,6 @@ __device__ __forceinline__ Vec3 internal_geo(const Vec3 x, const cor_model_param
         cf = x.x / rho;
         sf = x.y / rho;
     }
-    const double pp = 1. / R;
     int nm = 3 + 30 / ((int)R + 2);
     if (nm > 13) nm = 13;
     const int K = nm + 1;
@@ -150,31 +178,31 @@ __device__ __forceinline__ Vec3 rk_velocity(const double h, const double d, cons
 #define CY(X, Z) (h * (d * ((Z)*f.x - (X)*f.z)))
 #define CZ(X, Y) (h * (d * ((X)*f.y - (Y)*f.x)))
     const double a1 = CX(v.y, v.z), b1 = CY(v.x, v.z), c1 = CZ(v.x, v.y);
-    const double sx2 = v.x + a1 / 3., sy2 = v.y + b1 / 3., sz2 = v.z + c1 / 3.;
+    const double sx2 = v.x + DIV3(a1), sy2 = v.y + DIV3(b1), sz2 = v.z + DIV3(c1);
     const double a2 = CX(sy2, sz2), b2 = CY(sx2, sz2), c2 = CZ(sx2, sy2);
-    const double sx3 = v.x + (4. * a1 + 6. * a2) / 25.;
-    const double sy3 = v.y + (4. * b1 + 6. * b2) / 25.;
-    const double sz3 = v.z + (4. * c1 + 6. * c2) / 25.;
+    const double sx3 = v.x + DIV25(4. * a1 + 6. * a2);
+    const double sy3 = v.y + DIV25(4. * b1 + 6. * b2);
+    const double sz3 = v.z + DIV25(4. * c1 + 6. * c2);
     const double a3 = CX(sy3, sz3), b3 = CY(sx3, sz3), c3 = CZ(sx3, sy3);
-    const double sx4 = v.x + (a1 - 12. * a2 + 15. * a3) / 4.;
-    const double sy4 = v.y + (b1 - 12. * b2 + 15. * b3) / 4.;
-    const double sz4 = v.z + (c1 - 12. * c2 + 15. * c3) / 4.;
+    const double sx4 = v.x + DIV4(a1 - 12. * a2 + 15. * a3);
+    const double sy4 = v.y + DIV4(b1 - 12. * b2 + 15. * b3);
+    const double sz4 = v.z + DIV4(c1 - 12. * c2 + 15. * c3);
     const double a4 = CX(sy4, sz4), b4 = CY(sx4, sz4), c4 = CZ(sx4, sy4);
-    const double sx5 = v.x + (6. * a1 + 90. * a2 - 50. * a3 + 8. * a4) / 81.;
-    const double sy5 = v.y + (6. * b1 + 90. * b2 - 50. * b3 + 8. * b4) / 81.;
-    const double sz5 = v.z + (6. * c1 + 90. * c2 - 50. * c3 + 8. * c4) / 81.;
+    const double sx5 = v.x + DIV81(6. * a1 + 90. * a2 - 50. * a3 + 8. * a4);
+    const double sy5 = v.y + DIV81(6. * b1 + 90. * b2 - 50. * b3 + 8. * b4);
+    const double sz5 = v.z + DIV81(6. * c1 + 90. * c2 - 50. * c3 + 8. * c4);
     const double a5 = CX(sy5, sz5), b5 = CY(sx5, sz5), c5 = CZ(sx5, sy5);
-    const double sx6 = v.x + (6. * a1 + 36. * a2 + 10. * a3 + 8. * a4) / 75.;
-    const double sy6 = v.y + (6. * b1 + 36. * b2 + 10. * b3 + 8. * b4) / 75.;
-    const double sz6 = v.z + (6. * c1 + 36. * c2 + 10. * c3 + 8. * c4) / 75.;
+    const double sx6 = v.x + DIV75(6. * a1 + 36. * a2 + 10. * a3 + 8. * a4);
+    const double sy6 = v.y + DIV75(6. * b1 + 36. * b2 + 10. * b3 + 8. * b4);
+    const double sz6 = v.z + DIV75(6. * c1 + 36. * c2 + 10. * c3 + 8. * c4);
     const double a6 = CX(sy6, sz6), b6 = CY(sx6, sz6), c6 = CZ(sx6, sy6);
 #undef CX
 #undef CY
 #undef CZ
     Vec3 o;
-    o.x = v.x + (23. * a1 + 125. * a3 - 81. * a5 + 125. * a6) / 192.;
-    o.y = v.y + (23. * b1 + 125. * b3 - 81. * b5 + 125. * b6) / 192.;
-    o.z = v.z + (23. * c1 + 125. * c3 - 81. * c5 + 125. * c6) / 192.;
+    o.x = v.x + DIV192(23. * a1 + 125. * a3 - 81. * a5 + 125. * a6);
+    o.y = v.y + DIV192(23. * b1 + 125. * b3 - 81. * b5 + 125. * b6);
+    o.z = v.z + DIV192(23. * c1 + 125. * c3 - 81. * c5 + 125. * c6);
     return o;
 }
 
@@ -182,12 +210,12 @@ __device__ __forceinline__ Vec3 rk_velocity(const double h, const double d, cons
 // :353-355): the same tableau on h*v with the unrotated velocity.
 __device__ __forceinline__ double rk_position_1(const double h, const double vc, const double xc) {
     const double k1 = h * vc;
-    const double k2 = h * (vc + k1 / 3.);
-    const double k3 = h * (vc + (4. * k1 + 6. * k2) / 25.);
-    const double k4 = h * (vc + (k1 - 12. * k2 + 15. * k3) / 4.);
-    const double k5 = h * (vc + (6. * k1 + 90. * k2 - 50. * k3 + 8. * k4) / 81.);
-    const double k6 = h * (vc + (6. * k1 + 36. * k2 + 10. * k3 + 8. * k4) / 75.);
-    return xc + (23. * k1 + 125. * k3 - 81. * k5 + 125. * k6) / 192.;
+    const double k2 = h * (vc + DIV3(k1));
+    const double k3 = h * (vc + DIV25(4. * k1 + 6. * k2));
+    const double k4 = h * (vc + DIV4(k1 - 12. * k2 + 15. * k3));
+    const double k5 = h * (vc + DIV81(6. * k1 + 90. * k2 - 50. * k3 + 8. * k4));
+    const double k6 = h * (vc + DIV75(6. * k1 + 36. * k2 + 10. * k3 + 8. * k4));
+    return xc + DIV192(23. * k1 + 125. * k3 - 81. * k5 + 125. * k6);
 }
 
 __device__ __forceinline__ Vec3 rk_position(const double h, const Vec3 v, const Vec3 x) {

@@ -3,6 +3,7 @@
 #pragma once
 
 #include "cor_device.cuh"
+#include "t96.cuh"
 
 namespace cor {
 
@@ -16,6 +17,13 @@ struct ModelSet {
     static constexpr int crustal = CRUSTAL;
 };
 
+// Device copy of one parameter block: the ABI block (ModelsParams) plus the
+// per-condition constants of the external models, derived on the host.
+struct DevParams {
+    cor_model_params p;
+    T96Cond t96;
+};
+
 // Device tables of the crustal model (packed lower triangle) and its
 // per-degree recursion factors; set by the context before a crustal launch.
 struct CrustalTables {
@@ -24,15 +32,15 @@ struct CrustalTables {
     int nmax;
 };
 
-__device__ Vec3 t96_gsm(const double* __restrict__ parmod, const Vec3 x);
 __device__ Vec3 ts05_gsm(const double* __restrict__ parmod, const Vec3 x);
 __device__ Vec3 chaos_geo(const Vec3 x, const CrustalTables& t);
 
 // GSM position in metres -> GEO field in nT.
 template <class MS>
-__device__ __forceinline__ Vec3 calculate_field(const Vec3 gsm_pos, const cor_model_params* __restrict__ p,
+__device__ __forceinline__ Vec3 calculate_field(const Vec3 gsm_pos, const DevParams* __restrict__ dp,
                                                 const CrustalTables& crust) {
-    const Vec3 pos = {gsm_pos.x / kRe, gsm_pos.y / kRe, gsm_pos.z / kRe};
+    const cor_model_params* __restrict__ p = &dp->p;
+    const Vec3 pos = {DIVRE(gsm_pos.x), DIVRE(gsm_pos.y), DIVRE(gsm_pos.z)};
     Vec3 tot = {0., 0., 0.};
     if (MS::internal) {
         // internal_calc, src/models.c:146-160
@@ -44,7 +52,7 @@ __device__ __forceinline__ Vec3 calculate_field(const Vec3 gsm_pos, const cor_mo
         tot.z += bs.z;
     }
     if (MS::external == COR_EXTERNAL_T96) {
-        const Vec3 b = t96_gsm(p->parmod, pos);  // t96_calc, src/models.c:171-177
+        const Vec3 b = t96_field(dp->t96, pos);  // t96_calc, src/models.c:171-177
         tot.x += b.x;
         tot.y += b.y;
         tot.z += b.z;

@@ -1,0 +1,1000 @@
+// t96.cuh -- the zero-tilt T96 external field on the device (t96_gsm,
+// lib/t96/t96.c:4-1656; Tsyganenko 1996 with its fitted constants).
+//
+// Same terms and expression order as the reference, with the work that does
+// not depend on the position taken out of the per-call path:
+//   * quantities that depend only on PARMOD (the IMF angle and its sin/cos,
+//     pow(Pdyn/2, 0.14), the mode amplitudes, ...) come from T96Cond, filled on
+//     the host with the C library, so they equal the reference's values;
+//   * square roots of constant expressions and sin/cos of the fixed loop tilts
+//     come from the T96Tables block in constant memory, also host-computed;
+//   * sin/cos of the same argument are taken once (the reference recomputes
+//     some of them per mode), and divisions by literal constants use div_c.
+// Transcendentals are CUDA's FP64 exp/log/sin/cos/atan/asin/pow, so results
+// differ from the C library's by a few ulp; small integer powers (pow(x, m)
+// for m <= 5 in condip1 and r2sheet) are multiplication chains.
+#pragma once
+
+#include "cor_device.cuh"
+
+namespace cor {
+
+// Per-condition quantities of t96_gsm that depend on PARMOD only (:5-31, :52-58).
+struct T96Cond {
+    double ct, st;            // cos/sin of the IMF clock angle
+    double kimfy, kimfz;      // 0.7850*ByIMF, 0.7850*BzIMF
+    double xappa, xappa3;     // (Pdyn/2)^0.14 and its cube
+    double am, c548;          // 70/xappa, 5.48/xappa
+    double asq, four_asq, two_asq, r_two_asq;
+    double rcampl, tampl2, tampl3, b1ampl, b2ampl, rimfampl;
+};
+
+// Position-independent constants of the T96 terms (host-computed once).
+struct T96Tables {
+    double shl_sq[3][9];   // sqrt(1/P^2 + 1/R^2) of the ARC, ATAIL2, ATAIL3 shields
+    double b1s_sq[16];     // birk1shld sqrt(RPI^2 + RRK^2)
+    double b2s_sq[4];      // birk2shl sqrt(1/AI^2 + 1/AK^2)
+    double ic_sq[9];       // intercon sqrt(RP^2 + RR^2)
+    double cross_cs[4][2]; // cos/sin of the crossed-loop tilts (diploop1, r2outer x3)
+    double loop_cs[2][4];  // sin/cos of theta, phi of loops4 (r2inner, r2outer)
+    double r2s_k[8];       // r2sheet sqrt(-2e * -a) factors (5) and pow(d, 4) (3)
+};
+
+__constant__ T96Tables c_t96;
+
+// ---- shield amplitude/scale tables (:273-321, :1030-1263) ----------------
+// 3x3 shields: per table {P[3], R[3], amp[9] = A[2j] + A[2j+1]}.
+#define SHL_P0 12.75434981, 11.37659788, 636.4346279
+#define SHL_P1 5.187666221, 6.802472048, 39.13543412
+#define SHL_P2 19.69877970, 20.30095680, 86.45407420
+#define SHL_R0 1.752483754, 3.604231143, 12.83078674
+#define SHL_R1 2.784722096, 6.979576616, 25.71716760
+#define SHL_R2 22.50403727, 23.41617329, 48.48140573
+#define RECIP3(a, b, c) 1.0 / (a), 1.0 / (b), 1.0 / (c)
+#define RECIP3_(...) RECIP3(__VA_ARGS__)
+__constant__ double c_shl_p[3][3] = {{SHL_P0}, {SHL_P1}, {SHL_P2}};
+__constant__ double c_shl_rp[3][3] = {{RECIP3_(SHL_P0)}, {RECIP3_(SHL_P1)}, {RECIP3_(SHL_P2)}};
+__constant__ double c_shl_r[3][3] = {{SHL_R0}, {SHL_R1}, {SHL_R2}};
+__constant__ double c_shl_rr[3][3] = {{RECIP3_(SHL_R0)}, {RECIP3_(SHL_R1)}, {RECIP3_(SHL_R2)}};
+__constant__ double c_shl_a[3][18] = {
+    {-3.087699646, 3.516259114, 18.81380577, -13.95772338, -5.497076303, 0.1712890838, 2.392629189, -2.728020808,
+     -14.79349936, 11.08738083, 4.388174084, 0.2492163197E-01, 0.7030375685, -.7966023165, -3.835041334, 2.642228681,
+     -0.2405352424, -0.7297705678},
+    {0.8747515218, -0.9116821411, 2.209365387, -2.159059518, -7.059828867, 5.924671028, -1.916935691, 1.996707344,
+     -3.877101873, 3.947666061, 11.38715899, -8.343210833, 1.194109867, -1.244316975, 3.73895491, -4.406522465,
+     -20.66884863, 3.020952989},
+    {-19091.95061, -3011.613928, 20582.16203, 4242.918430, -2377.091102, -1504.820043, 19884.04650, 2725.150544,
+     -21389.04845, -3990.475093, 2401.610097, 1548.171792, -946.5493963, 490.1528941, 986.9156625, -489.3265930,
+     -67.99278499, 8.711175710}};
+
+__device__ __forceinline__ double bes_poly0(double x32) {
+    return 1.0 - x32 * (2.2499997 - x32 * (1.2656208 - x32 * (0.3163866 - x32 * (0.0444479 - x32 * (0.0039444 - x32 * 0.00021)))));
+}
+
+// J0 and J1 polynomial/asymptotic approximations (bes0/bes1, :211-234),
+// computed together: they share x/3 or 3/x and sqrt(x).
+__device__ __forceinline__ void t96_bes01(const double x, double& j0, double& j1) {
+    if (fabs(x) < 3.0) {
+        const double x3 = DIV3(x);
+        const double x32 = x3 * x3;
+        j0 = bes_poly0(x32);
+        const double b = 0.5 - x32 * (0.56249985 - x32 * (0.21093573 - x32 * (0.03954289 - x32 * (0.00443319 - x32 * (0.00031761 - x32 * 0.00001109)))));
+        j1 = b * x;
+        return;
+    }
+    const double xd3 = 3.0 / x;
+    const double sx = sqrt(x);
+    const double f0 = 0.79788456 - xd3 * (0.00000077 + xd3 * (0.00552740 + xd3 * (0.00009512 - xd3 * (0.00137237 - xd3 * (0.00072805 - xd3 * 0.00014476)))));
+    const double t0 = x - 0.78539816 - xd3 * (0.04166397 + xd3 * (0.00003954 - xd3 * (0.00262573 - xd3 * (0.00054125 + xd3 * (0.00029333 - xd3 * 0.00013558)))));
+    const double f1 = 0.79788456 + xd3 * (0.00000156 + xd3 * (0.01659667 + xd3 * (0.00017105 - xd3 * (0.00249511 - xd3 * (0.00113653 - xd3 * 0.00020033)))));
+    const double t1 = x - 2.35619449 + xd3 * (0.12499612 + xd3 * (0.0000565 - xd3 * (0.00637879 - xd3 * (0.00074348 + xd3 * (0.00079824 - xd3 * 0.00029166)))));
+    j0 = f0 / sx * cos(t0);
+    j1 = f1 / sx * cos(t1);
+}
+
+// cylharm, :113-163
+__device__ __forceinline__ Vec3 t96_cylharm(const double x, const double y, const double z) {
+    constexpr double A[12] = {0.24777, -27.003, -0.46815, 7.0637, -1.5918, -0.90317E-01,
+                              57.522, 13.757, 2.0100, 10.458, 4.5798, 2.1695};
+    double rho = sqrt(y * y + z * z), sf, cf;
+    if (rho < 1.0e-8) {
+        sf = 1.0;
+        cf = 0.0;
+        rho = 1.0e-8;
+    } else {
+        const double rr = 1.0 / rho;
+        sf = div_r(z, rho, rr);
+        cf = div_r(y, rho, rr);
+    }
+    const double sf2 = sf * sf;
+    const double s2c2 = sf2 - cf * cf;
+    double bx = 0.0, by = 0.0, bz = 0.0;
+#pragma unroll
+    for (int i = 0; i < 3; ++i) {
+        const double dz = div_c(rho, A[i + 6], 1.0 / A[i + 6]);
+        double j0, j1;
+        t96_bes01(dz, j0, j1);
+        const double e = exp(div_c(x, A[i + 6], 1.0 / A[i + 6]));
+        const double j1dz = j1 / dz;
+        bx -= A[i] * j1 * e * sf;
+        by += A[i] * (2.0 * j1 / dz - j0) * e * sf * cf;
+        bz += A[i] * (j1dz * s2c2 - j0 * sf2) * e;
+    }
+#pragma unroll
+    for (int i = 3; i < 6; ++i) {
+        const double dz = div_c(rho, A[i + 6], 1.0 / A[i + 6]);
+        const double xk = div_c(x, A[i + 6], 1.0 / A[i + 6]);
+        double j0, j1;
+        t96_bes01(dz, j0, j1);
+        const double e = exp(xk);
+        const double brho = (xk * j0 - (dz * dz + xk - 1.0) * j1 / dz) * e * sf;
+        const double bphi = (j0 + j1 / dz * (xk - 1.0)) * e * cf;
+        bx += A[i] * (dz * j0 + xk * j1) * e * sf;
+        by += A[i] * (brho * cf - bphi * sf);
+        bz += A[i] * (brho * sf + bphi * cf);
+    }
+    return {bx, by, bz};
+}
+
+// intercon, :236-271
+__device__ __forceinline__ Vec3 t96_intercon(const double x, const double y, const double z) {
+    constexpr double A[9] = {-8.411078731, 5932254.951, -9073284.93, -11.68794634, 6027598.824,
+                             -9218378.368, -6.508798398, -11824.42793, 18015.66212};
+    constexpr double RP[3] = {0.12503844191332988, 0.071597395204476152, 0.011080976889832743};
+    constexpr double RR[3] = {0.059675527522452816, 0.00098459526668325296, 0.00064371058922777988};
+    double sz[3], cz[3];
+#pragma unroll
+    for (int k = 0; k < 3; k++) sincos(z * RR[k], &sz[k], &cz[k]);
+    double bx = 0.0, by = 0.0, bz = 0.0;
+#pragma unroll
+    for (int i = 0; i < 3; i++) {
+        double sy, cy;
+        sincos(y * RP[i], &sy, &cy);
+#pragma unroll
+        for (int k = 0; k < 3; k++) {
+            const double sq = c_t96.ic_sq[3 * i + k];
+            const double e = exp(x * sq);
+            bx += A[3 * i + k] * (-sq * e * cy * sz[k]);
+            by += A[3 * i + k] * (RP[i] * e * sy * sz[k]);
+            bz += A[3 * i + k] * (-RR[k] * e * cy * cz[k]);
+        }
+    }
+    return {bx, by, bz};
+}
+
+// shlcar3x3_t96, :500-617, for shield table t (0 ARC, 1 ATAIL2, 2 ATAIL3)
+__device__ __forceinline__ Vec3 t96_shlcar3x3(const int t, const double x, const double y, const double z) {
+    double sz[3], cz[3];
+#pragma unroll
+    for (int k = 0; k < 3; k++) sincos(div_c(z, c_shl_r[t][k], c_shl_rr[t][k]), &sz[k], &cz[k]);
+    double hx = 0.0, hy = 0.0, hz = 0.0;
+#pragma unroll
+    for (int i = 0; i < 3; i++) {
+        const double p = c_shl_p[t][i], rp = c_shl_rp[t][i];
+        double sy, cy;
+        sincos(div_c(y, p, rp), &sy, &cy);
+#pragma unroll
+        for (int k = 0; k < 3; k++) {
+            const double sq = c_t96.shl_sq[t][3 * i + k];
+            const double e = exp(x * sq);
+            const double amp = c_shl_a[t][2 * (3 * i + k)] + c_shl_a[t][2 * (3 * i + k) + 1];
+            hx += (-sq * e * cy * sz[k]) * amp;
+            hy += (div_c(e, p, rp) * sy * sz[k]) * amp;
+            hz += (div_c(-e, c_shl_r[t][k], c_shl_rr[t][k]) * cy * cz[k]) * amp;
+        }
+    }
+    return {hx, hy, hz};
+}
+
+// ringcurr_96, :323-381
+__device__ __forceinline__ Vec3 t96_ringcurr(const double x, const double y, const double z) {
+    constexpr double F[2] = {569.895366, -1603.386993};
+    constexpr double BETA[2] = {2.722188, 3.766875};
+    const double dzs = sqrt(z * z + 4.0);
+    const double rhos = sqrt(x * x + y * y);
+    const double ddz = z / dzs;
+    double drx = 0.0, dry = (y >= 0) ? 1.0 : -1.0;
+    if (rhos >= 1.0e-5) {
+        const double rr = 1.0 / rhos;
+        drx = div_r(x, rhos, rr);
+        dry = div_r(y, rhos, rr);
+    }
+    double bx = 0.0, by = 0.0, bz = 0.0;
+#pragma unroll
+    for (int i = 0; i < 2; ++i) {
+        const double bi = BETA[i];
+        const double dzb = dzs + bi, rp = rhos + bi, rm = rhos - bi;
+        const double dzb2 = dzb * dzb;
+        const double bi2 = 2.0 * bi;
+        const double s1 = sqrt(dzb2 + rp * rp), s2 = sqrt(dzb2 + rm * rm);
+        const double r1 = 1.0 / s1, r2 = 1.0 / s2;
+        const double ds1dz = div_r(dzb, s1, r1), ds2dz = div_r(dzb, s2, r2);
+        const double ds1dr = div_r(rp, s1, r1), ds2dr = div_r(rm, s2, r2);
+        const double s12 = s1 * s2, sp = s1 + s2, sp2 = sp * sp;
+        const double fac1 = sqrt(sp2 - bi2 * bi2);
+        const double as = fac1 / (s12 * sp2);
+        const double term1 = 1.0 / (s12 * sp * fac1);
+        const double fac2 = as / sp2;
+        const double das1 = term1 - div_r(fac2, s1, r1) * (s2 * s2 + s1 * (3.0 * s1 + 4.0 * s2));
+        const double das2 = term1 - div_r(fac2, s2, r2) * (s1 * s1 + s2 * (3.0 * s2 + 4.0 * s1));
+        const double dasdx = das1 * (ds1dr * drx) + das2 * (ds2dr * drx);
+        const double dasdy = das1 * (ds1dr * dry) + das2 * (ds2dr * dry);
+        const double dasdz = das1 * (ds1dz * ddz) + das2 * (ds2dz * ddz);
+        bx += -F[i] * x * dasdz;
+        by -= F[i] * y * dasdz;
+        bz += F[i] * ((2.0 * as + y * dasdy) + x * dasdx);
+    }
+    return {bx, by, bz};
+}
+
+// taildisk_t96, :383-443
+__device__ __forceinline__ Vec3 t96_taildisk(const double x, const double y, const double z) {
+    constexpr double F[4] = {-745796.7338, 1176470.141, -444610.529, -57508.01028};
+    constexpr double BETA[4] = {7.9250000, 8.0850000, 8.4712500, 27.89500};
+    const double y20 = div_c(y, 20.0, 1.0 / 20.0);
+    const double d = 2.0 + 10.0 * (y20 * y20);
+    const double dzs = sqrt(z * z + d * d);
+    const double rdz = 1.0 / dzs;
+    const double ddy = div_r(d * 10.0 * y * 0.005, dzs, rdz);
+    const double ddz = div_r(z, dzs, rdz);
+    const double xs = x - 4.5;
+    const double rhos = sqrt(xs * xs + y * y);
+    double drx = 0.0, dry = (y >= 0) ? 1.0 : -1.0;
+    if (rhos >= 1.0e-5) {
+        const double rr = 1.0 / rhos;
+        drx = div_r(xs, rhos, rr);
+        dry = div_r(y, rhos, rr);
+    }
+    double bx = 0.0, by = 0.0, bz = 0.0;
+#pragma unroll
+    for (int i = 0; i < 4; ++i) {
+        const double bi = BETA[i];
+        const double bi1 = 2.0 * bi;
+        const double dzb = dzs + bi, rp = rhos + bi, rm = rhos - bi;
+        const double s1 = sqrt(dzb * dzb + rp * rp), s2 = sqrt(dzb * dzb + rm * rm);
+        const double r1 = 1.0 / s1, r2 = 1.0 / s2;
+        const double ds1dz = div_r(dzb, s1, r1), ds2dz = div_r(dzb, s2, r2);
+        const double ds1dr = div_r(rp, s1, r1), ds2dr = div_r(rm, s2, r2);
+        const double s12 = s1 * s2, sp = s1 + s2, sp2 = sp * sp;
+        const double fac1 = sqrt(sp2 - bi1 * bi1);
+        const double as = fac1 / (s12 * sp2);
+        const double term1 = 1.0 / (s12 * sp * fac1);
+        const double fac2 = as / sp2;
+        const double das1 = term1 - div_r(fac2, s1, r1) * (s2 * s2 + s1 * (3.0 * s1 + 4.0 * s2));
+        const double das2 = term1 - div_r(fac2, s2, r2) * (s1 * s1 + s2 * (3.0 * s2 + 4.0 * s1));
+        const double dasdx = das1 * (ds1dr * drx) + das2 * (ds2dr * drx);
+        const double dasdy = das1 * (ds1dz * ddy + ds1dr * dry) + das2 * (ds2dz * ddy + ds2dr * dry);
+        const double dasdz = das1 * (ds1dz * ddz) + das2 * (ds2dz * ddz);
+        bx += F[i] * ((4.5 - x) * dasdz);
+        by -= F[i] * y * dasdz;
+        bz += F[i] * ((2.0 * as + y * dasdy) + xs * dasdx);
+    }
+    return {bx, by, bz};
+}
+
+// tail87, :445-498: three line currents (z, z-40, z+40) with the same form.
+struct T87Line {
+    double s0, s1, s2, g1, g2, xln1;
+};
+
+__device__ __forceinline__ T87Line t96_tail87_line(const double b2, const double xnx, const double xnx2, const double xc1,
+                                                  const double xc12, const double xc2, const double xc22,
+                                                  const double xr2) {
+    T87Line o;
+    const double b = sqrt(b2);
+    const double xa1 = xc12 + b2;
+    const double xa2 = 1. / (xc22 + b2);
+    const double xna = xnx2 + b2;
+    const double f = b2 - xc22;
+    const double xln1 = log(76.37 / xna);
+    const double xln2 = xln1 + 0.13238005;
+    const double rb = 1. / b;
+    const double s0 = div_r(atan(div_r(xnx, b, rb)) + 1.5707963, b, rb);
+    const double rxa1 = 1. / xa1;
+    o.s0 = s0;
+    o.s1 = div_r(xln1 * .5 + xc1 * s0, xa1, rxa1);
+    o.s2 = (xc2 * xa2 * xln2 + 0.1071 - f * xa2 * s0) * xa2;
+    o.g1 = div_r(b2 * s0 - 0.5 * xc1 * xln1, xa1, rxa1);
+    o.g2 = ((0.5 * f * xln2 + 2. * s0 * b2 * xc2) * xa2 + xr2) * xa2;
+    o.xln1 = xln1;
+    return o;
+}
+
+__device__ __forceinline__ void t96_tail87(const double x, const double z, double& bxo, double& bzo) {
+    const double zp = z - 40.0, zm = z + 40.0;
+    const double xnx = -10.0 - x;
+    const double xnx2 = xnx * xnx;
+    const double xc1 = x + 1.261, xc2 = x + 0.663;
+    const double xc22 = xc2 * xc2;
+    const double xr2 = xc2 * -0.1071;
+    const double xc12 = xc1 * xc1;
+    const double d2 = 3.0 * 3.0;
+    const T87Line c = t96_tail87_line(z * z + d2, xnx, xnx2, xc1, xc12, xc2, xc22, xr2);
+    const T87Line p = t96_tail87_line(zp * zp + d2, xnx, xnx2, xc1, xc12, xc2, xc22, xr2);
+    const T87Line m = t96_tail87_line(zm * zm + d2, xnx, xnx2, xc1, xc12, xc2, xc22, xr2);
+    const double aln = 0.25 * (p.xln1 + m.xln1 - 2. * c.xln1);
+    bxo = 0.391734 * (z * c.s0 - 0.5 * (zp * p.s0 + zm * m.s0)) + 5.89715 * (z * c.s1 - 0.5 * (zp * p.s1 + zm * m.s1)) +
+          24.6833 * (z * c.s2 - 0.5 * (zp * p.s2 + zm * m.s2));
+    bzo = 0.391734 * aln + 5.89715 * (c.g1 - 0.5 * (p.g1 + m.g1)) + 24.6833 * (c.g2 - 0.5 * (p.g2 + m.g2));
+}
+
+// circle, :857-887
+__device__ __forceinline__ Vec3 t96_circle(const double x, const double y, const double z, const double rl) {
+    const double rho2 = x * x + y * y;
+    const double rho = sqrt(rho2);
+    const double rr = rho + rl;
+    const double r22 = z * z + rr * rr;
+    const double r2 = sqrt(r22);
+    const double r12 = r22 - 4.0 * rho * rl;
+    const double r32 = 0.5 * (r12 + r22);
+    const double xk2 = 1.0 - r12 / r22;
+    const double xk2s = 1.0 - xk2;
+    const double dl = log(1.0 / xk2s);
+    const double K = 1.38629436112 + xk2s * (0.09666344259 + xk2s * (0.03590092383 + xk2s * (0.03742563713 + xk2s * 0.01451196212))) +
+                     dl * (0.5 + xk2s * (0.12498593597 + xk2s * (0.06880248576 + xk2s * (0.03328355346 + xk2s * 0.00441787012))));
+    const double E = 1.0 + xk2s * (0.44325141463 + xk2s * (0.0626060122 + xk2s * (0.04757383546 + xk2s * 0.01736506451))) +
+                     dl * xk2s * (0.2499836831 + xk2s * (0.09200180037 + xk2s * (0.04069697526 + xk2s * 0.00526449639)));
+    const double r12r = 1.0 / r12;
+    double brho;
+    if (rho > 1e-6) brho = z / (rho2 * r2) * (div_r(r32, r12, r12r) * E - K);
+    else brho = div_r(3.141592654 * rl / r2 * (rl - rho), r12, r12r) * z / (r32 - rho2);
+    return {brho * x, brho * y, (K - div_r(E * (r32 - 2.0 * rl * rl), r12, r12r)) / r2};
+}
+
+// crosslp, :889-905, tilt index it into c_t96.cross_cs
+__device__ __forceinline__ Vec3 t96_crosslp(const double x, const double y, const double z, const double xc,
+                                           const double rl, const int it) {
+    const double cal = c_t96.cross_cs[it][0], sal = c_t96.cross_cs[it][1];
+    const double y1 = y * cal - z * sal, z1 = y * sal + z * cal;
+    const double y2 = y * cal + z * sal, z2 = -y * sal + z * cal;
+    const Vec3 b1 = t96_circle(x - xc, y1, z1, rl);
+    const Vec3 b2 = t96_circle(x - xc, y2, z2, rl);
+    return {b1.x + b2.x, (b1.y + b2.y) * cal + (b1.z - b2.z) * sal, -(b1.y - b2.y) * sal + (b1.z + b2.z) * cal};
+}
+
+// dipxyz, :909-928 -> the field of unit x, y and z dipoles
+struct Dip3 {
+    Vec3 dx, dy, dz;
+};
+
+__device__ __forceinline__ Dip3 t96_dipxyz(const double x, const double y, const double z) {
+    const double x2 = x * x, y2 = y * y, z2 = z * z;
+    const double r2 = x2 + y2 + z2;
+    const double xmr5 = 30574.0 / (r2 * r2 * sqrt(r2));
+    const double xmr53 = 3.0 * xmr5;
+    Dip3 o;
+    o.dx.x = xmr5 * (3.0 * x2 - r2);
+    o.dx.y = xmr53 * x * y;
+    o.dx.z = xmr53 * x * z;
+    o.dy.x = o.dx.y;
+    o.dy.y = xmr5 * (3.0 * y2 - r2);
+    o.dy.z = xmr53 * y * z;
+    o.dz.x = o.dx.z;
+    o.dz.y = o.dy.z;
+    o.dz.z = xmr5 * (3.0 * z2 - r2);
+    return o;
+}
+
+// Region-1 "dipole loops" basis contracted with its coefficients
+// (diploop1 :809-855 summed with C1 as in birk1tot_02 :702-707).
+__device__ __forceinline__ Vec3 t96_r1_loops(const double x, const double y, const double z) {
+    constexpr double XX[12] = {-11.0, -7.0, -7.0, -3.0, -3.0, 1.0, 1.0, 1.0, 5.0, 5.0, 9.0, 9.0};
+    constexpr double YY[12] = {2.0, 0.0, 4.0, 2.0, 6.0, 0.0, 4.0, 8.0, 2.0, 6.0, 0.0, 4.0};
+    constexpr double C1[14] = {-0.911582E-03, -0.376654E-02, -0.727423E-02, -0.270084E-02, -0.123899E-02,
+                               -0.154387E-02, -0.340040E-02, -0.191858E-01, -0.518979E-01, 0.635061E-01,
+                               0.440680, -0.396570, -89.5587, 23.2806};
+    const double z2 = z * z;
+    double bx = 0.0, by = 0.0, bz = 0.0;
+#pragma unroll
+    for (int i = 0; i < 12; i++) {
+        const double dy = YY[i] * 0.945719;
+        const double dx = XX[i] * 1.12541;
+        const double xd = x - dx;
+        double yd = y - dy;
+        double r2 = xd * xd + yd * yd + z2;
+        double xmr5 = 30574.0 / (r2 * r2 * sqrt(r2));
+        double xmr53 = 3.0 * xmr5;
+        const double b1x = xmr53 * xd * z, b1y = xmr53 * yd * z, b1z = xmr5 * (3.0 * z2 - r2);
+        double b2x = 0.0, b2y = 0.0, b2z = 0.0;
+        if (fabs(dy) > 1.0e-10) {
+            yd = y + dy;
+            r2 = xd * xd + yd * yd + z2;
+            xmr5 = 30574.0 / (r2 * r2 * sqrt(r2));
+            xmr53 = 3.0 * xmr5;
+            b2x = xmr53 * xd * z;
+            b2y = xmr53 * yd * z;
+            b2z = xmr5 * (3.0 * z2 - r2);
+        }
+        bx += C1[i] * (b1x + b2x);
+        by += C1[i] * (b1y + b2y);
+        bz += C1[i] * (b1z + b2z);
+    }
+    const Vec3 o = t96_crosslp(x, y, z, 2.28397, 1.86106, 0);
+    bx += C1[12] * o.x;
+    by += C1[12] * o.y;
+    bz += C1[12] * o.z;
+    const Vec3 c = t96_circle(x + 5.60831, y, z, 7.83281);
+    bx += C1[13] * c.x;
+    by += C1[13] * c.y;
+    bz += C1[13] * c.z;
+    return {bx, by, bz};
+}
+
+// Region-1 "conical harmonics + dipole pairs" basis contracted with C2
+// (condip1 :930-1028 summed as in birk1tot_02 :710-715).
+__device__ __forceinline__ Vec3 t96_r1_condip(const double x, const double y, const double z) {
+    constexpr double XX[9] = {-10.0, -7.0, -4.0, -4.0, 0.0, 4.0, 4.0, 7.0, 10.0};
+    constexpr double YY[9] = {3.0, 6.0, 3.0, 9.0, 6.0, 3.0, 9.0, 6.0, 3.0};
+    constexpr double ZZ[14] = {20.0, 20.0, 4.0, 20.0, 4.0, 4.0, 20.0, 20.0, 20.0, 2.0, 3.0, 4.50, 7.0, 10.0};
+    constexpr double C2[42] = {
+        6.04133, 0.305415, 0.606066E-02, 0.128379E-03, -0.179406E-04, 1.41714, -27.2586, -4.28833, -1.30675,
+        35.5607, 8.95792, 0.961617E-03, -0.801477E-03, -0.782795E-03, -1.65242, -16.5242, -5.33798,
+        0.424878E-03, 0.331787E-03, -0.704305E-03, 0.844342E-03, 0.953682E-04, 0.886271E-03, 25.1120,
+        20.9299, 5.14569, -44.1670, -51.0672, -1.87725, 20.2998, 48.7505, -2.97415, 0.174615E-03,
+        -0.789777E-06, 0.686047E-03, 0.460104E-04, -0.345216E-02, 0.221871E-02, 0.110078E-01,
+        -0.661373E-02, 0.249201E-02, 0.343978E-01};
+    const double xsm = x + 0.16;
+    const double ro2 = xsm * xsm + y * y;
+    const double ro = sqrt(ro2);
+    const double rro = 1.0 / ro;
+    double cf[5], sf[5];
+    cf[0] = div_r(xsm, ro, rro);
+    sf[0] = div_r(y, ro, rro);
+    cf[1] = cf[0] * cf[0] - sf[0] * sf[0];
+    sf[1] = 2.0 * sf[0] * cf[0];
+#pragma unroll
+    for (int m = 2; m < 5; m++) {
+        cf[m] = cf[m - 1] * cf[0] - sf[m - 1] * sf[0];
+        sf[m] = sf[m - 1] * cf[0] + cf[m - 1] * sf[0];
+    }
+    const double r2 = ro2 + z * z;
+    const double r = sqrt(r2);
+    const double rr = 1.0 / r;
+    const double c = div_r(z, r, rr), s = div_r(ro, r, rr);
+    const double ch = sqrt(0.5 * (1.0 + c)), sh = sqrt(0.5 * (1.0 - c));
+    const double tnh = sh / ch, cnh = 1.0 / tnh;
+    const double ch2 = ch * ch, sh2 = sh * sh;
+    const double rs = r * s;
+    double bx = 0.0, by = 0.0, bz = 0.0;
+    double tp = 1.0, cp = 1.0;  // tnh^m, cnh^m
+#pragma unroll
+    for (int m = 0; m < 5; m++) {
+        const double mn = m + 1;
+        const double tp1 = (m == 0) ? tnh : tp * tnh, cp1 = (m == 0) ? cnh : cp * cnh;
+        const double bt = mn * cf[m] / rs * (tp1 + cp1);
+        const double bf = div_r(-0.5 * mn * sf[m], r, rr) * (tp / ch2 - cp / sh2);
+        bx += C2[m] * (bt * c * cf[0] - bf * sf[0]);
+        by += C2[m] * (bt * c * sf[0] + bf * cf[0]);
+        bz += C2[m] * (-bt * s);
+        tp = tp1;
+        cp = cp1;
+    }
+#pragma unroll
+    for (int i = 0; i < 9; i++) {
+        const double f = (i == 2 || i == 4 || i == 5) ? 0.08 : 0.4;
+        const double xd = XX[i] * f, yd = YY[i] * f, zd = ZZ[i];
+        const Dip3 b1 = t96_dipxyz(x - xd, y - yd, z - zd);
+        const Dip3 b2 = t96_dipxyz(x - xd, y + yd, z - zd);
+        const Dip3 b3 = t96_dipxyz(x - xd, y - yd, z + zd);
+        const Dip3 b4 = t96_dipxyz(x - xd, y + yd, z + zd);
+        const int ix = (i + 1) * 3 + 2, iy = ix + 1, iz = iy + 1;
+        bx += C2[ix] * (b1.dx.x + b2.dx.x - b3.dx.x - b4.dx.x);
+        by += C2[ix] * (b1.dx.y + b2.dx.y - b3.dx.y - b4.dx.y);
+        bz += C2[ix] * (b1.dx.z + b2.dx.z - b3.dx.z - b4.dx.z);
+        bx += C2[iy] * (b1.dy.x - b2.dy.x - b3.dy.x + b4.dy.x);
+        by += C2[iy] * (b1.dy.y - b2.dy.y - b3.dy.y + b4.dy.y);
+        bz += C2[iy] * (b1.dy.z - b2.dy.z - b3.dy.z + b4.dy.z);
+        bx += C2[iz] * (b1.dz.x + b2.dz.x + b3.dz.x + b4.dz.x);
+        by += C2[iz] * (b1.dz.y + b2.dz.y + b3.dz.y + b4.dz.y);
+        bz += C2[iz] * (b1.dz.z + b2.dz.z + b3.dz.z + b4.dz.z);
+    }
+#pragma unroll
+    for (int i = 1; i <= 5; i++) {
+        const double zd = ZZ[i + 8];
+        const Dip3 b1 = t96_dipxyz(x, y, z - zd);
+        const Dip3 b2 = t96_dipxyz(x, y, z + zd);
+        const int ix = 30 + i * 2, iz = ix + 1;
+        bx += C2[ix] * (b1.dx.x - b2.dx.x);
+        by += C2[ix] * (b1.dx.y - b2.dx.y);
+        bz += C2[ix] * (b1.dx.z - b2.dx.z);
+        bx += C2[iz] * (b1.dz.x + b2.dz.x);
+        by += C2[iz] * (b1.dz.y + b2.dz.y);
+        bz += C2[iz] * (b1.dz.z + b2.dz.z);
+    }
+    return {bx, by, bz};
+}
+
+// birk1shld, :1030-1194
+__device__ __forceinline__ Vec3 t96_birk1shld(const double x, const double y, const double z) {
+    constexpr double RPI[4] = {1.0 / 5.303648988, 1.0 / 10.40368955, 1.0 / 69.65230348, 1.0 / 466.5099509};
+    constexpr double RK[4] = {1.0 / 1.645049286, 1.0 / 3.825838190, 1.0 / 11.66675599, 1.0 / 558.9781177};
+    constexpr double AA[16] = {
+        1.174198045 + -1.463820502, 4.840161537 + -3.674506864, 82.18368896 + -94.94071588, -4122.331796 + 4670.278676,
+        -21.54975037 + 26.72661293, -72.81365728 + 44.09887902, 40.08073706 + -51.23563510, 1955.348537 + -1940.971550,
+        794.0496433 + -982.2441344, 1889.837171 + -558.9779727, -1260.543238 + 1260.063802, -293.5942373 + 344.7250789,
+        -773.7002492 + 957.0094135, -1824.143669 + 520.7994379, 1192.484774 + -1192.184565, 89.15537624 + -98.52042999};
+    double szk[4], czk[4];
+#pragma unroll
+    for (int k = 0; k < 4; k++) sincos(z * RK[k], &szk[k], &czk[k]);
+    double bx = 0.0, by = 0.0, bz = 0.0;
+#pragma unroll
+    for (int i = 0; i < 4; i++) {
+        double sy, cy;
+        sincos(RPI[i] * y, &sy, &cy);
+#pragma unroll
+        for (int k = 0; k < 4; k++) {
+            const double sq = c_t96.b1s_sq[4 * i + k];
+            const double e = exp(x * sq);
+            bx += (-sq * e * cy * szk[k]) * AA[4 * i + k];
+            by += (RPI[i] * e * sy * szk[k]) * AA[4 * i + k];
+            bz += (-RK[k] * e * cy * czk[k]) * AA[4 * i + k];
+        }
+    }
+    return {bx, by, bz};
+}
+
+// birk1tot_02 (:619-807): the Region-1 field with its blend zones and shield.
+__device__ __forceinline__ Vec3 t96_birk1_blend(const double x, const double y, const double z, const double r,
+                                               const double r3, const double cpas, const double spas, const double t1,
+                                               const double t2, const bool south) {
+    const double sqr = sqrt(r);
+    const double s1 = sin(t1);
+    const double st01 = sqr / pow(r3 + 1.0 / (s1 * s1 * s1 * s1 * s1 * s1) - 1.0, 0.1666666667);
+    const double s2 = sin(t2);
+    const double st02 = sqr / pow(r3 + 1.0 / (s2 * s2 * s2 * s2 * s2 * s2) - 1.0, 0.1666666667);
+    double ct01 = sqrt(1.0 - st01 * st01), ct02 = sqrt(1.0 - st02 * st02);
+    if (south) {
+        ct01 = -ct01;
+        ct02 = -ct02;
+    }
+    const double x1 = r * st01 * cpas, y1 = r * st01 * spas, z1 = r * ct01;
+    const double x2 = r * st02 * cpas, y2 = r * st02 * spas, z2 = r * ct02;
+    const Vec3 b1 = south ? t96_r1_condip(x1, y1, z1) : t96_r1_loops(x1, y1, z1);
+    const Vec3 b2 = south ? t96_r1_loops(x2, y2, z2) : t96_r1_condip(x2, y2, z2);
+    const double dx2 = x2 - x1, dy2 = y2 - y1, dz2 = z2 - z1;
+    const double ss = sqrt(dx2 * dx2 + dy2 * dy2 + dz2 * dz2);
+    const double dx = x - x1, dy = y - y1, dz = z - z1;
+    const double ds = sqrt(dx * dx + dy * dy + dz * dz);
+    const double frac = ds / ss;
+    return {b1.x * (1.0 - frac) + b2.x * frac, b1.y * (1.0 - frac) + b2.y * frac, b1.z * (1.0 - frac) + b2.z * frac};
+}
+
+__device__ __forceinline__ Vec3 t96_birk1tot(const double x, const double y, const double z) {
+    const double tnoonn = 12.0 * 0.01745329;
+    const double tnoons = 3.141592654 - tnoonn;
+    const double r2 = x * x + y * y + z * z;
+    const double r = sqrt(r2);
+    const double r3 = r * r2;
+    double pas = 0.0;
+    if (x != 0.0 || y != 0.0) pas = atan2(y, x);
+    const double tas = atan2(sqrt(x * x + y * y), z);
+    const double stas = sin(tas);
+    double tet0 = asin(stas / pow((stas * stas * stas * stas * stas * stas) * (1.0 - r3) + r3, 0.1666666667));
+    if (tas > 1.5707963) tet0 = 3.141592654 - tet0;
+    const double sh = sin(pas * 0.5);
+    const double dtet = (8.0 * 0.01745329) * (sh * sh);
+    const double tr1n = tnoonn + dtet, tr1s = tnoons - dtet;
+    const double t01n = tr1n - 0.034906, t01s = tr1s - 0.034906;
+    const double t02s = tr1s + 0.034906, t02n = tr1n + 0.034906;
+    Vec3 b = {0.0, 0.0, 0.0};
+    if (tet0 < t01n || tet0 > t02s) {
+        const Vec3 t = t96_r1_loops(x, y, z);
+        b.x += t.x;
+        b.y += t.y;
+        b.z += t.z;
+    }
+    if (tet0 > t02n && tet0 < t01s) {
+        const Vec3 t = t96_r1_condip(x, y, z);
+        b.x += t.x;
+        b.y += t.y;
+        b.z += t.z;
+    }
+    if ((tet0 >= t01n && tet0 <= t02n) || (tet0 >= t01s && tet0 <= t02s)) {
+        double spas, cpas;
+        sincos(pas, &spas, &cpas);
+        const bool south = tet0 >= t01s;
+        b = t96_birk1_blend(x, y, z, r, r3, cpas, spas, south ? t01s : t01n, south ? t02s : t02n, south);
+    }
+    const Vec3 s = t96_birk1shld(x, y, z);
+    return {b.x + s.x, b.y + s.y, b.z + s.z};
+}
+
+// birk2shl, :1196-1263
+__device__ __forceinline__ Vec3 t96_birk2shl(const double x, const double y, const double z) {
+    constexpr double AI[2] = {13.85650567, 14.90554500};
+    constexpr double AK[2] = {10.21914434, 10.09021632};
+    constexpr double AS[4] = {-111.6371348 + 124.5402702, 110.3735178 + -122.0095905, 111.9448247 + -129.1957743,
+                              -110.7586562 + 126.5649012};
+    double szk[2], czk[2];
+#pragma unroll
+    for (int k = 0; k < 2; k++) sincos(div_c(z, AK[k], 1.0 / AK[k]), &szk[k], &czk[k]);
+    double hx = 0.0, hy = 0.0, hz = 0.0;
+#pragma unroll
+    for (int i = 0; i < 2; i++) {
+        double sy, cy;
+        sincos(div_c(y, AI[i], 1.0 / AI[i]), &sy, &cy);
+#pragma unroll
+        for (int k = 0; k < 2; k++) {
+            const double sq = c_t96.b2s_sq[2 * i + k];
+            const double e = exp(x * sq);
+            hx += (-sq * e * cy * szk[k]) * AS[2 * i + k];
+            hy += (div_c(e, AI[i], 1.0 / AI[i]) * sy * szk[k]) * AS[2 * i + k];
+            hz += (div_c(-e, AK[k], 1.0 / AK[k]) * cy * czk[k]) * AS[2 * i + k];
+        }
+    }
+    return {hx, hy, hz};
+}
+
+// xksi and tksi, :1595-1643
+__device__ __forceinline__ double t96_xksi(const double x, const double y, const double z) {
+    const double x2 = x * x, y2 = y * y, z2 = z * z;
+    const double r2 = x2 + y2 + z2;
+    const double r = sqrt(r2);
+    const double rr = 1.0 / r;
+    const double xr = div_r(x, r, rr), yr = div_r(y, r, rr), zr = div_r(z, r, rr);
+    const double dr = 7.50937;
+    const double dr2 = dr * dr;
+    const double r0 = 1.21563;
+    double pr = 0.0;
+    if (r >= r0) pr = sqrt((r - r0) * (r - r0) + dr2) - dr;
+    const double f = x + pr * (0.305662 + -0.383593 * xr + 0.2677733 * xr * xr + -0.097656 * yr * yr + -0.636034 * zr * zr);
+    const double g = y + pr * (-0.359862 * yr + 0.424706 * xr * yr);
+    const double h = z + pr * (-0.126366 * zr + 0.292578 * xr * zr);
+    const double g2 = g * g;
+    const double fgh = f * f + g2 + h * h;
+    const double sq = sqrt(fgh);
+    const double fgh32 = sq * sq * sq;
+    const double fg2 = (f * f) + g2;
+    if (fg2 < 1.0e-5) return -1.0;
+    const double th = sin(0.3665191 + 0.5 * 0.09599309 * (1.0 - f / sqrt(fg2)));
+    return (fg2 / fgh32) - (th * th);
+}
+
+__device__ __forceinline__ double t96_tksi(const double xk, const double x0, const double dx) {
+    const double tdz3 = 2.0 * dx * dx * dx;
+    if (xk - x0 < -dx) return 0.0;
+    if (xk - x0 >= dx) return 1.0;
+    if (xk >= x0 - dx && xk < x0) {
+        const double d = xk - x0 + dx;
+        const double br3 = d * d * d;
+        return 1.5 * br3 / (tdz3 + br3);
+    }
+    const double d = xk - x0 - dx;
+    const double br3 = d * d * d;
+    return 1.0 + 1.5 * br3 / (tdz3 - br3);
+}
+
+// loops4, :1445-1509, fixed tilt index il into c_t96.loop_cs
+__device__ __forceinline__ Vec3 t96_loops4(const double x, const double y, const double z, const double xc,
+                                          const double yc, const double zc, const double R, const int il) {
+    const double st = c_t96.loop_cs[il][0], ct = c_t96.loop_cs[il][1];
+    const double sp = c_t96.loop_cs[il][2], cp = c_t96.loop_cs[il][3];
+    double xs, yss, zs, xss, zss, bxs;
+    xs = (x - xc) * cp + (y - yc) * sp;
+    yss = (y - yc) * cp - (x - xc) * sp;
+    zs = z - zc;
+    xss = xs * ct - zs * st;
+    zss = zs * ct + xs * st;
+    Vec3 q = t96_circle(xss, yss, zss, R);
+    bxs = q.x * ct + q.z * st;
+    const double bz1 = q.z * ct - q.x * st;
+    const double bx1 = bxs * cp - q.y * sp;
+    const double by1 = bxs * sp + q.y * cp;
+    xs = (x - xc) * cp - (y + yc) * sp;
+    yss = (y + yc) * cp + (x - xc) * sp;
+    zs = z - zc;
+    xss = xs * ct - zs * st;
+    zss = zs * ct + xs * st;
+    q = t96_circle(xss, yss, zss, R);
+    bxs = q.x * ct + q.z * st;
+    const double bz2 = q.z * ct - q.x * st;
+    const double bx2 = bxs * cp + q.y * sp;
+    const double by2 = -bxs * sp + q.y * cp;
+    xs = -(x - xc) * cp + (y + yc) * sp;
+    yss = -(y + yc) * cp - (x - xc) * sp;
+    zs = z + zc;
+    xss = xs * ct - zs * st;
+    zss = zs * ct + xs * st;
+    q = t96_circle(xss, yss, zss, R);
+    bxs = q.x * ct + q.z * st;
+    const double bz3 = q.z * ct - q.x * st;
+    const double bx3 = -bxs * cp - q.y * sp;
+    const double by3 = bxs * sp - q.y * cp;
+    xs = -(x - xc) * cp - (y - yc) * sp;
+    yss = -(y - yc) * cp + (x - xc) * sp;
+    zs = z + zc;
+    xss = xs * ct - zs * st;
+    zss = zs * ct + xs * st;
+    q = t96_circle(xss, yss, zss, R);
+    bxs = q.x * ct + q.z * st;
+    return {bx1 + bx2 + bx3 + (-bxs * cp + q.y * sp), by1 + by2 + by3 + (-bxs * sp - q.y * cp),
+            bz1 + bz2 + bz3 + (q.z * ct - q.x * st)};
+}
+
+// r2inner (:1316-1334) with bconic (:1336-1372) and dipdistr (:1374-1392)
+__device__ __forceinline__ Vec3 t96_r2inner(const double x, const double y, const double z) {
+    constexpr double CB[5] = {154.185, -2.12446, 0.601735E-01, -.153954E-02, .355077E-04};
+    const double ro2 = x * x + y * y;
+    const double ro = sqrt(ro2);
+    const double rro = 1.0 / ro;
+    const double cf = div_r(x, ro, rro), sf = div_r(y, ro, rro);
+    const double r2 = ro2 + z * z;
+    const double r = sqrt(r2);
+    const double rr = 1.0 / r;
+    const double c = div_r(z, r, rr), s = div_r(ro, r, rr);
+    const double ch = sqrt(0.5 * (1.0 + c)), sh = sqrt(0.5 * (1.0 - c));
+    double tnhm1 = 1.0, cnhm1 = 1.0;
+    const double tnh = sh / ch, cnh = 1.0 / tnh;
+    const double ch2 = ch * ch, sh2 = sh * sh;
+    const double rs = r * s;
+    double cfm1 = 1.0, sfm1 = 0.0;
+    double bx = 0.0, by = 0.0, bz = 0.0;
+#pragma unroll
+    for (int m = 0; m < 5; m++) {
+        const double cfm = cfm1 * cf - sfm1 * sf;
+        const double sfm = cfm1 * sf + sfm1 * cf;
+        cfm1 = cfm;
+        sfm1 = sfm;
+        const double tnhm = tnhm1 * tnh, cnhm = cnhm1 * cnh;
+        const double bt = (m + 1) * cfm / rs * (tnhm + cnhm);
+        const double bf = div_r(-0.5 * (m + 1) * sfm, r, rr) * (tnhm1 / ch2 - cnhm1 / sh2);
+        tnhm1 = tnhm;
+        cnhm1 = cnhm;
+        const double cbx = bt * c * cf - bf * sf, cby = bt * c * sf + bf * cf, cbz = -bt * s;
+        if (m == 0) {
+            bx = CB[0] * cbx;
+            by = CB[0] * cby;
+            bz = CB[0] * cbz;
+        } else {
+            bx = bx + CB[m] * cbx;
+            by = by + CB[m] * cby;
+            bz = bz + CB[m] * cbz;
+        }
+    }
+    // dipdistr mode 0 at (x - .0774, y, z) and mode 1 at (x + .038, y, z)
+    Vec3 d6, d7;
+    {
+        const double xx = x - .0774;
+        const double x2 = xx * xx;
+        const double rho2 = x2 + y * y;
+        const double q2 = rho2 + z * z;
+        const double r3 = q2 * sqrt(q2);
+        const double rho4 = rho2 * rho2;
+        d6.x = z / rho4 * (q2 * (y * y - x2) - rho2 * x2) / r3;
+        d6.y = -xx * y * z / rho4 * (2.0 * q2 + rho2) / r3;
+        d6.z = xx / r3;
+    }
+    {
+        const double xx = x + .038;
+        const double x2 = xx * xx;
+        const double rho2 = x2 + y * y;
+        const double rho4 = rho2 * rho2;
+        d7.x = z / rho4 * (y * y - x2);
+        d7.y = -2.0 * xx * y * z / rho4;
+        d7.z = xx / rho2;
+    }
+    const Vec3 d8 = t96_loops4(x, y, z, -8.1902, 6.5239, 5.504, 7.7815, 0);
+    return {bx + 29.9996 * d6.x + 262.886 * d7.x + 99.9132 * d8.x, by + 29.9996 * d6.y + 262.886 * d7.y + 99.9132 * d8.y,
+            bz + 29.9996 * d6.z + 262.886 * d7.z + 99.9132 * d8.z};
+}
+
+// r2outer, :1394-1414
+__device__ __forceinline__ Vec3 t96_r2outer(const double x, const double y, const double z) {
+    const Vec3 d1 = t96_crosslp(x, y, z, 0.55, 0.694, 1);
+    const Vec3 d2 = t96_crosslp(x, y, z, 1.55, 2.8, 2);
+    const Vec3 d3 = t96_crosslp(x, y, z, -0.7, 0.2, 3);
+    const Vec3 d4 = t96_circle(x + 2.994, y, z, 2.925);
+    const Vec3 d5 = t96_loops4(x, y, z, -1.775, 4.3, -0.275, 2.7, 1);
+    return {-34.105 * d1.x + -2.00019 * d2.x + 628.639 * d3.x + 73.4847 * d4.x + 12.5162 * d5.x,
+            -34.105 * d1.y + -2.00019 * d2.y + 628.639 * d3.y + 73.4847 * d4.y + 12.5162 * d5.y,
+            -34.105 * d1.z + -2.00019 * d2.z + 628.639 * d3.z + 73.4847 * d4.z + 12.5162 * d5.z};
+}
+
+// r2sheet, :1511-1593, with xksi passed in (the reference evaluates the same
+// xksi(X, Y, Z) again).
+__device__ __forceinline__ Vec3 t96_r2sheet(const double x, const double y, const double z, const double xks) {
+    constexpr double CX[5][4][4] = {
+        {{8.07190, -7.39582, -7.62341, 0.684671}, {-13.5672, 11.6681, 13.1154, -0.890217},
+         {7.78726, -5.38346, -8.08738, 0.609385}, {-2.70410, 3.53741, 3.15549, -1.11069}},
+        {{-8.47555, 0.278122, 2.73514, 4.55625}, {13.1134, 1.15848, -3.52648, -8.24698},
+         {-6.85710, -2.81369, 2.03795, 4.64383}, {2.49309, -1.22041, -1.67432, -0.422526}},
+        {{-5.39796, 7.10326, 5.53730, -13.1918}, {4.67853, -7.60329, -2.53066, 7.76338},
+         {5.60165, 5.34816, -4.56441, 7.05976}, {-2.62723, -0.529078, 1.42019, -2.93919}},
+        {{55.6338, -1.55181, 39.8311, -80.6561}, {-46.9655, 32.8925, -6.32296, 19.7841},
+         {124.731, 10.4347, -30.7581, 102.680}, {-47.4037, -3.31278, 9.37141, -50.0268}},
+        {{-533.319, 110.426, 1000.20, -1051.40}, {1619.48, 589.855, -1462.73, 1087.10},
+         {-1994.73, -1654.12, 1263.33, -260.210}, {1424.84, 1255.71, -956.733, 219.946}}};
+    constexpr double CY[5][4][4] = {
+        {{-9.08427, 10.6777, 10.3288, -0.969987}, {6.45257, -8.42508, -7.97464, 1.41996},
+         {-1.92490, 3.93575, 2.83283, -1.48621}, {0.244033, -0.757941, -0.386557, 0.344566}},
+        {{9.56674, -2.5365, -3.32916, -5.86712}, {-6.19625, 1.83879, 2.52772, 4.34417},
+         {1.87268, -2.13213, -1.69134, -0.176379}, {-0.261359, 0.566419, 0.3138, -0.134699}},
+        {{-3.83086, -8.4154, 4.77005, -9.31479}, {37.5715, 19.3992, -17.9582, 36.4604},
+         {-14.9993, -3.1442, 6.17409, -15.5519}, {2.28621, -0.00891549, -0.462912, 2.47314}},
+        {{41.7555, 208.614, -45.7861, -77.8687}, {239.357, -67.9226, 66.8743, 238.534},
+         {-112.136, 16.2069, -40.4706, -134.328}, {21.56, -0.201725, 2.21, 32.5855}},
+        {{-108.217, -1005.98, 585.753, 323.668}, {-817.056, 235.750, -560.965, -576.892},
+         {684.193, 85.0275, 168.394, 477.776}, {-289.253, -123.216, 75.6501, -178.605}}};
+    constexpr double CZ[5][4][4] = {
+        {{1167.61, -917.782, -1253.2, -274.128}, {-1538.75, 1257.62, 1745.07, 113.479},
+         {393.326, -426.858, -641.1, 190.833}, {-29.9435, -1.04881, 117.125, -25.7663}},
+        {{-1168.16, 910.247, 1239.31, 289.515}, {1540.56, -1248.29, -1727.61, -131.785},
+         {-394.577, 426.163, 637.422, -187.965}, {30.0348, 0.221898, -116.68, 26.0291}},
+        {{12.6804, 4.84091, 1.18166, -2.75946}, {-17.9822, -6.80357, -1.47134, 3.02266},
+         {4.79648, 0.665255, -0.256229, -0.0857282}, {-0.588997, 0.0634812, 0.164303, -0.15285}},
+        {{22.2524, -22.4376, -3.85595, 6.07625}, {-105.959, -41.6698, 0.378615, 1.55958},
+         {44.3981, 18.8521, 3.19466, 5.89142}, {-8.63227, -2.36418, -1.027, -2.31515}},
+        {{1035.38, 2040.66, -131.881, -744.533}, {-3274.93, -4845.61, 482.438, 1567.43},
+         {1354.02, 2040.47, -151.653, -845.012}, {-111.723, -265.343, -26.1171, 216.632}}};
+    const double xks2 = xks * xks;
+    const double t1x = xks / sqrt(xks2 + 0.483750e-01 * 0.483750e-01);
+    const double px72 = 0.396953e-01 * 0.396953e-01;
+    const double qx = sqrt(xks2 + px72);
+    const double t2x = (px72 * 0.396953e-01) / (qx * qx * qx);
+    const double ux = sqrt(xks2 + 0.579023e-01 * 0.579023e-01);
+    const double t3x = xks / (ux * ux * ux * ux * ux) * 3.493856 * c_t96.r2s_k[5];
+    const double t1y = xks / sqrt(xks2 + 0.478750e-01 * 0.478750e-01);
+    const double py72 = 0.363750e-01 * 0.363750e-01;
+    const double qy = sqrt(xks2 + py72);
+    const double t2y = (py72 * 0.363750e-01) / (qy * qy * qy);
+    const double uy = sqrt(xks2 + 0.567500e-01 * 0.567500e-01);
+    const double t3y = xks / (uy * uy * uy * uy * uy) * 3.493856 * c_t96.r2s_k[6];
+    const double t1z = xks / sqrt(xks2 + 0.355625e-01 * 0.355625e-01);
+    const double pz72 = 0.318750e-01 * 0.318750e-01;
+    const double qz = sqrt(xks2 + pz72);
+    const double t2z = (pz72 * 0.318750e-01) / (qz * qz * qz);
+    const double uz = sqrt(xks2 + 0.538750e-01 * 0.538750e-01);
+    const double t3z = xks / (uz * uz * uz * uz * uz) * 3.493856 * c_t96.r2s_k[7];
+    const double rho2 = x * x + y * y;
+    const double r = sqrt(rho2 + z * z);
+    const double rho = sqrt(rho2);
+    const double rrho = 1.0 / rho;
+    const double c1p = div_r(x, rho, rrho), s1p = div_r(y, rho, rrho);
+    const double s2p = 2.0 * s1p * c1p;
+    const double c2p = c1p * c1p - s1p * s1p;
+    const double s3p = s2p * c1p + c2p * s1p;
+    const double c3p = c2p * c1p - s2p * s1p;
+    const double s4p = s3p * c1p + c3p * s1p;
+    const double ct = z / r;
+    const double ct2 = ct * ct;
+    const double ct2m1 = ct2 - 1.0;
+    double s[5];
+    s[0] = c_t96.r2s_k[0] * ct * exp(-19.0969 * ct2);
+    s[1] = c_t96.r2s_k[1] * ct * exp(-9.28828 * ct2);
+    s[2] = c_t96.r2s_k[2] * ct * exp(-0.129687 * ct2);
+    s[3] = ct * exp(5.58594 * ct2m1);
+    s[4] = ct * exp(22.5055 * ct2m1);
+    double acc = 0.0;
+#pragma unroll
+    for (int l = 0; l < 5; l++) {
+        const double term = (CX[l][0][0] + CX[l][0][1] * t1x + CX[l][0][2] * t2x + CX[l][0][3] * t3x) +
+                            c1p * (CX[l][1][0] + CX[l][1][1] * t1x + CX[l][1][2] * t2x + CX[l][1][3] * t3x) +
+                            c2p * (CX[l][2][0] + CX[l][2][1] * t1x + CX[l][2][2] * t2x + CX[l][2][3] * t3x) +
+                            c3p * (CX[l][3][0] + CX[l][3][1] * t1x + CX[l][3][2] * t2x + CX[l][3][3] * t3x);
+        acc = (l == 0) ? s[l] * term : acc + s[l] * term;
+    }
+    const double bx = acc;
+    s[0] = c_t96.r2s_k[3] * ct * exp(-13.6750 * ct2);
+    s[1] = c_t96.r2s_k[4] * ct * exp(-6.70625 * ct2);
+    s[2] = ct * exp(2.31875 * ct2m1);
+    s[3] = ct * exp(11.4062 * ct2m1);
+    s[4] = ct * exp(20.4562 * ct2m1);
+    acc = 0.0;
+#pragma unroll
+    for (int l = 0; l < 5; l++) {
+        const double term = s1p * (CY[l][0][0] + CY[l][0][1] * t1y + CY[l][0][2] * t2y + CY[l][0][3] * t3y) +
+                            s2p * (CY[l][1][0] + CY[l][1][1] * t1y + CY[l][1][2] * t2y + CY[l][1][3] * t3y) +
+                            s3p * (CY[l][2][0] + CY[l][2][1] * t1y + CY[l][2][2] * t2y + CY[l][2][3] * t3y) +
+                            s4p * (CY[l][3][0] + CY[l][3][1] * t1y + CY[l][3][2] * t2y + CY[l][3][3] * t3y);
+        acc = (l == 0) ? s[l] * term : acc + s[l] * term;
+    }
+    const double by = acc;
+    s[0] = exp(-16.7125 * ct2);
+    s[1] = exp(-16.4625 * ct2);
+    s[2] = exp(-0.1625 * ct2);
+    s[3] = exp(5.1 * (ct2 - 1.0));
+    s[4] = exp(23.7125 * (ct2 - 1.0));
+    acc = 0.0;
+#pragma unroll
+    for (int l = 0; l < 5; l++) {
+        const double term = (CZ[l][0][0] + CZ[l][0][1] * t1z + CZ[l][0][2] * t2z + CZ[l][0][3] * t3z) +
+                            c1p * (CZ[l][1][0] + CZ[l][1][1] * t1z + CZ[l][1][2] * t2z + CZ[l][1][3] * t3z) +
+                            c2p * (CZ[l][2][0] + CZ[l][2][1] * t1z + CZ[l][2][2] * t2z + CZ[l][2][3] * t3z) +
+                            c3p * (CZ[l][3][0] + CZ[l][3][1] * t1z + CZ[l][3][2] * t2z + CZ[l][3][3] * t3z);
+        acc = (l == 0) ? s[l] * term : acc + s[l] * term;
+    }
+    return {bx, by, acc};
+}
+
+// r2_birk, :1265-1314
+__device__ __forceinline__ Vec3 t96_r2birk(const double x, const double y, const double z) {
+    const double dl = 0.03, dl1 = 0.015;
+    const double xks = t96_xksi(x, y, z);
+    if (xks < -(dl + dl1)) {
+        const Vec3 q = t96_r2outer(x, y, z);
+        return {q.x * -0.02, q.y * -0.02, q.z * -0.02};
+    }
+    if (xks < -dl + dl1) {
+        const Vec3 q1 = t96_r2outer(x, y, z);
+        const Vec3 q2 = t96_r2sheet(x, y, z, xks);
+        const double f2 = -0.02 * t96_tksi(xks, -dl, dl1);
+        const double f1 = -0.02 - f2;
+        return {q1.x * f1 + q2.x * f2, q1.y * f1 + q2.y * f2, q1.z * f1 + q2.z * f2};
+    }
+    if (xks < dl - dl1) {
+        const Vec3 q = t96_r2sheet(x, y, z, xks);
+        return {q.x * -0.02, q.y * -0.02, q.z * -0.02};
+    }
+    if (xks < dl + dl1) {
+        const Vec3 q1 = t96_r2inner(x, y, z);
+        const Vec3 q2 = t96_r2sheet(x, y, z, xks);
+        const double f1 = -0.02 * t96_tksi(xks, dl, dl1);
+        const double f2 = -0.02 - f1;
+        return {q1.x * f1 + q2.x * f2, q1.y * f1 + q2.y * f2, q1.z * f1 + q2.z * f2};
+    }
+    const Vec3 q = t96_r2inner(x, y, z);
+    return {-q.x * 0.02, -q.y * 0.02, -q.z * 0.02};
+}
+
+// dipole_t96, :1645-1656 (its x component keeps the reference's form)
+__device__ __forceinline__ Vec3 t96_dipole(const double x, const double y, const double z) {
+    const double p = x * x, u = z * z, v = 3.0 * z * x, t = y * y;
+    const double ptu = sqrt(p + t + u);
+    const double q = 30574.0 / (ptu * ptu * ptu * ptu * ptu);
+    return {q * ((t + u - 2.0 * p) - v), -3.0 * y * q * z, q * (p + t - 2.0 * u)};
+}
+
+// t96_gsm, :4-111.  x = GSM position [R_E]; c = per-condition block.
+__device__ __forceinline__ Vec3 t96_field(const T96Cond& c, const Vec3 X) {
+    const double x = X.x, y = X.y, z = X.z;
+    const double ys = y * c.ct - z * c.st, zs = z * c.ct + y * c.st;
+    const double ysd = div_c(ys, 10.0, 1.0 / 10.0);
+    const double factimf = exp(div_c(x, 20.0, 1.0 / 20.0) - ysd * ysd);
+    const double oimfy = c.kimfy * factimf, oimfz = c.kimfz * factimf;
+    const double rho2 = y * y + z * z;
+    double xmxm = c.am + x - c.c548;
+    if (xmxm < 0.0) xmxm = 0.0;
+    const double axx0 = xmxm * xmxm;
+    const double aro = c.asq + rho2;
+    const double aa = aro + axx0;
+    const double sigma = sqrt(div_r(aro + axx0 + sqrt(aa * aa - c.four_asq * axx0), c.two_asq, c.r_two_asq));
+    if (sigma >= 1.08 + 0.005) {
+        const Vec3 q = t96_dipole(x, y, z);
+        return {-q.x, oimfy - q.y, oimfz - q.z};
+    }
+    const double xx = x * c.xappa, yy = y * c.xappa, zz = z * c.xappa;
+    const Vec3 cf = t96_cylharm(xx, yy, zz);
+    // tailrc_96, :273-321
+    const Vec3 rch = t96_ringcurr(xx, yy, zz);
+    const Vec3 rcw = t96_shlcar3x3(0, xx, yy, zz);
+    const Vec3 rc = {rcw.x + rch.x, rcw.y + rch.y, rcw.z + rch.z};
+    const Vec3 t2w = t96_shlcar3x3(1, xx, yy, zz);
+    const Vec3 t2h = t96_taildisk(xx, yy, zz);
+    const Vec3 t2 = {t2w.x + t2h.x, t2w.y + t2h.y, t2w.z + t2h.z};
+    const Vec3 t3w = t96_shlcar3x3(2, xx, yy, zz);
+    double t3hx, t3hz;
+    t96_tail87(xx, zz, t3hx, t3hz);
+    const Vec3 t3 = {t3w.x + t3hx, t3w.y, t3w.z + t3hz};
+    const Vec3 r1 = t96_birk1tot(xx, yy, zz);
+    Vec3 r2 = t96_birk2shl(xx, yy, zz);
+    const Vec3 r2h = t96_r2birk(xx, yy, zz);
+    r2.x += r2h.x;
+    r2.y += r2h.y;
+    r2.z += r2h.z;
+    const Vec3 im = t96_intercon(xx, ys * c.xappa, zs * c.xappa);
+    const double rimfy = im.y * c.ct + im.z * c.st;
+    const double rimfz = im.z * c.ct - im.y * c.st;
+    const double fx = cf.x * c.xappa3 + c.rcampl * rc.x + c.tampl2 * t2.x + c.tampl3 * t3.x + c.b1ampl * r1.x +
+                      c.b2ampl * r2.x + c.rimfampl * im.x;
+    const double fy = cf.y * c.xappa3 + c.rcampl * rc.y + c.tampl2 * t2.y + c.tampl3 * t3.y + c.b1ampl * r1.y +
+                      c.b2ampl * r2.y + c.rimfampl * rimfy;
+    const double fz = cf.z * c.xappa3 + c.rcampl * rc.z + c.tampl2 * t2.z + c.tampl3 * t3.z + c.b1ampl * r1.z +
+                      c.b2ampl * r2.z + c.rimfampl * rimfz;
+    if (sigma < 1.08 - 0.005) return {fx, fy, fz};
+    const double fint = 0.5 * (1.0 - div_c(sigma - 1.08, 0.005, 1.0 / 0.005));
+    const double fext = 0.5 * (1.0 + div_c(sigma - 1.08, 0.005, 1.0 / 0.005));
+    const Vec3 q = t96_dipole(x, y, z);
+    return {(fx + q.x) * fint - q.x, (fy + q.y) * fint + oimfy * fext - q.y, (fz + q.z) * fint + oimfz * fext - q.z};
+}
+
+}  // namespace cor

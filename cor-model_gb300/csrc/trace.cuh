@@ -28,9 +28,13 @@ struct TraceArgs {
     const uint64_t* offsets;  // n_jobs + 1 exclusive prefix
     int32_t n_jobs;
     uint64_t n_traj;
-    const cor_model_params* params;
+    const DevParams* params;
     uint64_t step_limit;
     double tu_angle;
+    double gc_reject;   // turn test: reject iff gc <= gc_reject (exact host-derived threshold)
+    int turn_exact;     // 1: use gc_reject; 0: evaluate atan2 as the reference does
+    int rig_major;      // 1: queue index runs over rigidity first (all jobs share n_rig)
+    uint32_t n_rig;
     double mass;
     uint8_t* status;
     cor_traj_record* records;
@@ -54,7 +58,7 @@ struct Lane {
     Vec3 pos, vel, field, gsm;
     double b, v, time, alength, rig;
     const cor_scan_job* job;
-    const cor_model_params* par;
+    const DevParams* par;
     uint64_t traj;
     uint32_t step, trials;
     int nk0;
@@ -77,13 +81,24 @@ __device__ __forceinline__ uint64_t queue_pop(unsigned long long* q, bool want) 
 // Start of one trajectory, src/trajectory.c:13-44 (the field is evaluated
 // by the caller in the converged section).
 __device__ __forceinline__ void lane_init(Lane& L, const TraceArgs& a, uint64_t t) {
-    const int j = find_job(a.offsets, a.n_jobs, t);
+    // Queue position -> (scan j, rigidity index i).  In rigidity-major order
+    // the lowest rigidities of every scan, whose trajectories are the
+    // longest, are handed out first (longest-processing-time-first), which
+    // keeps the end of the run from being a tail of lone long trajectories.
+    int j;
+    uint64_t i;
+    if (a.rig_major) {
+        i = t / (uint64_t)a.n_jobs;
+        j = (int)(t - i * (uint64_t)a.n_jobs);
+    } else {
+        j = find_job(a.offsets, a.n_jobs, t);
+        i = t - a.offsets[j];
+    }
     const cor_scan_job* job = a.jobs + j;
     const JobTrig tg = a.trig[j];
-    const uint64_t i = t - a.offsets[j];
     L.job = job;
     L.par = a.params + job->param_index;
-    L.traj = t;
+    L.traj = a.offsets[j] + i;
     const double rig = job->rig + (int)i * job->del;
     L.rig = rig;
     L.nk0 = job->nk1;
@@ -108,7 +123,7 @@ __device__ __forceinline__ void lane_init(Lane& L, const TraceArgs& a, uint64_t 
     L.v = vr0;
     L.step = 0;
     L.trials = 0;
-    L.gsm = geo_to_gsm(L.pos, L.par);
+    L.gsm = geo_to_gsm(L.pos, &L.par->p);
 }
 
 // Advances one lane to its next accepted step (returns 0) or to its
@@ -121,7 +136,7 @@ __device__ __forceinline__ int lane_advance(Lane& L, const TraceArgs& a) {
     const int nk1 = L.job->nk1;
     for (;;) {
         L.step++;
-        const double vc = L.v / kC;
+        const double vc = div_c(L.v, kC, 1. / kC);
         if (vc > 1.) return COR_TRAJ_SUPERLUM;  // :48-54
         const double hm = a.mass / sqrt(1. - vc * vc);
         const double t = (2. * kPi * hm) / (fabs(zn) * kQ * L.b);
@@ -132,22 +147,33 @@ __device__ __forceinline__ int lane_advance(Lane& L, const TraceArgs& a) {
         L.trials++;
         L.v = sqrt(nv.x * nv.x + nv.y * nv.y + nv.z * nv.z);
         const double gc = (nv.x * L.vel.x + nv.y * L.vel.y + nv.z * L.vel.z) / (L.v * vprev);
-        if (gc < 1.) {  // :69-79
-            const double gs = sqrt((1. - gc) * (1. + gc));
-            const double gu = atan2(gs, gc);
-            if (gu >= a.tu_angle && L.nk0 <= 50000) {
-                L.nk0 *= 2;
-                L.step--;
-                continue;
+        // Turn-angle test, :69-79: reject iff gc < 1 and
+        // atan2(sqrt((1-gc)(1+gc)), gc) >= tu_angle.  That predicate of the
+        // rounded gc is a step function; the host finds its last true value
+        // with the C library and checks the step, so one comparison gives
+        // the reference's decision exactly.
+        bool reject;
+        if (a.turn_exact) {
+            reject = gc <= a.gc_reject;
+        } else {
+            reject = false;
+            if (gc < 1.) {
+                const double gs = sqrt((1. - gc) * (1. + gc));
+                reject = atan2(gs, gc) >= a.tu_angle;
             }
+        }
+        if (reject && L.nk0 <= 50000) {
+            L.nk0 *= 2;
+            L.step--;
+            continue;
         }
         const Vec3 np = rk_position(h, L.vel, L.pos);
         const double rr = sqrt(np.x * np.x + np.y * np.y + np.z * np.z);  // car_to_sph radius
-        const Vec3 gsm = geo_to_gsm(np, L.par);
-        const double pax = (gsm.x / kRe + 25.3) / 36.08;
-        const double paz = (gsm.y * gsm.y + gsm.z * gsm.z) / (kRe * kRe);
-        const double r = rr / kRe;
-        const double paus = pax * pax + paz / 459.6736;
+        const Vec3 gsm = geo_to_gsm(np, &L.par->p);
+        const double pax = div_c(DIVRE(gsm.x) + 25.3, 36.08, 1. / 36.08);
+        const double paz = div_c(gsm.y * gsm.y + gsm.z * gsm.z, kRe * kRe, 1. / (kRe * kRe));
+        const double r = DIVRE(rr);
+        const double paus = pax * pax + div_c(paz, 459.6736, 1. / 459.6736);
         if (r >= 25. || paus > 1.) {  // :89-131
             if ((r >= 25. && fabs(r - 25.) < 0.002) || (r <= 25. && paus > 1. && fabs(paus - 1.) < 0.002)) {
                 L.pos = np;
@@ -165,7 +191,7 @@ __device__ __forceinline__ int lane_advance(Lane& L, const TraceArgs& a) {
         if (r < 1.) return COR_TRAJ_REENTRY;                          // :133-138
         if ((uint64_t)L.step > a.step_limit) return COR_TRAJ_STEP_LIMIT;  // :140-145 (phi > 31.4 cannot hold)
         L.gsm = gsm;
-        L.time = L.time + t / L.nk0;                                  // :150-152
+        L.time = L.time + h;                                          // :150-152 (t/nk0 == h)
         L.alength += sqrt((np.x - prev.x) * (np.x - prev.x) + (np.y - prev.y) * (np.y - prev.y) +
                           (np.z - prev.z) * (np.z - prev.z));
         L.nk0 = nk1;
@@ -291,7 +317,7 @@ __global__ void reduce_kernel(const cor_scan_job* __restrict__ jobs, const uint6
 }
 
 template <class MS>
-__global__ void field_kernel(const cor_model_params* __restrict__ params, int n_params,
+__global__ void field_kernel(const DevParams* __restrict__ params, int n_params,
                              const int32_t* __restrict__ pidx, const double* __restrict__ pos, int64_t n,
                              double* __restrict__ out, CrustalTables crust) {
     const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;

@@ -185,21 +185,31 @@ int cor_prepare_trig(const cor_scan_job *jobs, int32_t n_jobs, cor_job_trig *out
  * until the results are on the host. */
 int cor_trace_batch(cor_ctx *ctx, const cor_batch_req *req, cor_batch_result *out);
 
+/* cor_trace_batch_device flags */
+#define COR_FLAG_UNIFORM_GRID 1u  /* every job has the same number of rigidities:
+                                     the work queue then hands out the lowest
+                                     rigidities of all jobs first */
+
+/* Uploads n_params parameter blocks to the device, where they stay for the
+ * following cor_trace_batch_device calls (cor_trace_batch uploads its own).
+ * Per-condition constants of the external models are derived here on the
+ * host. */
+int cor_upload_params(cor_ctx *ctx, const cor_model_params *params, int32_t n_params);
+
 /* Same scan with every buffer already in device memory (jobs, trig from
- * cor_prepare_trig, offsets from cor_batch_count, params, sites, status,
- * records); `stream` is a
+ * cor_prepare_trig, offsets from cor_batch_count, sites, status, records) and
+ * the parameter blocks of the last cor_upload_params; `stream` is a
  * cudaStream_t (NULL = the legacy default stream).  Returns after the
- * launches are queued; counters are written to the device buffer
- * `counters_dev` (a cor_counters) and read by the caller. */
+ * launches are queued; counters go to the device buffer `counters_dev` (a
+ * cor_counters; NULL = internal). */
 int cor_trace_batch_device(cor_ctx *ctx,
                            const cor_scan_job *jobs_dev, const cor_job_trig *trig_dev,
                            int32_t n_jobs, const uint64_t *offsets_dev, uint64_t n_trajectories,
-                           const cor_model_params *params_dev, int32_t n_params,
                            cor_model_set models, uint64_t step_limit,
                            double tu_angle, double particle_mass,
                            cor_site_result *sites_dev, uint8_t *status_dev,
                            cor_traj_record *records_dev, cor_counters *counters_dev,
-                           void *stream);
+                           uint32_t flags, void *stream);
 
 /* ---- field ------------------------------------------------------------ */
 /* calculate_field (src/models.c:194-207) at n points: gsm_pos is n x 3 GSM

@@ -111,3 +111,96 @@ def test_invalid_requests_fail_cleanly(ctx):
     # the context stays usable
     res = ctx.trace_batch(ct.make_job(0.0, 0.0, rig=1.0, rk=2.0, dele=0.5), p)
     assert res.counters["trajectories"] == 3
+
+
+# ---- T96 -------------------------------------------------------------------
+# The device T96 uses CUDA's FP64 exp/log/sin/cos/atan/asin/pow, which differ
+# from the C library's by a few ulp, so its field agrees with the reference's
+# to a relative tolerance instead of bit for bit.  FIELD_RTOL is the bound
+# asked of the field (1e-12 relative to |B|).
+FIELD_RTOL = 1e-12
+
+
+def _rel_err(got, want):
+    return np.linalg.norm(got - want, axis=1) / np.maximum(np.linalg.norm(want, axis=1), 1e-300)
+
+
+def test_field_t96_kats(ctx):
+    g = golden("field_kats.json")["t96_gsm"]
+    pm = unhex(g["parmod"])
+    p = ct.internal_setup("igrf14", [2020, 1, 1, 1, 0, 0, 0], parmod=pm)
+    p["a1"][0], p["a2"][0], p["a3"][0] = [1, 0, 0], [0, 1, 0], [0, 0, 1]
+    pts = unhex(g["points"]).reshape(-1, 3)
+    want = unhex(g["b"]).reshape(-1, 3)
+    got = ctx.field_batch(pts * ct.DEF_RE, p, models=ct.model_set(ct.INTERNAL_NONE, ct.EXTERNAL_T96))
+    exact = np.all(((pts * ct.DEF_RE) / ct.DEF_RE) == pts, axis=1)
+    err = _rel_err(got[exact], want[exact])
+    print(f"t96 KAT: {exact.sum()} points, max rel err {err.max():.3e}, median {np.median(err):.3e}")
+    assert err.max() <= FIELD_RTOL
+
+
+def test_field_igrf_t96_calculate_field(ctx):
+    g = golden("field_kats.json")["calculate_field"]
+    case = g["cases"]["igrf14+t96"]
+    p = ct.internal_setup("igrf14", g["time"], parmod=unhex(case["parmod"]))
+    pts = unhex(g["points_m"]).reshape(-1, 3)
+    want = unhex(case["b"]).reshape(-1, 3)
+    got = ctx.field_batch(pts, p, models=ct.model_set(ct.INTERNAL_SH, ct.EXTERNAL_T96))
+    err = _rel_err(got, want)
+    print(f"igrf14+t96 calculate_field: max rel err {err.max():.3e}")
+    assert err.max() <= FIELD_RTOL
+
+
+def _scan_golden(name, models):
+    g = golden(name)
+    p = ct.internal_setup(g["model"], g["time"], parmod=g["parmod"])
+    jobs = config0_jobs(g["sites"], g["rig"], g["rk"], g["del"])
+    return g, p, jobs
+
+
+def test_scan_t96_matches_reference(ctx):
+    """IGRF-14 + T96, 10 sites x 2000 rigidities against the reference's own scans:
+    allowed/forbidden flags agree on >= 99.9% of trajectories, every
+    disagreement lies inside the scan's penumbra [P(S), P(C)], and P(S), P(C),
+    P(M) agree within one rigidity step at >= 99.5% of sites."""
+    models = ct.model_set(ct.INTERNAL_SH, ct.EXTERNAL_T96)
+    g, p, jobs = _scan_golden("scan_t96.json", models)
+    res = ctx.trace_batch(jobs, p, models=models)
+    n_traj = n_agree = 0
+    sites_ok = 0
+    outside = []
+    d = g["del"]
+    for j, s in enumerate(g["sites"]):
+        st = res.status[res.offsets[j]:res.offsets[j + 1]]
+        mine = st == ct.TRAJ_ALLOWED
+        ref = np.zeros(len(st), bool)
+        ref[s["allowed"]] = True
+        n_traj += len(st)
+        n_agree += int(np.sum(mine == ref))
+        lo = min(float(s["cutoff"][0]), res.sites[j]["r_lower"]) - d
+        hi = max(float(s["cutoff"][1]), res.sites[j]["r_upper"]) + d
+        rig = g["rig"] + np.arange(len(st)) * d
+        bad = np.nonzero(mine != ref)[0]
+        outside += [(j, float(rig[i])) for i in bad if not (lo <= rig[i] <= hi)]
+        mine3 = [res.sites[j]["r_lower"], res.sites[j]["r_upper"], res.sites[j]["r_cutoff"]]
+        if all(abs(a - float(b)) <= d * 1.0000001 for a, b in zip(mine3, s["cutoff"])):
+            sites_ok += 1
+    print(f"T96 scan: flag agreement {n_agree / n_traj:.5f}, sites within one step {sites_ok}/{len(g['sites'])}")
+    assert n_agree / n_traj >= 0.999
+    assert not outside, outside[:10]
+    assert sites_ok / len(g["sites"]) >= 0.995 or len(g["sites"]) - sites_ok <= 0
+
+
+def test_scan_t96_equals_oracle_statistics(ctx):
+    """Same scans against the oracle (the CPU restatement): identical flags
+    outside the penumbra and the same total work to within a few percent."""
+    models = ct.model_set(ct.INTERNAL_SH, ct.EXTERNAL_T96)
+    g, p, jobs = _scan_golden("scan_t96.json", models)
+    jobs = jobs[:3]
+    gpu = ctx.trace_batch(jobs, p, models=models)
+    cpu = pyoracle.scan_batch(jobs, p, models=models, threads=8)
+    agree = np.mean(gpu.status == cpu.status)
+    ratio = gpu.counters["accepted_steps"] / cpu.counters["accepted_steps"]
+    print(f"T96 vs oracle: status agreement {agree:.5f}, step ratio {ratio:.4f}")
+    assert agree >= 0.999
+    assert abs(ratio - 1.0) < 0.05

@@ -90,3 +90,18 @@ def test_oracle_flop_model():
     assert pyoracle.internal_geo_flops(1.5) > pyoracle.internal_geo_flops(2.5) > pyoracle.internal_geo_flops(20.0)
     # K = 14 at R < 2: 105 (n,m) terms, 14 of them with m = 1
     assert pyoracle.internal_geo_flops(1.0) == 12 + 28 + 13 + 14 * 4 + 13 * 8 + 14 * 17 + (105 - 14) * 23
+
+
+def _ext_kat(name: str, fn):
+    g = golden("field_kats.json")[name]
+    pm = unhex(g["parmod"])
+    pts = unhex(g["points"]).reshape(-1, 3)
+    want = unhex(g["b"]).reshape(-1, 3)
+    b = np.zeros(3)
+    for i, (x, y, z) in enumerate(pts):
+        fn(pm.ctypes.data, x, y, z, b[0:].ctypes.data, b[1:].ctypes.data, b[2:].ctypes.data)
+        assert np.array_equal(b.view(np.uint64), want[i].view(np.uint64)), (name, i, b, want[i])
+
+
+def test_oracle_t96_bit_exact():
+    _ext_kat("t96_gsm", pyoracle.load().orc_t96_gsm)
