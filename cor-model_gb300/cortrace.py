@@ -23,6 +23,8 @@ INTERNAL_NONE, INTERNAL_SH = 0, 1
 EXTERNAL_NONE, EXTERNAL_T96, EXTERNAL_TS05 = 0, 1, 2
 CRUSTAL_NONE, CRUSTAL_CHAOS = 0, 1
 
+FLAG_UNIFORM_GRID = 1
+
 TRAJ_NONE, TRAJ_ALLOWED, TRAJ_REENTRY, TRAJ_SUPERLUM, TRAJ_STEP_LIMIT, TRAJ_WATCHDOG = range(6)
 
 # Physical constants of the reference (src/common.h:4-11).
@@ -80,7 +82,7 @@ class BatchResult(C.Structure):
 EXPORTS = [
     "cor_ctx_create", "cor_ctx_destroy", "cor_last_error_string", "cor_abi_version", "cor_batch_count",
     "cor_prepare_trig", "cor_trace_batch", "cor_trace_batch_device", "cor_upload_params", "cor_field_batch",
-    "cor_internal_setup", "cor_gsm_setup",
+    "cor_internal_setup", "cor_gsm_setup", "cor_probe_fp64_peak",
 ]
 
 _lib = None
@@ -106,6 +108,7 @@ def load(path: str = LIB_PATH) -> C.CDLL:
     lib.cor_trace_batch_device.argtypes = [vp, vp, vp, i32, vp, u64, ModelSet, u64, dbl, dbl,
                                            vp, vp, vp, vp, C.c_uint32, vp]
     lib.cor_upload_params.argtypes = [vp, vp, i32]
+    lib.cor_probe_fp64_peak.argtypes = [vp, C.POINTER(C.c_double)]
     lib.cor_field_batch.argtypes = [vp, ModelSet, vp, i32, vp, vp, i64, vp]
     lib.cor_internal_setup.argtypes = [C.c_char_p, vp, vp]
     lib.cor_gsm_setup.argtypes = [vp, vp]

@@ -8,7 +8,9 @@
 #include <stdlib.h>
 #include <string.h>
 
-#include "trace.cuh"
+#include "model_ops.h"
+#include "reduce.cuh"
+#include "ts05_tables.h"
 
 using namespace cor;
 
@@ -32,6 +34,10 @@ struct cor_ctx {
     DevBuf jobs, trig, offsets, params, sites, status, records;
     int32_t n_params = 0;                 // resident DevParams blocks (cor_upload_params)
     unsigned long long* queue = nullptr;  // work-queue counter (scratch)
+    DevBuf park[2];                       // parked trajectories between generations (scratch)
+    GenCounters* gen = nullptr;           // per-generation counters (scratch)
+    unsigned int* park_count_host = nullptr;  // pinned readback of the parked count
+    int generations = 0;                  // generations of the last scan (diagnostics)
     cor_counters* counters = nullptr;
     const double* crust_g = nullptr;      // device copies of the crustal table
     const double* crust_h = nullptr;
@@ -167,11 +173,125 @@ static void t96_tables(T96Tables* t) {
     t->r2s_k[7] = pow(0.538750e-01, 4);
 }
 
+// Per-condition quantities of ts05_gsm that depend only on PARMOD
+// (lib/ts05/ts05.c:19-110), and the condition-dependent shield amplitudes
+// (shlcar5x5 deformed.c:196-197, birk_shl birk_tot.c:393, rc_shield
+// full_rc.c:691-711), with the reference's expressions.
+static void ts05_shield_amps(const double* T, double xsc, double* amp) {
+    for (int m = 0; m < 9; m++) {
+        const int l = 4 * m;
+        amp[m] = T[l] + xsc * T[l + 1] + T[l + 2] + xsc * T[l + 3];
+    }
+}
+
+static void ts05_prepare(const double* parmod, TS05Cond* c) {
+    using namespace ts05h;
+    const double pdyn = parmod[0];
+    const double dst = parmod[1] * 0.8 - 13. * sqrt(pdyn);
+    const double w1 = parmod[4], w2 = parmod[5], w3 = parmod[6], w4 = parmod[7], w5 = parmod[8], w6 = parmod[9];
+    c->byimf = parmod[2];
+    c->bzimf = parmod[3];
+    c->xappa = pow((pdyn / 2.), A[22]);
+    c->xappa3 = c->xappa * c->xappa * c->xappa;
+    c->am = 34.586 / c->xappa;
+    c->x0 = 3.4397 / c->xappa;
+    c->oimfy_k = c->byimf * A[19];
+    c->oimfz_k = c->bzimf * A[19];
+    c->asq = c->am * c->am;
+    c->four_asq = 4. * c->asq;
+    c->two_asq = 2. * c->asq;
+    c->r_two_asq = 1. / c->two_asq;
+    double dstt = -20.;
+    if (dst < dstt) dstt = dst;
+    double znam = pow(fabs(dstt), 0.37);
+    c->dx1 = A[23] - A[24] / znam;
+    c->dx2 = A[25] - A[26] / znam;
+    c->d = A[35] * exp(-w1 / A[36]) + A[68];
+    znam = fabs(dst);
+    if (dst >= -20.) znam = 20.;
+    c->xk1 = A[31] * pow(znam / 20., A[32]);
+    c->xk2 = A[33] * pow(znam / 20., A[34]);
+    c->scsy = A[27] * pow((20. / znam), A[28]) * c->xappa;
+    c->scpr = A[29] * pow((20. / znam), A[30]) * c->xappa;
+    const double dlp1 = pow((pdyn / 2.), A[20]);
+    const double dlp2 = pow((pdyn / 2.), A[21]);
+    c->tamp1 = A[1] + A[2] * dlp1 + A[3] * (A[38] * w1) / sqrt(w1 * w1 + A[38] * A[38]);
+    c->tamp2 = A[5] + A[6] * dlp2 + A[7] * (A[39] * w2) / sqrt(w2 * w2 + A[39] * A[39]);
+    c->a_src = A[9] + A[10] * (A[40] * w3) / sqrt(w3 * w3 + A[40] * A[40]) + A[11] * dst;
+    c->a_prc = A[12] + A[13] * (A[41] * w4) / sqrt(w4 * w4 + A[41] * A[41]) + A[14] * dst;
+    c->a_r11 = A[15] + A[16] * (A[42] * w5) / sqrt(w5 * w5 + A[42] * A[42]);
+    c->a_r21 = A[17] + A[18] * (A[43] * w6) / sqrt(w6 * w6 + A[43] * A[43]);
+    for (int l = 0; l < 25; l++) {
+        c->coef1[l] = U1[2 * l] + U1[2 * l + 1] * c->dx1;
+        c->coef2[l] = U2[2 * l] + U2[2 * l + 1] * c->dx2;
+    }
+    ts05_shield_amps(SH11, c->xk1 - 1.1, c->amp11);
+    ts05_shield_amps(SH21, c->xk2 - 1.0, c->amp21);
+    const double xs_sy = c->scsy - 1., xs_pr = c->scpr - 1.;
+    ts05_shield_amps(CSY, xs_sy, c->amp_sy);
+    ts05_shield_amps(CPR, xs_pr, c->amp_pr);
+    const double f1 = xs_sy + 1., f2 = xs_pr + 1.;
+    c->fac_sy = f1 * f1 * f1;
+    c->fac_pr = f2 * f2 * f2;
+}
+
+// Position-independent constants of the TS05 terms (shlcar3x3 ts05.c:137-217,
+// shlcar5x5 deformed.c:178-186, birk_shl birk_tot.c:379-390, rc_shield
+// full_rc.c:697-708, src_prc full_rc.c:91-92, r_s/theta_s birk_tot.c:294-308).
+static void ts05_tables(TS05Tables* t) {
+    using namespace ts05h;
+    const double PS[3] = {9.620648151, 6.082014949, 27.75216226};
+    const double R1 = 12.44199571, R2 = 5.122226936, R3 = 6.982039615;
+    const double r12 = 1. / (R1 * R1), r22 = 1. / (R2 * R2), r32_1 = 1. / (R3 * R3);
+    for (int i = 0; i < 3; i++) {
+        const double pp = 1. / (PS[i] * PS[i]);
+        t->s3_sq[3 * i] = sqrt(pp + r12);
+        t->s3_sq[3 * i + 1] = sqrt(pp + r22);
+        t->s3_sq[3 * i + 2] = sqrt(pp + r32_1);
+        t->s3_rsq[i] = 1. / t->s3_sq[3 * i + 2];
+    }
+    const double* U[2] = {U1, U2};
+    for (int m = 0; m < 2; m++) {
+        for (int i = 0; i < 5; i++) t->s5_rp[m][i] = 1. / U[m][50 + i];
+        for (int k = 0; k < 5; k++) t->s5_rr[m][k] = 1. / U[m][55 + k];
+        for (int i = 0; i < 5; i++)
+            for (int k = 0; k < 5; k++)
+                t->s5_sq[m][5 * i + k] = sqrt(t->s5_rp[m][i] * t->s5_rp[m][i] + t->s5_rr[m][k] * t->s5_rr[m][k]);
+    }
+    const double* SH[2] = {SH11, SH21};
+    const double* RC[2] = {CSY, CPR};
+    for (int m = 0; m < 2; m++) {
+        for (int j = 0; j < 3; j++) {
+            t->bs_p[m][j] = SH[m][72 + j];
+            t->bs_r[m][j] = SH[m][75 + j];
+            t->rc_p[m][j] = RC[m][72 + j];
+            t->rc_r[m][j] = RC[m][75 + j];
+        }
+        for (int j = 0; j < 3; j++) {
+            const double pb = 1. / (t->bs_p[m][j] * t->bs_p[m][j]);
+            const double pr = 1. / (t->rc_p[m][j] * t->rc_p[m][j]);
+            for (int k = 0; k < 3; k++) {
+                t->bs_sq[m][3 * j + k] = sqrt(pb + 1. / (t->bs_r[m][k] * t->bs_r[m][k]));
+                t->rc_sq[m][3 * j + k] = sqrt(pr + 1. / (t->rc_r[m][k] * t->rc_r[m][k]));
+            }
+        }
+    }
+    t->cphi = cos(A[37]);
+    t->sphi = sin(A[37]);
+    const double* AC[2] = {A11, A21};
+    for (int m = 0; m < 2; m++) {
+        for (int k = 0; k < 20; k++) t->rs_sq[m][k] = 0.;
+        for (int k = 10; k <= 15; k++) t->rs_sq[m][k] = AC[m][k] * AC[m][k];
+        for (int k = 26; k <= 29; k++) t->rs_sq[m][k - 10] = AC[m][k] * AC[m][k];
+    }
+}
+
 static void prepare_params(const cor_model_params* in, int32_t n, DevParams* out) {
     for (int32_t i = 0; i < n; i++) {
         memset(&out[i], 0, sizeof(DevParams));
         out[i].p = in[i];
         t96_prepare(in[i].parmod, &out[i].t96);
+        ts05_prepare(in[i].parmod, &out[i].ts05);
     }
 }
 
@@ -193,9 +313,16 @@ extern "C" int cor_ctx_create(int device, cor_ctx** out) {
         if (cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking) != cudaSuccess) { rc = COR_ERR_CUDA; break; }
         if (cudaMalloc(&ctx->queue, 256) != cudaSuccess) { rc = COR_ERR_NOMEM; break; }
         if (cudaMalloc(&ctx->counters, sizeof(cor_counters)) != cudaSuccess) { rc = COR_ERR_NOMEM; break; }
+        if (cudaMalloc(&ctx->gen, sizeof(GenCounters)) != cudaSuccess) { rc = COR_ERR_NOMEM; break; }
+        if (cudaMallocHost(&ctx->park_count_host, sizeof(unsigned int)) != cudaSuccess) { rc = COR_ERR_NOMEM; break; }
         T96Tables tt;
         t96_tables(&tt);
-        if (cudaMemcpyToSymbol(c_t96, &tt, sizeof tt) != cudaSuccess) { rc = COR_ERR_CUDA; break; }
+        TS05Tables t5;
+        ts05_tables(&t5);
+        const ModelOps* all[] = {&ops_igrf, &ops_igrf_t96, &ops_t96, &ops_igrf_ts05, &ops_ts05};
+        for (const ModelOps* o : all)
+            if (o->upload_tables(&tt, &t5) != cudaSuccess) rc = COR_ERR_CUDA;
+        if (rc != COR_OK) break;
     } while (0);
     if (rc != COR_OK) {
         cor_ctx_destroy(ctx);
@@ -209,7 +336,10 @@ extern "C" int cor_ctx_destroy(cor_ctx* ctx) {
     if (!ctx) return COR_OK;
     cudaSetDevice(ctx->device);
     if (ctx->stream) cudaStreamSynchronize(ctx->stream);
-    DevBuf* bufs[] = {&ctx->jobs, &ctx->trig, &ctx->offsets, &ctx->params, &ctx->sites, &ctx->status, &ctx->records};
+    DevBuf* bufs[] = {&ctx->jobs,   &ctx->trig,    &ctx->offsets, &ctx->params,  &ctx->sites,
+                      &ctx->status, &ctx->records, &ctx->park[0], &ctx->park[1]};
+    if (ctx->gen) cudaFree(ctx->gen);
+    if (ctx->park_count_host) cudaFreeHost(ctx->park_count_host);
     for (DevBuf* b : bufs)
         if (b->p) cudaFree(b->p);
     if (ctx->queue) cudaFree(ctx->queue);
@@ -305,36 +435,68 @@ static bool find_turn_threshold(double tu, double* thr) {
 // ---- dispatch over the compile-time model sets ---------------------------
 static bool model_set_ok(const cor_model_set& m) {
     const bool in_ok = m.internal_model == COR_INTERNAL_NONE || m.internal_model == COR_INTERNAL_SH;
-    const bool ex_ok = m.external_model == COR_EXTERNAL_NONE || m.external_model == COR_EXTERNAL_T96;
+    const bool ex_ok = m.external_model == COR_EXTERNAL_NONE || m.external_model == COR_EXTERNAL_T96 ||
+                       m.external_model == COR_EXTERNAL_TS05;
     const bool cr_ok = m.crustal_model == COR_CRUSTAL_NONE;
     const bool any = m.internal_model || m.external_model || m.crustal_model;
     return in_ok && ex_ok && cr_ok && any && m.reserved == 0;
 }
 
-// Calls fn.template operator()<ModelSet<...>>() for the compile-time set
-// matching m (model_set_ok(m) must hold).
-template <class F>
-static int dispatch_models(const cor_model_set& m, F&& fn) {
+// The compile-time model set matching m (model_set_ok(m) must hold).
+static const ModelOps* find_ops(const cor_model_set& m) {
     const int key = m.internal_model * 100 + m.external_model * 10 + m.crustal_model;
-    switch (key) {
-        case 100: return fn(ModelSet<1, 0, 0>{});
-        case 110: return fn(ModelSet<1, 1, 0>{});
-        case 10: return fn(ModelSet<0, 1, 0>{});
-        default: return COR_ERR_UNSUPPORTED;
-    }
+    static const ModelOps* const all[] = {&ops_igrf, &ops_igrf_t96, &ops_t96, &ops_igrf_ts05, &ops_ts05};
+    for (const ModelOps* o : all)
+        if (o->key == key) return o;
+    return nullptr;
 }
 
-template <class MS>
-static int launch_trace(cor_ctx* ctx, const TraceArgs& a, cudaStream_t s) {
+// Generations of the scan kernel.  Generation 0 drains the work queue; every
+// later one restores the trajectories the previous one parked, in a grid
+// sized to their count, so the survivors run in full warps.  Each live
+// trajectory count at least halves per generation (a warp parks with fewer
+// than half its lanes live, or when half the warps have parked), so the loop
+// is short; the last generations (or the 48th) run without parking.  The host
+// reads the parked count between generations, so this call synchronises the
+// stream once per generation.
+constexpr int kParkBelow = 16;
+constexpr int kMaxGenerations = 48;
+constexpr uint64_t kMinPark = 256;
+
+static int launch_trace(cor_ctx* ctx, const ModelOps* ops, TraceArgs a, cudaStream_t s) {
     int per_sm = 0;
-    CUDA_TRY(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, trace_kernel<MS>, 128, 0));
+    CUDA_TRY(ctx, ops->occupancy(&per_sm));
     if (per_sm < 1) per_sm = 1;
-    uint64_t blocks = (uint64_t)ctx->sms * (uint64_t)per_sm;
-    const uint64_t need = (a.n_traj + 127) / 128;
-    if (blocks > need) blocks = need;
-    if (blocks < 1) blocks = 1;
-    trace_kernel<MS><<<(unsigned)blocks, 128, 0, s>>>(a);
-    CUDA_TRY(ctx, cudaGetLastError());
+    const uint64_t cap_blocks = (uint64_t)ctx->sms * (uint64_t)per_sm;
+    const size_t park_bytes = sizeof(ParkedLane) * (size_t)cap_blocks * 128;
+    int rc;
+    if ((rc = ensure(ctx, ctx->park[0], park_bytes)) != COR_OK) return rc;
+    if ((rc = ensure(ctx, ctx->park[1], park_bytes)) != COR_OK) return rc;
+    uint64_t live = a.n_traj;
+    uint32_t n_restore = 0;
+    int cur = 0;
+    ctx->generations = 0;
+    for (int g = 0; g < kMaxGenerations && live > 0; g++) {
+        uint64_t blocks = (live + 127) / 128;
+        if (blocks > cap_blocks) blocks = cap_blocks;
+        a.restore = g == 0 ? nullptr : (const ParkedLane*)ctx->park[cur ^ 1].p;
+        a.n_restore = n_restore;
+        a.park = (ParkedLane*)ctx->park[cur].p;
+        a.gen = ctx->gen;
+        a.allow_park = (g + 1 < kMaxGenerations && live > kMinPark) ? 1 : 0;
+        a.park_below = kParkBelow;
+        a.launched_warps = (uint32_t)(blocks * 4);
+        CUDA_TRY(ctx, cudaMemsetAsync(ctx->gen, 0, sizeof(GenCounters), s));
+        CUDA_TRY(ctx, ops->launch_generation(a, (unsigned)blocks, s));
+        ctx->generations = g + 1;
+        if (!a.allow_park) break;
+        CUDA_TRY(ctx, cudaMemcpyAsync(ctx->park_count_host, &ctx->gen->park_count, sizeof(unsigned int),
+                                      cudaMemcpyDeviceToHost, s));
+        CUDA_TRY(ctx, cudaStreamSynchronize(s));
+        n_restore = *ctx->park_count_host;
+        live = n_restore;
+        cur ^= 1;
+    }
     return COR_OK;
 }
 
@@ -342,7 +504,9 @@ static int launch_scan(cor_ctx* ctx, const TraceArgs& a, cor_model_set models, c
     CUDA_TRY(ctx, cudaMemsetAsync(a.queue, 0, sizeof(unsigned long long), s));
     CUDA_TRY(ctx, cudaMemsetAsync(a.counters, 0, sizeof(cor_counters), s));
     if (a.n_traj > 0) {
-        const int rc = dispatch_models(models, [&](auto ms) { return launch_trace<decltype(ms)>(ctx, a, s); });
+        const ModelOps* ops = find_ops(models);
+        if (!ops) return fail(ctx, COR_ERR_UNSUPPORTED, "model set not available");
+        const int rc = launch_trace(ctx, ops, a, s);
         if (rc != COR_OK) return rc;
     }
     if (a.n_jobs > 0) {
@@ -525,14 +689,9 @@ extern "C" int cor_field_batch(cor_ctx* ctx, cor_model_set models, const cor_mod
         free(hp);
         cudaMemcpyAsync(dpos, gsm_pos, sizeof(double) * 3 * (size_t)n, cudaMemcpyHostToDevice, s);
         if (param_index) cudaMemcpyAsync(didx, param_index, sizeof(int32_t) * (size_t)n, cudaMemcpyHostToDevice, s);
-        const int threads = 128;
-        const unsigned blocks = (unsigned)((n + threads - 1) / threads);
         const CrustalTables crust{ctx->crust_g, ctx->crust_h, ctx->crust_nmax};
-        dispatch_models(models, [&](auto ms) {
-            field_kernel<decltype(ms)><<<blocks, threads, 0, s>>>((const DevParams*)dp, n_params, (const int32_t*)didx,
-                                                                   (const double*)dpos, n, (double*)dout, crust);
-            return COR_OK;
-        });
+        find_ops(models)->launch_field((const DevParams*)dp, n_params, (const int32_t*)didx, (const double*)dpos, n,
+                                       (double*)dout, crust, s);
         cudaMemcpyAsync(geo_field, dout, sizeof(double) * 3 * (size_t)n, cudaMemcpyDeviceToHost, s);
         cudaError_t e = cudaStreamSynchronize(s);
         if (e == cudaSuccess) e = cudaGetLastError();
@@ -543,4 +702,49 @@ extern "C" int cor_field_batch(cor_ctx* ctx, cor_model_set models, const cor_mod
     if (dout) cudaFree(dout);
     if (didx) cudaFree(didx);
     return rc;
+}
+
+// ---- FP64 peak probe -------------------------------------------------------
+// Eight independent DFMA chains per thread, all operands in registers.
+__global__ void fp64_peak_kernel(double* out, int iters, double s) {
+    double a[8];
+#pragma unroll
+    for (int c = 0; c < 8; ++c) a[c] = 1.0 + 1e-9 * (threadIdx.x + c);
+    for (int i = 0; i < iters; ++i) {
+#pragma unroll
+        for (int c = 0; c < 8; ++c) a[c] = __fma_rn(a[c], s, 1e-12);
+    }
+    double t = 0.;
+#pragma unroll
+    for (int c = 0; c < 8; ++c) t += a[c];
+    out[blockIdx.x * blockDim.x + threadIdx.x] = t;
+}
+
+extern "C" int cor_probe_fp64_peak(cor_ctx* ctx, double* flops_per_s) {
+    if (!ctx || !flops_per_s) return COR_ERR_INVALID;
+    CUDA_TRY(ctx, cudaSetDevice(ctx->device));
+    const int blocks = ctx->sms * 8, threads = 256, iters = 4000;
+    double* out = nullptr;
+    CUDA_TRY(ctx, cudaMalloc(&out, sizeof(double) * (size_t)blocks * threads));
+    cudaEvent_t e0, e1;
+    cudaEventCreate(&e0);
+    cudaEventCreate(&e1);
+    fp64_peak_kernel<<<blocks, threads, 0, ctx->stream>>>(out, 100, 0.999999);
+    float best = 1e30f;
+    for (int r = 0; r < 3; r++) {
+        cudaEventRecord(e0, ctx->stream);
+        fp64_peak_kernel<<<blocks, threads, 0, ctx->stream>>>(out, iters, 0.999999);
+        cudaEventRecord(e1, ctx->stream);
+        cudaEventSynchronize(e1);
+        float ms = 0.f;
+        cudaEventElapsedTime(&ms, e0, e1);
+        if (ms < best) best = ms;
+    }
+    cudaError_t e = cudaGetLastError();
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    cudaFree(out);
+    if (e != cudaSuccess) return fail(ctx, COR_ERR_CUDA, "fp64 probe: %s", cudaGetErrorString(e));
+    *flops_per_s = 2.0 * 8.0 * iters * (double)blocks * threads / (best * 1e-3);
+    return COR_OK;
 }

@@ -4,6 +4,7 @@
 
 #include "cor_device.cuh"
 #include "t96.cuh"
+#include "ts05.cuh"
 
 namespace cor {
 
@@ -22,6 +23,7 @@ struct ModelSet {
 struct DevParams {
     cor_model_params p;
     T96Cond t96;
+    TS05Cond ts05;
 };
 
 // Device tables of the crustal model (packed lower triangle) and its
@@ -32,7 +34,6 @@ struct CrustalTables {
     int nmax;
 };
 
-__device__ Vec3 ts05_gsm(const double* __restrict__ parmod, const Vec3 x);
 __device__ Vec3 chaos_geo(const Vec3 x, const CrustalTables& t);
 
 // GSM position in metres -> GEO field in nT.
@@ -57,7 +58,7 @@ __device__ __forceinline__ Vec3 calculate_field(const Vec3 gsm_pos, const DevPar
         tot.y += b.y;
         tot.z += b.z;
     } else if (MS::external == COR_EXTERNAL_TS05) {
-        const Vec3 b = ts05_gsm(p->parmod, pos);  // ts05_calc, src/models.c:162-169
+        const Vec3 b = ts05_field(dp->ts05, pos);  // ts05_calc, src/models.c:162-169
         tot.x += b.x;
         tot.y += b.y;
         tot.z += b.z;

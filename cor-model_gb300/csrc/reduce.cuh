@@ -1,0 +1,59 @@
+// reduce.cuh -- per-scan reduction of the trajectory classes to P(S), P(C), P(M).
+#pragma once
+
+#include "../../include/cor_trace.h"
+
+namespace cor {
+
+// Per-scan reduction, src/trajectory.c:156-160, one warp per scan.  The
+// reference's fmin/fmax over thread_rig = rig + i*del are taken through the
+// extreme indices (thread_rig increases with i), so the result does not
+// depend on the order in which trajectories finished.
+__global__ void reduce_kernel(const cor_scan_job* __restrict__ jobs, const uint64_t* __restrict__ off,
+                              int n_jobs, const uint8_t* __restrict__ status, cor_site_result* __restrict__ out) {
+    const int w = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int lane = threadIdx.x & 31;
+    if (w >= n_jobs) return;
+    const uint64_t b = off[w], e = off[w + 1];
+    int imin_allowed = 0x7fffffff, imax1 = -1, imax2 = -1, nza = 0;
+    for (uint64_t t = b + lane; t < e; t += 32) {
+        const int i = (int)(t - b);
+        const int st = status[t];
+        if (st == COR_TRAJ_ALLOWED) {
+            imin_allowed = min(imin_allowed, i);
+        } else if (st == COR_TRAJ_REENTRY || st == COR_TRAJ_SUPERLUM) {
+            imax1 = max(imax1, i);
+            nza++;
+        } else {
+            imax2 = max(imax2, i);
+            nza++;
+        }
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        imin_allowed = min(imin_allowed, __shfl_xor_sync(0xffffffffu, imin_allowed, o));
+        imax1 = max(imax1, __shfl_xor_sync(0xffffffffu, imax1, o));
+        imax2 = max(imax2, __shfl_xor_sync(0xffffffffu, imax2, o));
+        nza += __shfl_xor_sync(0xffffffffu, nza, o);
+    }
+    if (lane == 0) {
+        const cor_scan_job job = jobs[w];
+        double rmi = job.rk, rmx1 = 0., rmx2 = 0.;
+        if (imin_allowed != 0x7fffffff) rmi = fmin(rmi, job.rig + imin_allowed * job.del);
+        if (imax1 >= 0) rmx1 = fmax(rmx1, job.rig + imax1 * job.del);
+        if (imax2 >= 0) rmx2 = fmax(rmx2, job.rig + imax2 * job.del);
+        double rmx = fmax(rmx1, rmx2);
+        const double zan = nza - (rmi - job.rig) / job.del;
+        const double rms = rmi + zan * job.del;
+        rmx = rmx + job.del;
+        cor_site_result r;
+        r.r_lower = rmi;
+        r.r_upper = rmx;
+        r.r_cutoff = rms;
+        r.n_forbidden = nza;
+        r.n_traj = (int32_t)(e - b);
+        out[w] = r;
+    }
+}
+
+}  // namespace cor

@@ -40,7 +40,7 @@ struct T96Tables {
     double r2s_k[8];       // r2sheet sqrt(-2e * -a) factors (5) and pow(d, 4) (3)
 };
 
-__constant__ T96Tables c_t96;
+static __constant__ T96Tables c_t96;
 
 // ---- shield amplitude/scale tables (:273-321, :1030-1263) ----------------
 // 3x3 shields: per table {P[3], R[3], amp[9] = A[2j] + A[2j+1]}.
@@ -52,11 +52,11 @@ __constant__ T96Tables c_t96;
 #define SHL_R2 22.50403727, 23.41617329, 48.48140573
 #define RECIP3(a, b, c) 1.0 / (a), 1.0 / (b), 1.0 / (c)
 #define RECIP3_(...) RECIP3(__VA_ARGS__)
-__constant__ double c_shl_p[3][3] = {{SHL_P0}, {SHL_P1}, {SHL_P2}};
-__constant__ double c_shl_rp[3][3] = {{RECIP3_(SHL_P0)}, {RECIP3_(SHL_P1)}, {RECIP3_(SHL_P2)}};
-__constant__ double c_shl_r[3][3] = {{SHL_R0}, {SHL_R1}, {SHL_R2}};
-__constant__ double c_shl_rr[3][3] = {{RECIP3_(SHL_R0)}, {RECIP3_(SHL_R1)}, {RECIP3_(SHL_R2)}};
-__constant__ double c_shl_a[3][18] = {
+static __constant__ double c_shl_p[3][3] = {{SHL_P0}, {SHL_P1}, {SHL_P2}};
+static __constant__ double c_shl_rp[3][3] = {{RECIP3_(SHL_P0)}, {RECIP3_(SHL_P1)}, {RECIP3_(SHL_P2)}};
+static __constant__ double c_shl_r[3][3] = {{SHL_R0}, {SHL_R1}, {SHL_R2}};
+static __constant__ double c_shl_rr[3][3] = {{RECIP3_(SHL_R0)}, {RECIP3_(SHL_R1)}, {RECIP3_(SHL_R2)}};
+static __constant__ double c_shl_a[3][18] = {
     {-3.087699646, 3.516259114, 18.81380577, -13.95772338, -5.497076303, 0.1712890838, 2.392629189, -2.728020808,
      -14.79349936, 11.08738083, 4.388174084, 0.2492163197E-01, 0.7030375685, -.7966023165, -3.835041334, 2.642228681,
      -0.2405352424, -0.7297705678},

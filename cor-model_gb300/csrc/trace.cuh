@@ -22,6 +22,25 @@ struct JobTrig {
     double st1, ct1, sp1, cp1;
 };
 
+// A trajectory in flight, parked between two generations of the kernel
+// (bitwise copy of the lane state, so a parked and restored trajectory
+// continues exactly as if it had not moved).
+struct ParkedLane {
+    double pos[3], vel[3], field[3], gsm[3];
+    double b, v, time, alength, rig;
+    unsigned long long traj;
+    int32_t job;
+    uint32_t step, trials;
+    int32_t nk0;
+};
+
+// Per-generation scratch counters (zeroed before each generation).
+struct GenCounters {
+    unsigned long long restore_cursor;  // next parked trajectory to restore
+    unsigned int park_count;            // trajectories parked by this generation
+    unsigned int parked_warps;          // warps that have parked and exited
+};
+
 struct TraceArgs {
     const cor_scan_job* jobs;
     const JobTrig* trig;
@@ -41,6 +60,14 @@ struct TraceArgs {
     unsigned long long* queue;     // scratch: next trajectory index
     cor_counters* counters;
     CrustalTables crust;
+    // compaction between generations
+    const ParkedLane* restore;     // trajectories parked by the previous generation
+    uint32_t n_restore;
+    ParkedLane* park;              // where this generation parks (capacity = launched threads)
+    GenCounters* gen;
+    int allow_park;                // 0 in the last generation
+    int park_below;                // a warp parks when fewer lanes than this are live
+    uint32_t launched_warps;
 };
 
 __device__ __forceinline__ int find_job(const uint64_t* __restrict__ off, int n_jobs, uint64_t t) {
@@ -62,20 +89,47 @@ struct Lane {
     uint64_t traj;
     uint32_t step, trials;
     int nk0;
+    int32_t job_index;
 };
 
-// Claims the next trajectory index for every lane in `want` with one
-// atomic per warp.  Returns this lane's index (>= n_traj when the queue is
-// drained).
+__device__ __forceinline__ void lane_park(const Lane& L, ParkedLane& o) {
+    o.pos[0] = L.pos.x; o.pos[1] = L.pos.y; o.pos[2] = L.pos.z;
+    o.vel[0] = L.vel.x; o.vel[1] = L.vel.y; o.vel[2] = L.vel.z;
+    o.field[0] = L.field.x; o.field[1] = L.field.y; o.field[2] = L.field.z;
+    o.gsm[0] = L.gsm.x; o.gsm[1] = L.gsm.y; o.gsm[2] = L.gsm.z;
+    o.b = L.b; o.v = L.v; o.time = L.time; o.alength = L.alength; o.rig = L.rig;
+    o.traj = L.traj;
+    o.job = L.job_index;
+    o.step = L.step; o.trials = L.trials; o.nk0 = L.nk0;
+}
+
+__device__ __forceinline__ void lane_restore(Lane& L, const ParkedLane& o, const cor_scan_job* jobs,
+                                             const DevParams* params) {
+    L.pos = {o.pos[0], o.pos[1], o.pos[2]};
+    L.vel = {o.vel[0], o.vel[1], o.vel[2]};
+    L.field = {o.field[0], o.field[1], o.field[2]};
+    L.gsm = {o.gsm[0], o.gsm[1], o.gsm[2]};
+    L.b = o.b; L.v = o.v; L.time = o.time; L.alength = o.alength; L.rig = o.rig;
+    L.traj = o.traj;
+    L.job_index = o.job;
+    L.job = jobs + o.job;
+    L.par = params + L.job->param_index;
+    L.step = o.step; L.trials = o.trials; L.nk0 = o.nk0;
+}
+
+// Claims the next index of a queue for every lane in `want` with one atomic
+// per warp; called by all 32 lanes of a warp together.  Returns this lane's
+// index (the caller compares it with the queue length).
 __device__ __forceinline__ uint64_t queue_pop(unsigned long long* q, bool want) {
-    const unsigned mask = __ballot_sync(__activemask(), want);
-    if (!want) return ~0ull;
-    const int leader = __ffs(mask) - 1;
+    const unsigned mask = __ballot_sync(0xffffffffu, want);
     const int lane = threadIdx.x & 31;
     unsigned long long base = 0;
-    if (lane == leader) base = atomicAdd(q, (unsigned long long)__popc(mask));
-    base = __shfl_sync(mask, base, leader);
-    return base + __popc(mask & ((1u << lane) - 1u));
+    if (mask) {
+        const int leader = __ffs(mask) - 1;
+        if (lane == leader) base = atomicAdd(q, (unsigned long long)__popc(mask));
+        base = __shfl_sync(0xffffffffu, base, leader);
+    }
+    return want ? base + __popc(mask & ((1u << lane) - 1u)) : ~0ull;
 }
 
 // Start of one trajectory, src/trajectory.c:13-44 (the field is evaluated
@@ -97,6 +151,7 @@ __device__ __forceinline__ void lane_init(Lane& L, const TraceArgs& a, uint64_t 
     const cor_scan_job* job = a.jobs + j;
     const JobTrig tg = a.trig[j];
     L.job = job;
+    L.job_index = j;
     L.par = a.params + job->param_index;
     L.traj = a.offsets[j] + i;
     const double rig = job->rig + (int)i * job->del;
@@ -222,11 +277,20 @@ __device__ __forceinline__ void warp_add_u64(unsigned long long* dst, unsigned l
     if ((threadIdx.x & 31) == 0 && v) atomicAdd(dst, v);
 }
 
+// One generation of the scan.  All 32 lanes of a warp stay in the loop
+// until the warp leaves it as a whole (every exit below is warp-uniform).
+// A lane with no trajectory takes the next parked one, else the next queue
+// index.  Once the queue is drained, a warp whose live lanes fall below
+// park_below -- or any warp, once half of the generation's warps have
+// parked -- writes its live trajectories to the park list and leaves; the
+// host then launches the next generation sized to the parked count, which
+// restores them densely (the regroup step).
 template <class MS>
 __global__ void __launch_bounds__(128) trace_kernel(const TraceArgs a) {
     Lane L;
     bool has = false, done = false;
     unsigned long long n_steps = 0, n_trials = 0, n_traj = 0, n_wd = 0;
+    const int lane = threadIdx.x & 31;
     for (;;) {
         bool need_field = false;
         if (has) {
@@ -242,7 +306,16 @@ __global__ void __launch_bounds__(128) trace_kernel(const TraceArgs a) {
                 has = false;
             }
         }
-        const bool want = !has && !done;
+        __syncwarp();
+        bool want = !has && !done;
+        if (a.n_restore) {
+            const uint64_t r = queue_pop(&a.gen->restore_cursor, want);
+            if (want && r < a.n_restore) {
+                lane_restore(L, a.restore[r], a.jobs, a.params);
+                has = true;
+                want = false;
+            }
+        }
         const uint64_t t = queue_pop(a.queue, want);
         if (want) {
             if (t < a.n_traj) {
@@ -254,6 +327,33 @@ __global__ void __launch_bounds__(128) trace_kernel(const TraceArgs a) {
             }
         }
         if (__all_sync(0xffffffffu, done)) break;
+        if (a.allow_park && __any_sync(0xffffffffu, done)) {
+            const unsigned live = __ballot_sync(0xffffffffu, has);
+            bool park = __popc(live) < a.park_below;
+            if (!park) {
+                unsigned pw = 0;
+                if (lane == 0) pw = *((volatile unsigned int*)&a.gen->parked_warps);
+                pw = __shfl_sync(0xffffffffu, pw, 0);
+                park = 2u * pw >= a.launched_warps;
+            }
+            if (park) {
+                // need_field lanes were just initialised or advanced: their
+                // field is evaluated by the next generation's first pass.
+                const int leader = __ffs(live) - 1;
+                unsigned base = 0;
+                if (live && lane == leader) base = atomicAdd(&a.gen->park_count, (unsigned)__popc(live));
+                base = __shfl_sync(0xffffffffu, base, live ? leader : 0);
+                if (has) {
+                    if (need_field) {
+                        L.field = calculate_field<MS>(L.gsm, L.par, a.crust);
+                        L.b = 1.E-09 * sqrt(L.field.x * L.field.x + L.field.y * L.field.y + L.field.z * L.field.z);
+                    }
+                    lane_park(L, a.park[base + __popc(live & ((1u << lane) - 1u))]);
+                }
+                if (lane == 0) atomicAdd(&a.gen->parked_warps, 1u);
+                break;
+            }
+        }
         if (need_field) {
             L.field = calculate_field<MS>(L.gsm, L.par, a.crust);
             L.b = 1.E-09 * sqrt(L.field.x * L.field.x + L.field.y * L.field.y + L.field.z * L.field.z);
@@ -263,57 +363,6 @@ __global__ void __launch_bounds__(128) trace_kernel(const TraceArgs a) {
     warp_add_u64(reinterpret_cast<unsigned long long*>(&a.counters->trials), n_trials);
     warp_add_u64(reinterpret_cast<unsigned long long*>(&a.counters->trajectories), n_traj);
     warp_add_u64(reinterpret_cast<unsigned long long*>(&a.counters->watchdog), n_wd);
-}
-
-// Per-scan reduction, src/trajectory.c:156-160, one warp per scan.  The
-// reference's fmin/fmax over thread_rig = rig + i*del are taken through the
-// extreme indices (thread_rig increases with i), so the result does not
-// depend on the order in which trajectories finished.
-__global__ void reduce_kernel(const cor_scan_job* __restrict__ jobs, const uint64_t* __restrict__ off,
-                              int n_jobs, const uint8_t* __restrict__ status, cor_site_result* __restrict__ out) {
-    const int w = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-    const int lane = threadIdx.x & 31;
-    if (w >= n_jobs) return;
-    const uint64_t b = off[w], e = off[w + 1];
-    int imin_allowed = 0x7fffffff, imax1 = -1, imax2 = -1, nza = 0;
-    for (uint64_t t = b + lane; t < e; t += 32) {
-        const int i = (int)(t - b);
-        const int st = status[t];
-        if (st == COR_TRAJ_ALLOWED) {
-            imin_allowed = min(imin_allowed, i);
-        } else if (st == COR_TRAJ_REENTRY || st == COR_TRAJ_SUPERLUM) {
-            imax1 = max(imax1, i);
-            nza++;
-        } else {
-            imax2 = max(imax2, i);
-            nza++;
-        }
-    }
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) {
-        imin_allowed = min(imin_allowed, __shfl_xor_sync(0xffffffffu, imin_allowed, o));
-        imax1 = max(imax1, __shfl_xor_sync(0xffffffffu, imax1, o));
-        imax2 = max(imax2, __shfl_xor_sync(0xffffffffu, imax2, o));
-        nza += __shfl_xor_sync(0xffffffffu, nza, o);
-    }
-    if (lane == 0) {
-        const cor_scan_job job = jobs[w];
-        double rmi = job.rk, rmx1 = 0., rmx2 = 0.;
-        if (imin_allowed != 0x7fffffff) rmi = fmin(rmi, job.rig + imin_allowed * job.del);
-        if (imax1 >= 0) rmx1 = fmax(rmx1, job.rig + imax1 * job.del);
-        if (imax2 >= 0) rmx2 = fmax(rmx2, job.rig + imax2 * job.del);
-        double rmx = fmax(rmx1, rmx2);
-        const double zan = nza - (rmi - job.rig) / job.del;
-        const double rms = rmi + zan * job.del;
-        rmx = rmx + job.del;
-        cor_site_result r;
-        r.r_lower = rmi;
-        r.r_upper = rmx;
-        r.r_cutoff = rms;
-        r.n_forbidden = nza;
-        r.n_traj = (int32_t)(e - b);
-        out[w] = r;
-    }
 }
 
 template <class MS>

@@ -199,9 +199,12 @@ int cor_upload_params(cor_ctx *ctx, const cor_model_params *params, int32_t n_pa
 /* Same scan with every buffer already in device memory (jobs, trig from
  * cor_prepare_trig, offsets from cor_batch_count, sites, status, records) and
  * the parameter blocks of the last cor_upload_params; `stream` is a
- * cudaStream_t (NULL = the legacy default stream).  Returns after the
- * launches are queued; counters go to the device buffer `counters_dev` (a
- * cor_counters; NULL = internal). */
+ * cudaStream_t (NULL = the legacy default stream).  The scan runs in
+ * generations: between two of them the host reads how many trajectories the
+ * kernel parked for regrouping, so the call synchronises `stream` a few
+ * times and returns with the last generation and the reduction queued.
+ * Counters go to the device buffer `counters_dev` (a cor_counters; NULL =
+ * internal). */
 int cor_trace_batch_device(cor_ctx *ctx,
                            const cor_scan_job *jobs_dev, const cor_job_trig *trig_dev,
                            int32_t n_jobs, const uint64_t *offsets_dev, uint64_t n_trajectories,
@@ -231,6 +234,12 @@ int cor_internal_setup(const char *version, const int32_t time[7], cor_model_par
  * The reference leaves these uninitialised in that case (src/main.c:51);
  * here they are computed from the date with the IGRF-14 dipole. */
 int cor_gsm_setup(const int32_t time[7], cor_model_params *out);
+
+/* ---- measurement -------------------------------------------------------- */
+/* Measures the device's FP64 FMA throughput with a register-resident DFMA
+ * loop on every SM (an FMA counts as 2 flops) and writes flops/s.  The
+ * denominator of the scan's FP64 roofline; no counterpart in the reference. */
+int cor_probe_fp64_peak(cor_ctx *ctx, double *flops_per_s);
 
 #ifdef __cplusplus
 }

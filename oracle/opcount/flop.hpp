@@ -1,0 +1,79 @@
+// flop.hpp -- TEST INFRASTRUCTURE: an operation-counting stand-in for double.
+//
+// Force-included (g++ -include) before the oracle's C sources compiled as
+// C++: every `double` in them becomes flop_t, whose arithmetic counts one
+// operation per + - * / and sqrt, and one transcendental per libm call
+// (exp, log, sin, cos, tan, atan, atan2, asin, pow, fmod).  Comparisons,
+// negation, fabs, fmin/fmax and conversions are free.  Values are computed
+// in plain double, so results stay identical to the normal build.
+#pragma once
+#include <math.h>
+#include <pthread.h>
+#include <stddef.h>
+#include <stdint.h>
+#include <stdio.h>
+#include <stdlib.h>
+#include <string.h>
+
+#include <atomic>
+#include <cmath>
+#include <cstddef>
+#include <cstdlib>
+
+struct FlopTally {
+    uint64_t ops = 0, trans = 0;
+};
+extern thread_local FlopTally g_tally;
+
+struct flop_t {
+    double v;
+    flop_t() = default;
+    constexpr flop_t(double x) : v(x) {}
+    constexpr flop_t(float x) : v(x) {}
+    constexpr flop_t(int x) : v(x) {}
+    constexpr flop_t(unsigned x) : v(x) {}
+    constexpr flop_t(long x) : v((double)x) {}
+    constexpr flop_t(unsigned long x) : v((double)x) {}
+    constexpr flop_t(long long x) : v((double)x) {}
+    constexpr flop_t(unsigned long long x) : v((double)x) {}
+    explicit operator int() const { return (int)v; }
+    explicit operator long() const { return (long)v; }
+    explicit operator long long() const { return (long long)v; }
+    explicit operator unsigned long() const { return (unsigned long)v; }
+    explicit operator double() const { return v; }
+    explicit operator bool() const { return v != 0.0; }
+    flop_t operator-() const { return flop_t(-v); }
+    flop_t operator+() const { return *this; }
+    flop_t& operator+=(flop_t o) { g_tally.ops++; v = v + o.v; return *this; }
+    flop_t& operator-=(flop_t o) { g_tally.ops++; v = v - o.v; return *this; }
+    flop_t& operator*=(flop_t o) { g_tally.ops++; v = v * o.v; return *this; }
+    flop_t& operator/=(flop_t o) { g_tally.ops++; v = v / o.v; return *this; }
+};
+static_assert(sizeof(flop_t) == 8, "layout must match double");
+
+inline flop_t operator+(flop_t a, flop_t b) { g_tally.ops++; return flop_t(a.v + b.v); }
+inline flop_t operator-(flop_t a, flop_t b) { g_tally.ops++; return flop_t(a.v - b.v); }
+inline flop_t operator*(flop_t a, flop_t b) { g_tally.ops++; return flop_t(a.v * b.v); }
+inline flop_t operator/(flop_t a, flop_t b) { g_tally.ops++; return flop_t(a.v / b.v); }
+inline bool operator<(flop_t a, flop_t b) { return a.v < b.v; }
+inline bool operator>(flop_t a, flop_t b) { return a.v > b.v; }
+inline bool operator<=(flop_t a, flop_t b) { return a.v <= b.v; }
+inline bool operator>=(flop_t a, flop_t b) { return a.v >= b.v; }
+inline bool operator==(flop_t a, flop_t b) { return a.v == b.v; }
+inline bool operator!=(flop_t a, flop_t b) { return a.v != b.v; }
+
+inline flop_t sqrt(flop_t a) { g_tally.ops++; return flop_t(std::sqrt(a.v)); }
+inline flop_t fabs(flop_t a) { return flop_t(std::fabs(a.v)); }
+inline flop_t fmin(flop_t a, flop_t b) { return flop_t(std::fmin(a.v, b.v)); }
+inline flop_t fmax(flop_t a, flop_t b) { return flop_t(std::fmax(a.v, b.v)); }
+inline flop_t round(flop_t a) { return flop_t(std::round(a.v)); }
+#define FLOP_T1(fn) \
+    inline flop_t fn(flop_t a) { g_tally.trans++; return flop_t(std::fn(a.v)); }
+FLOP_T1(exp) FLOP_T1(log) FLOP_T1(sin) FLOP_T1(cos) FLOP_T1(tan) FLOP_T1(atan) FLOP_T1(asin)
+#undef FLOP_T1
+inline flop_t atan2(flop_t a, flop_t b) { g_tally.trans++; return flop_t(std::atan2(a.v, b.v)); }
+inline flop_t pow(flop_t a, flop_t b) { g_tally.trans++; return flop_t(std::pow(a.v, b.v)); }
+inline flop_t fmod(flop_t a, flop_t b) { g_tally.trans++; return flop_t(std::fmod(a.v, b.v)); }
+inline int isfinite(flop_t a) { return std::isfinite(a.v); }
+
+#define double flop_t

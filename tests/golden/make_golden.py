@@ -228,10 +228,10 @@ def make_scan0() -> dict:
             "sites": recs}
 
 
-def make_scan_ext(kind: str) -> dict:
+def make_scan_ext(kind: str, n_sites: int = 200, rig: float = 0.05, dele: float = 0.05) -> dict:
     rng = np.random.default_rng(7 if kind == "t96" else 11)
-    lats = rng.choice(np.arange(-90, 91, 5), 10)
-    lons = rng.choice(np.arange(0, 360, 5), 10)
+    lats = rng.choice(np.arange(-90, 91, 5), n_sites)
+    lons = rng.choice(np.arange(0, 360, 5), n_sites)
     sites = [(float(a), float(o), float(a), float(o)) for a, o in zip(lats, lons)]
     t7 = [2020, 6, 21, 173, 12, 0, 0]
     if kind == "t96":
@@ -242,9 +242,9 @@ def make_scan_ext(kind: str) -> dict:
         ext = ["-20 2 0 -1", "1 1 1 1 1 1"]              # + W1..W6 (src/io.c:98-113)
         args = ["-i", "igrf14", "-e", "ts05"]
         pm = TS05_PARMOD
-    recs = run_scan_set(sites, 0.01, 20.0, 0.01, t7, args, ext_lines=ext, keep_text={0})
-    return {"config": f"IGRF-14 + {kind.upper()} at 2020-06-21 12 UT, vertical, 20 km, 20 -> 0.01 GV by 0.01",
-            "rig": 0.01, "rk": 20.0, "del": 0.01, "time": t7, "model": "igrf14", "external": kind,
+    recs = run_scan_set(sites, rig, 20.0, dele, t7, args, ext_lines=ext, keep_text={0})
+    return {"config": f"IGRF-14 + {kind.upper()} at 2020-06-21 12 UT, vertical, 20 km, 20 -> {rig} GV by {dele}",
+            "rig": rig, "rk": 20.0, "del": dele, "time": t7, "model": "igrf14", "external": kind,
             "parmod": pm, "sites": recs}
 
 

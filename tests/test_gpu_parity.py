@@ -159,7 +159,7 @@ def _scan_golden(name, models):
 
 
 def test_scan_t96_matches_reference(ctx):
-    """IGRF-14 + T96, 10 sites x 2000 rigidities against the reference's own scans:
+    """IGRF-14 + T96, 200 sites x 400 rigidities against the reference's own scans:
     allowed/forbidden flags agree on >= 99.9% of trajectories, every
     disagreement lies inside the scan's penumbra [P(S), P(C)], and P(S), P(C),
     P(M) agree within one rigidity step at >= 99.5% of sites."""
@@ -188,7 +188,7 @@ def test_scan_t96_matches_reference(ctx):
     print(f"T96 scan: flag agreement {n_agree / n_traj:.5f}, sites within one step {sites_ok}/{len(g['sites'])}")
     assert n_agree / n_traj >= 0.999
     assert not outside, outside[:10]
-    assert sites_ok / len(g["sites"]) >= 0.995 or len(g["sites"]) - sites_ok <= 0
+    assert sites_ok / len(g["sites"]) >= 0.995
 
 
 def test_scan_t96_equals_oracle_statistics(ctx):
@@ -196,7 +196,7 @@ def test_scan_t96_equals_oracle_statistics(ctx):
     outside the penumbra and the same total work to within a few percent."""
     models = ct.model_set(ct.INTERNAL_SH, ct.EXTERNAL_T96)
     g, p, jobs = _scan_golden("scan_t96.json", models)
-    jobs = jobs[:3]
+    jobs = jobs[:16]
     gpu = ctx.trace_batch(jobs, p, models=models)
     cpu = pyoracle.scan_batch(jobs, p, models=models, threads=8)
     agree = np.mean(gpu.status == cpu.status)
@@ -204,3 +204,86 @@ def test_scan_t96_equals_oracle_statistics(ctx):
     print(f"T96 vs oracle: status agreement {agree:.5f}, step ratio {ratio:.4f}")
     assert agree >= 0.999
     assert abs(ratio - 1.0) < 0.05
+
+
+# ---- TS05 -----------------------------------------------------------------
+# TS05 takes central differences with steps of 1e-6 and 1e-4 (birk_tot.c:267-275,
+# full_rc.c:119-146), which turn one ulp of difference in a transcendental into
+# up to ~1e-8 of relative change in the field.  Its tolerance is therefore the
+# point's own conditioning: TS05_RTOL_K times the relative change the oracle
+# shows for a one-ulp nudge of the position, and at least FIELD_RTOL.
+TS05_RTOL_K = 64.0
+
+
+def _ts05_sensitivity(pts, pm):
+    lib = pyoracle.load()
+    b0, b1 = np.zeros(3), np.zeros(3)
+    sens = np.zeros(len(pts))
+    for i, (x, y, z) in enumerate(pts):
+        lib.orc_ts05_gsm(pm.ctypes.data, x, y, z, b0[0:].ctypes.data, b0[1:].ctypes.data, b0[2:].ctypes.data)
+        worst = 0.0
+        for d in range(3):
+            q = [x, y, z]
+            q[d] = np.nextafter(q[d], np.inf)
+            lib.orc_ts05_gsm(pm.ctypes.data, q[0], q[1], q[2], b1[0:].ctypes.data, b1[1:].ctypes.data, b1[2:].ctypes.data)
+            worst = max(worst, np.linalg.norm(b1 - b0) / max(np.linalg.norm(b0), 1e-300))
+        sens[i] = worst
+    return sens
+
+
+def test_field_ts05_kats(ctx):
+    g = golden("field_kats.json")["ts05_gsm"]
+    pm = unhex(g["parmod"])
+    p = ct.internal_setup("igrf14", [2020, 1, 1, 1, 0, 0, 0], parmod=pm)
+    p["a1"][0], p["a2"][0], p["a3"][0] = [1, 0, 0], [0, 1, 0], [0, 0, 1]
+    pts = unhex(g["points"]).reshape(-1, 3)
+    want = unhex(g["b"]).reshape(-1, 3)
+    got = ctx.field_batch(pts * ct.DEF_RE, p, models=ct.model_set(ct.INTERNAL_NONE, ct.EXTERNAL_TS05))
+    exact = np.all(((pts * ct.DEF_RE) / ct.DEF_RE) == pts, axis=1)
+    err = _rel_err(got[exact], want[exact])
+    tol = np.maximum(FIELD_RTOL, TS05_RTOL_K * _ts05_sensitivity(pts[exact], pm))
+    print(f"ts05 KAT: {exact.sum()} points, max rel err {err.max():.3e}, median {np.median(err):.3e}, "
+          f"points above 1e-12: {np.sum(err > FIELD_RTOL)}, max err/tol {np.max(err / tol):.3f}")
+    assert np.all(err <= tol)
+
+
+def test_field_igrf_ts05_calculate_field(ctx):
+    g = golden("field_kats.json")["calculate_field"]
+    case = g["cases"]["igrf14+ts05"]
+    pm = unhex(case["parmod"])
+    p = ct.internal_setup("igrf14", g["time"], parmod=pm)
+    pts = unhex(g["points_m"]).reshape(-1, 3)
+    want = unhex(case["b"]).reshape(-1, 3)
+    got = ctx.field_batch(pts, p, models=ct.model_set(ct.INTERNAL_SH, ct.EXTERNAL_TS05))
+    err = _rel_err(got, want)
+    print(f"igrf14+ts05 calculate_field: max rel err {err.max():.3e}")
+    assert err.max() <= 1e-9
+
+
+def test_scan_ts05_matches_reference(ctx):
+    """IGRF-14 + TS05 scans against the reference's: flag agreement >= 99.9%,
+    disagreements inside the penumbra, cutoffs within one step at >= 99.5%."""
+    models = ct.model_set(ct.INTERNAL_SH, ct.EXTERNAL_TS05)
+    g, p, jobs = _scan_golden("scan_ts05.json", models)
+    res = ctx.trace_batch(jobs, p, models=models)
+    n_traj = n_agree = sites_ok = 0
+    outside = []
+    d = g["del"]
+    for j, s in enumerate(g["sites"]):
+        st = res.status[res.offsets[j]:res.offsets[j + 1]]
+        mine = st == ct.TRAJ_ALLOWED
+        ref = np.zeros(len(st), bool)
+        ref[s["allowed"]] = True
+        n_traj += len(st)
+        n_agree += int(np.sum(mine == ref))
+        lo = min(float(s["cutoff"][0]), res.sites[j]["r_lower"]) - d
+        hi = max(float(s["cutoff"][1]), res.sites[j]["r_upper"]) + d
+        rig = g["rig"] + np.arange(len(st)) * d
+        outside += [(j, float(rig[i])) for i in np.nonzero(mine != ref)[0] if not (lo <= rig[i] <= hi)]
+        mine3 = [res.sites[j]["r_lower"], res.sites[j]["r_upper"], res.sites[j]["r_cutoff"]]
+        if all(abs(a - float(b)) <= d * 1.0000001 for a, b in zip(mine3, s["cutoff"])):
+            sites_ok += 1
+    print(f"TS05 scan: flag agreement {n_agree / n_traj:.5f}, sites within one step {sites_ok}/{len(g['sites'])}")
+    assert n_agree / n_traj >= 0.999
+    assert not outside, outside[:10]
+    assert sites_ok / len(g["sites"]) >= 0.995

@@ -105,3 +105,18 @@ def _ext_kat(name: str, fn):
 
 def test_oracle_t96_bit_exact():
     _ext_kat("t96_gsm", pyoracle.load().orc_t96_gsm)
+
+
+def test_oracle_ts05_bit_exact():
+    _ext_kat("ts05_gsm", pyoracle.load().orc_ts05_gsm)
+
+
+def test_oracle_calculate_field_external_bit_exact():
+    g = golden("field_kats.json")["calculate_field"]
+    pts = unhex(g["points_m"]).reshape(-1, 3)
+    for key, ext in (("igrf14+t96", ct.EXTERNAL_T96), ("igrf14+ts05", ct.EXTERNAL_TS05)):
+        case = g["cases"][key]
+        p = ct.internal_setup("igrf14", g["time"], parmod=unhex(case["parmod"]))
+        want = unhex(case["b"]).reshape(-1, 3)
+        got = pyoracle.calculate_field(pts, p, models=ct.model_set(ct.INTERNAL_SH, ext))
+        assert np.array_equal(got.view(np.uint64), want.view(np.uint64)), key
