@@ -1,0 +1,135 @@
+/*
+ * cli_scan.c -- trajectory_simulation_cutoff (src/trajectory.c:6-161) on the
+ * GPU: the scan of one INFILE goes to libcortrace as a batch of one, and the
+ * allowed rows and the CUTOFF line are printed from the returned records with
+ * the reference's formulas and formats (src/trajectory.c:90-122, :160), using
+ * the host C library, so the text equals the reference's wherever the final
+ * states do.
+ */
+#include <math.h>
+#include <stdlib.h>
+#include <string.h>
+
+#include "cli.h"
+
+static cor_ctx *g_ctx = NULL;
+
+int cli_context(cor_ctx **ctx) {
+    if (!g_ctx) {
+        const int rc = cor_ctx_create(0, &g_ctx);
+        if (rc != COR_OK) {
+            fprintf(stderr, "Error: no usable CUDA device (code %d)\n", rc);
+            return rc;
+        }
+    }
+    *ctx = g_ctx;
+    return COR_OK;
+}
+
+static void job_from_header(const InfileHeader *h, cor_scan_job *j) {
+    j->r0 = h->r0;
+    j->the0 = h->the0;
+    j->fi0 = h->fi0;
+    j->the1 = h->the1;
+    j->fi1 = h->fi1;
+    j->rig = h->rig;
+    j->del = h->del;
+    j->rk = h->rk;
+    j->zn = h->zn;
+    j->nk1 = h->nk1;
+    j->param_index = 0;
+}
+
+/* car_to_sph, src/utils.c:43-73 */
+static void car_to_sph(const double car[3], double sph[3]) {
+    const double x = car[0], y = car[1], z = car[2];
+    const double sq = x * x + y * y;
+    const double r = sqrt(sq + z * z);
+    if (sq != 0.) {
+        double phi = atan2(y, x);
+        const double theta = atan2(sqrt(sq), z);
+        if (phi < 0.) phi += DEF_2PI;
+        sph[0] = r; sph[1] = theta; sph[2] = phi;
+        return;
+    }
+    sph[0] = r;
+    sph[1] = z < 0. ? DEF_PI : 0.;
+    sph[2] = 0.;
+}
+
+/* One allowed row, src/trajectory.c:81-122. */
+static void write_row(FILE *out, double rig, const cor_traj_record *r) {
+    double sph[3];
+    car_to_sph(r->pos, sph);
+    const double rr = sph[0] / DEF_RE;
+    const double td = 90. - (sph[1] / DEF_TO_RAD);
+    const double fei = sph[2] / DEF_TO_RAD;
+    const double s = sin(sph[1]), c = cos(sph[1]), sf = sin(sph[2]), cf = cos(sph[2]);
+    const double be = r->vel[0] * cf + r->vel[1] * sf;
+    const double vr = be * s + r->vel[2] * c;
+    const double vt = be * c - r->vel[2] * s;
+    const double vp = -r->vel[0] * sf + r->vel[1] * cf;
+    const double va = vt * c + vr * s;
+    const double dm = sqrt(vt * vt + va * va);
+    const double ast = atan2(-vt * s + vr * c, dm) / DEF_TO_RAD;
+    double asf = (sph[2] + atan2(vp, va)) / DEF_TO_RAD;
+    if (asf > 360.) asf -= 360.;
+    fprintf(out, "%10.6f%15.10f%12.6f%10.3f%10.3f%10.3f%10.3f%12.6f%16.2f\n", rig, r->v / DEF_C, rr, td, fei, ast, asf,
+            r->time, r->length / 1000.);
+}
+
+int cli_write_scan(FILE *out, const InfileHeader *h, const cor_site_result *site, const uint8_t *status,
+                   const cor_traj_record *records) {
+    const int n = (int)round((h->rk - h->rig) / h->del);
+    for (int i = 0; i <= n; i++)
+        if (status[i] == COR_TRAJ_ALLOWED) write_row(out, h->rig + i * h->del, &records[i]);
+    return fprintf(out, "  CUTOFF with rigidities P(S),P(C),P(M) are:\n%12.5f%12.5f%12.5f\n\n", site->r_lower,
+                   site->r_upper, site->r_cutoff) < 0
+               ? -1
+               : 0;
+}
+
+void trajectory_simulation_cutoff(InfileHeader *header, const Model **models, ModelsParams *models_params,
+                                  FILE *outfile, uint64_t step_limit, double tu_angle, double particle_mass,
+                                  uint32_t parallel) {
+    (void)parallel; /* the scan always runs on the GPU */
+    cor_ctx *ctx = NULL;
+    if (cli_context(&ctx) != COR_OK) exit(1);
+    cor_scan_job job;
+    job_from_header(header, &job);
+    uint64_t n = 0;
+    if (cor_batch_count(&job, 1, &n, NULL) != COR_OK) {
+        fprintf(stderr, "Error: invalid rigidity grid\n");
+        exit(1);
+    }
+    cor_site_result site;
+    uint8_t *status = (uint8_t *)malloc(n);
+    cor_traj_record *records = (cor_traj_record *)malloc(sizeof(cor_traj_record) * n);
+    if (!status || !records) {
+        fprintf(stderr, "Error: out of memory\n");
+        exit(1);
+    }
+    cor_batch_req req;
+    memset(&req, 0, sizeof req);
+    req.jobs = &job;
+    req.n_jobs = 1;
+    req.params = models_params;
+    req.n_params = 1;
+    req.models = models_device_set(models);
+    req.step_limit = step_limit;
+    req.tu_angle = tu_angle;
+    req.particle_mass = particle_mass;
+    cor_batch_result res;
+    memset(&res, 0, sizeof res);
+    res.sites = &site;
+    res.status = status;
+    res.records = records;
+    const int rc = cor_trace_batch(ctx, &req, &res);
+    if (rc != COR_OK) {
+        fprintf(stderr, "Error: %s\n", cor_last_error_string(ctx));
+        exit(1);
+    }
+    cli_write_scan(outfile, header, &site, status, records);
+    free(status);
+    free(records);
+}

@@ -169,6 +169,7 @@ def test_scan_t96_matches_reference(ctx):
     n_traj = n_agree = 0
     sites_ok = 0
     outside = []
+    off_sites = []
     d = g["del"]
     for j, s in enumerate(g["sites"]):
         st = res.status[res.offsets[j]:res.offsets[j + 1]]
@@ -185,7 +186,12 @@ def test_scan_t96_matches_reference(ctx):
         mine3 = [res.sites[j]["r_lower"], res.sites[j]["r_upper"], res.sites[j]["r_cutoff"]]
         if all(abs(a - float(b)) <= d * 1.0000001 for a, b in zip(mine3, s["cutoff"])):
             sites_ok += 1
+        else:
+            off_sites.append((s["lat"], s["lon"], [round(float(v), 3) for v in mine3], s["cutoff"],
+                              int(np.sum(mine != ref))))
     print(f"T96 scan: flag agreement {n_agree / n_traj:.5f}, sites within one step {sites_ok}/{len(g['sites'])}")
+    for o in off_sites:
+        print("  site off by more than one step (lat, lon, gpu, reference, flipped):", o)
     assert n_agree / n_traj >= 0.999
     assert not outside, outside[:10]
     assert sites_ok / len(g["sites"]) >= 0.995
