@@ -159,20 +159,80 @@ def cpu_baseline(n_batches: int, seconds_hint: float = 20.0) -> dict:
 
 
 # ---- the GPU arm -------------------------------------------------------------
+class Lane:
+    """One in-flight slot: a context with its own stream, work queue and park
+    buffers.  Batches on different slots overlap on the GPU, so one batch's
+    tail of long trajectories runs beside the next batch's bulk."""
+
+    def __init__(self, dev: int, p):
+        import torch
+        self.torch = torch
+        self.ctx = ct.Context(dev)
+        self.stream = torch.cuda.Stream(device=dev)
+        rc = self.ctx.lib.cor_upload_params(self.ctx.h, p.ctypes.data, len(p))
+        if rc != 0:
+            raise ct.CorError(rc, self.ctx.error())
+        self.cnt = torch.zeros(5, dtype=torch.int64, device=f"cuda:{dev}")
+
+    def run(self, bf, step_limit: int = 25000) -> None:
+        """Scan one batch (device buffers) on this slot's stream; returns when done."""
+        lib = self.ctx.lib
+        e0 = self.torch.cuda.Event(enable_timing=True)
+        e1 = self.torch.cuda.Event(enable_timing=True)
+        e0.record(self.stream)
+        rc = lib.cor_trace_batch_device(
+            self.ctx.h, bf["jobs"].data_ptr(), bf["trig"].data_ptr(), bf["n_jobs"], bf["off"].data_ptr(), bf["n"],
+            models(), step_limit, 0.01, ct.DEF_HM0_P, bf["sites"].data_ptr(), bf["status"].data_ptr(), None,
+            self.cnt.data_ptr(), ct.FLAG_UNIFORM_GRID, C.c_void_p(self.stream.cuda_stream))
+        if rc != 0:
+            raise ct.CorError(rc, self.ctx.error())
+        e1.record(self.stream)
+        self.stream.synchronize()
+        bf["counters"] = self.cnt.cpu().numpy().copy()
+        bf["kernel_ms"] = e0.elapsed_time(e1)
+
+
+def run_batches(slots, bufs, order) -> None:
+    """Runs the batches in `order` over the slots, each slot taking the next
+    batch as soon as it is free (one host thread per slot)."""
+    import queue
+    q = queue.Queue()
+    for i in order:
+        q.put(i)
+    errors = []
+
+    def worker(slot):
+        while True:
+            try:
+                i = q.get_nowait()
+            except queue.Empty:
+                return
+            try:
+                slot.run(bufs[i])
+            except Exception as e:  # noqa: BLE001
+                errors.append(e)
+                return
+
+    ts = [threading.Thread(target=worker, args=(s,)) for s in slots]
+    for t in ts:
+        t.start()
+    for t in ts:
+        t.join()
+    if errors:
+        raise errors[0]
+
+
 def run_ours(args, rank: int, world: int, dist) -> dict | None:
     import torch
     dev = int(os.environ.get("LOCAL_RANK", "0"))
     torch.cuda.set_device(dev)
-    lib = ct.load()
-    ctx = ct.Context(dev)
     p = params()
-    rc = lib.cor_upload_params(ctx.h, p.ctypes.data, len(p))
-    if rc != 0:
-        raise ct.CorError(rc, ctx.error())
-    stream = torch.cuda.current_stream()
+    slots = [Lane(dev, p) for _ in range(args.inflight)]
     mine = rank_batches(rank, world, args.batches)
+    n_steps = args.warmup + args.steps
     bufs = []
-    for b in mine:
+    for k in range(n_steps):
+        b = mine[k % len(mine)]
         jobs = make_jobs(batch_sites(b, args.batches))
         n, off = ct.batch_offsets(jobs)
         trig = ct.prepare_trig(jobs)
@@ -181,49 +241,27 @@ def run_ours(args, rank: int, world: int, dist) -> dict | None:
             "n_jobs": len(jobs), "n": n, "jobs": t(jobs), "trig": t(trig), "off": t(off),
             "sites": torch.zeros(len(jobs) * ct.SITE_DTYPE.itemsize, dtype=torch.uint8, device=f"cuda:{dev}"),
             "status": torch.zeros(n, dtype=torch.uint8, device=f"cuda:{dev}"),
-            "cnt": torch.zeros(5, dtype=torch.int64, device=f"cuda:{dev}"),
             "host_jobs": jobs,
         })
     peak = C.c_double(0.0)
-    lib.cor_probe_fp64_peak(ctx.h, C.byref(peak))
+    slots[0].ctx.lib.cor_probe_fp64_peak(slots[0].ctx.h, C.byref(peak))
 
-    def step(i: int) -> dict:
-        bf = bufs[i % len(bufs)]
-        rc = lib.cor_trace_batch_device(
-            ctx.h, bf["jobs"].data_ptr(), bf["trig"].data_ptr(), bf["n_jobs"], bf["off"].data_ptr(), bf["n"],
-            models(), 25000, 0.01, ct.DEF_HM0_P, bf["sites"].data_ptr(), bf["status"].data_ptr(), None,
-            bf["cnt"].data_ptr(), ct.FLAG_UNIFORM_GRID, C.c_void_p(stream.cuda_stream))
-        if rc != 0:
-            raise ct.CorError(rc, ctx.error())
-        return bf
-
-    for i in range(args.warmup):
-        step(i)
+    run_batches(slots, bufs, range(args.warmup))
     torch.cuda.synchronize()
     if dist:
         dist.barrier(device_ids=[dev])
     torch.cuda.synchronize()
-    evs = []
-    steps_acc = trials_acc = sites_done = traj_done = 0
     with ClockSampler(dev) as clocks:
-        t_wall = time.perf_counter()
-        for i in range(args.steps):
-            e0 = torch.cuda.Event(enable_timing=True)
-            e1 = torch.cuda.Event(enable_timing=True)
-            e0.record(stream)
-            bf = step(args.warmup + i)
-            e1.record(stream)
-            evs.append((e0, e1, bf))
+        t0 = time.perf_counter()
+        run_batches(slots, bufs, range(args.warmup, n_steps))
         torch.cuda.synchronize()
-        wall = time.perf_counter() - t_wall
-    for e0, e1, bf in evs:
-        c = bf["cnt"].cpu().numpy()
-        steps_acc += int(c[0])
-        trials_acc += int(c[1])
-        traj_done += int(c[2])
-        sites_done += bf["n_jobs"]
-    launch_ms = [e0.elapsed_time(e1) for e0, e1, _ in evs]
-    dev_s = sum(launch_ms) / 1e3
+        dev_s = time.perf_counter() - t0
+    timed = bufs[args.warmup:]
+    steps_acc = sum(int(b["counters"][0]) for b in timed)
+    trials_acc = sum(int(b["counters"][1]) for b in timed)
+    traj_done = sum(int(b["counters"][2]) for b in timed)
+    sites_done = sum(b["n_jobs"] for b in timed)
+    launch_ms = [b["kernel_ms"] for b in timed]
     if dist:
         import torch.distributed as tdist
         t = torch.tensor([dev_s], dtype=torch.float64, device=f"cuda:{dev}")
@@ -233,21 +271,42 @@ def run_ours(args, rank: int, world: int, dist) -> dict | None:
         tdist.all_reduce(tot)
         sites_done, traj_done, steps_acc, trials_acc = (int(v) for v in tot.tolist())
 
-    # e2e through the public C ABI with host buffers
+    # e2e through the public C ABI with host buffers (same overlap, one host
+    # thread per slot, cor_trace_batch copies in and out inside the call)
     h2d = d2h = 0
+    import queue
+    qe = queue.Queue()
+    for i in range(args.warmup, n_steps):
+        qe.put(i)
+    sizes = []
+
+    def e2e_worker(slot):
+        while True:
+            try:
+                i = qe.get_nowait()
+            except queue.Empty:
+                return
+            jobs = bufs[i]["host_jobs"]
+            r = slot.ctx.trace_batch(jobs, p, models=models())
+            sizes.append((jobs.nbytes + len(jobs) * ct.TRIG_DTYPE.itemsize + (len(jobs) + 1) * 8 + p.nbytes,
+                          r.sites.nbytes + r.status.nbytes + 40))
+
     t0 = time.perf_counter()
-    for i in range(args.steps):
-        jobs = bufs[(args.warmup + i) % len(bufs)]["host_jobs"]
-        r = ctx.trace_batch(jobs, p, models=models())
-        h2d += jobs.nbytes + len(jobs) * ct.TRIG_DTYPE.itemsize + (len(jobs) + 1) * 8 + p.nbytes
-        d2h += r.sites.nbytes + r.status.nbytes + 40
+    ths = [threading.Thread(target=e2e_worker, args=(s,)) for s in slots]
+    for t in ths:
+        t.start()
+    for t in ths:
+        t.join()
     e2e_s = time.perf_counter() - t0
+    h2d = sum(a for a, _ in sizes)
+    d2h = sum(b for _, b in sizes)
     if dist:
         import torch.distributed as tdist
         t = torch.tensor([e2e_s], dtype=torch.float64, device=f"cuda:{dev}")
         tdist.all_reduce(t, op=tdist.ReduceOp.MAX)
         e2e_s = float(t.item())
-    ctx.close()
+    for s in slots:
+        s.ctx.close()
     if rank != 0:
         return None
     wm = work_model()
@@ -261,22 +320,57 @@ def run_ours(args, rank: int, world: int, dist) -> dict | None:
         "data": "synthetic grid of sites (the configuration's own sites; no dataset)",
         "config": {"workload": WORKLOAD, "sites_per_step": sites_done // max(1, args.steps * world),
                    "trajectories_per_step": traj_done // max(1, args.steps * world),
-                   "batches": args.batches, "l2": "inputs/outputs are KB-sized; the kernel is FP64-bound, "
-                   "no L2 flush needed (state lives in registers)", "parallelism": f"sites split over {world} GPU(s)"},
+                   "batches": args.batches, "inflight": args.inflight,
+                   "l2": "no L2 flush: the kernel is FP64-bound and its state lives in registers; inputs and "
+                         "outputs are MB-sized", "parallelism": f"sites split over {world} GPU(s)"},
         "trajectories_per_s": traj_done / dev_s, "steps_per_s": steps_acc / dev_s,
+        "batch_kernel_ms": launch_ms,
         "roofline": {"bound": "fp64", "achieved": achieved, "peak": peak.value / 1e12, "unit": "TFLOP/s",
                      "frac": achieved / (peak.value / 1e12) if peak.value else None,
                      "traffic": None, "work_model": wm.get("source"),
+                     "flops_per_step": wm["flops_per_step"],
                      "peak_source": "DFMA microbenchmark in libcortrace (cor_probe_fp64_peak), FMA = 2 flops"},
-        "e2e": {"value": sites_done / e2e_s if not dist else sites_done / e2e_s, "unit": METRIC,
+        "e2e": {"value": sites_done / e2e_s, "unit": METRIC,
                 "h2d_bytes_per_step": h2d // args.steps, "d2h_bytes_per_step": d2h // args.steps},
-        "gpu_launches": 2 * args.steps,
+        "gpu_launches": sum(int(b["counters"][4]) for b in timed),
         "clocks": clocks.summary(),
-        "wall_s_timed": wall,
     }
     if world == 1 and not args.no_cpu_baseline:
         out["cpu_baseline"] = cpu_baseline(args.batches)
     return out
+
+
+# ---- small case of the same kernel, for profiler captures ---------------------
+PROFILE_SITES = 32
+PROFILE_STEP_LIMIT = 2500
+
+
+def run_profile_case(args) -> dict:
+    """PROFILE_SITES sites spread over all latitudes x the 2,000 rigidities, with
+    the step limit lowered to PROFILE_STEP_LIMIT so that a launch lasts about a
+    second: the bulk of the scan kernel's work without the 25,000-step tail.
+    Not a bench line; it exists to be captured under ncu."""
+    import torch
+    dev = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(dev)
+    p = params()
+    slot = Lane(dev, p)
+    sites = grid_sites()[::len(grid_sites()) // PROFILE_SITES][:PROFILE_SITES]
+    jobs = make_jobs(sites)
+    n, off = ct.batch_offsets(jobs)
+    t = lambda a: torch.from_numpy(a.view(np.uint8).copy()).to(f"cuda:{dev}")
+    bf = {"n_jobs": len(jobs), "n": n, "jobs": t(jobs), "trig": t(ct.prepare_trig(jobs)), "off": t(off),
+          "sites": torch.zeros(len(jobs) * ct.SITE_DTYPE.itemsize, dtype=torch.uint8, device=f"cuda:{dev}"),
+          "status": torch.zeros(n, dtype=torch.uint8, device=f"cuda:{dev}")}
+    ms = []
+    for _ in range(args.warmup + args.steps):
+        slot.run(bf, step_limit=PROFILE_STEP_LIMIT)
+        ms.append(bf["kernel_ms"])
+    c = bf["counters"]
+    slot.ctx.close()
+    return {"profile_case": f"{len(sites)} sites x {N_RIG} rigidities, step limit {PROFILE_STEP_LIMIT}",
+            "trajectories": int(c[2]), "accepted_steps": int(c[0]), "trials": int(c[1]),
+            "kernel_launches": int(c[4]), "call_ms": ms}
 
 
 def run_reference(args, rank: int) -> dict | None:
@@ -318,8 +412,11 @@ def main():
     ap.add_argument("--steps", type=int, default=4)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--batches", type=int, default=16)
+    ap.add_argument("--inflight", type=int, default=3, help="batches in flight at once (one stream each)")
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--profile-case", action="store_true",
+                    help="run only the small profiling case of the scan kernel (prints its own JSON, not a bench line)")
     args = ap.parse_args()
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
@@ -329,7 +426,9 @@ def main():
         backend = "gloo" if args.impl == "reference" else "nccl"
         tdist.init_process_group(backend)
         dist = tdist
-    if args.impl == "reference":
+    if args.profile_case:
+        out = run_profile_case(args) if rank == 0 else None
+    elif args.impl == "reference":
         out = run_reference(args, rank)
     else:
         out = run_ours(args, rank, world, dist)

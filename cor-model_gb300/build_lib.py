@@ -30,7 +30,7 @@ CC_FLAGS = ["-O2", "-std=gnu17", "-fPIC", "-ffp-contract=off", "-fno-math-errno"
 
 # Sources of the shared library.
 CU_SOURCES = ["cortrace.cu", "inst_igrf.cu", "inst_igrf_t96.cu", "inst_t96.cu", "inst_igrf_ts05.cu",
-              "inst_ts05.cu"]
+              "inst_ts05.cu", "inst_crustal.cu"]
 LIB_C_SOURCES = ["setup.c", "coef_tables.c"]
 # Sources of the drop-in CLI (linked against the library).
 CLI_C_SOURCES = ["cli_main.c", "cli_io.c", "cli_models.c", "cli_scan.c"]

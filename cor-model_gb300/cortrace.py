@@ -62,7 +62,7 @@ class ModelSet(C.Structure):
 
 class Counters(C.Structure):
     _fields_ = [("accepted_steps", C.c_uint64), ("trials", C.c_uint64), ("trajectories", C.c_uint64),
-                ("watchdog", C.c_uint64), ("turn_fallbacks", C.c_uint64)]
+                ("watchdog", C.c_uint64), ("kernel_launches", C.c_uint64)]
 
     def as_dict(self) -> dict:
         return {k: int(getattr(self, k)) for k, _ in self._fields_}
@@ -82,7 +82,7 @@ class BatchResult(C.Structure):
 EXPORTS = [
     "cor_ctx_create", "cor_ctx_destroy", "cor_last_error_string", "cor_abi_version", "cor_batch_count",
     "cor_prepare_trig", "cor_trace_batch", "cor_trace_batch_device", "cor_upload_params", "cor_field_batch",
-    "cor_internal_setup", "cor_gsm_setup", "cor_probe_fp64_peak",
+    "cor_internal_setup", "cor_gsm_setup", "cor_probe_fp64_peak", "cor_upload_crustal",
 ]
 
 _lib = None
@@ -108,6 +108,7 @@ def load(path: str = LIB_PATH) -> C.CDLL:
     lib.cor_trace_batch_device.argtypes = [vp, vp, vp, i32, vp, u64, ModelSet, u64, dbl, dbl,
                                            vp, vp, vp, vp, C.c_uint32, vp]
     lib.cor_upload_params.argtypes = [vp, vp, i32]
+    lib.cor_upload_crustal.argtypes = [vp, vp, vp, i32]
     lib.cor_probe_fp64_peak.argtypes = [vp, C.POINTER(C.c_double)]
     lib.cor_field_batch.argtypes = [vp, ModelSet, vp, i32, vp, vp, i64, vp]
     lib.cor_internal_setup.argtypes = [C.c_char_p, vp, vp]
@@ -222,6 +223,14 @@ class Context:
         res = BatchResult(_ptr(sites), _ptr(status), _ptr(records), Counters())
         self._check(self.lib.cor_trace_batch(self.h, C.byref(req), C.byref(res)), "trace_batch")
         return ScanResult(sites, status, records, off, res.counters.as_dict())
+
+    def upload_crustal(self, g: np.ndarray, h: np.ndarray, nmax: int) -> None:
+        """cor_upload_crustal: packed lower-triangle G, H (index n(n+1)/2 + m)."""
+        g = np.ascontiguousarray(g, np.float64)
+        h = np.ascontiguousarray(h, np.float64)
+        if len(g) < nmax * (nmax + 1) // 2 or len(h) < nmax * (nmax + 1) // 2:
+            raise ValueError("crustal table shorter than nmax(nmax+1)/2")
+        self._check(self.lib.cor_upload_crustal(self.h, g.ctypes.data, h.ctypes.data, nmax), "cor_upload_crustal")
 
     def field_batch(self, gsm_pos_m: np.ndarray, params: np.ndarray, models: ModelSet | None = None,
                     param_index: np.ndarray | None = None) -> np.ndarray:

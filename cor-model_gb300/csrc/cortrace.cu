@@ -12,6 +12,10 @@
 #include "reduce.cuh"
 #include "ts05_tables.h"
 
+extern "C" {
+#include "../host/coef_tables.h"
+}
+
 using namespace cor;
 
 static_assert(sizeof(cor_job_trig) == sizeof(JobTrig), "trig layout");
@@ -37,11 +41,12 @@ struct cor_ctx {
     DevBuf park[2];                       // parked trajectories between generations (scratch)
     GenCounters* gen = nullptr;           // per-generation counters (scratch)
     unsigned int* park_count_host = nullptr;  // pinned readback of the parked count
+    unsigned long long* launches_host = nullptr;  // pinned: kernels launched by the last scan
     int generations = 0;                  // generations of the last scan (diagnostics)
     cor_counters* counters = nullptr;
-    const double* crust_g = nullptr;      // device copies of the crustal table
-    const double* crust_h = nullptr;
+    double* crust = nullptr;              // crustal tables: g, h, k1, k2 (packed), kd
     int crust_nmax = 0;
+    int crust_n_first = 0;
 };
 
 extern "C" {
@@ -315,11 +320,12 @@ extern "C" int cor_ctx_create(int device, cor_ctx** out) {
         if (cudaMalloc(&ctx->counters, sizeof(cor_counters)) != cudaSuccess) { rc = COR_ERR_NOMEM; break; }
         if (cudaMalloc(&ctx->gen, sizeof(GenCounters)) != cudaSuccess) { rc = COR_ERR_NOMEM; break; }
         if (cudaMallocHost(&ctx->park_count_host, sizeof(unsigned int)) != cudaSuccess) { rc = COR_ERR_NOMEM; break; }
+        if (cudaMallocHost(&ctx->launches_host, sizeof(unsigned long long)) != cudaSuccess) { rc = COR_ERR_NOMEM; break; }
         T96Tables tt;
         t96_tables(&tt);
         TS05Tables t5;
         ts05_tables(&t5);
-        const ModelOps* all[] = {&ops_igrf, &ops_igrf_t96, &ops_t96, &ops_igrf_ts05, &ops_ts05};
+        const ModelOps* all[] = {&ops_igrf, &ops_igrf_t96, &ops_t96, &ops_igrf_ts05, &ops_ts05, &ops_crustal};
         for (const ModelOps* o : all)
             if (o->upload_tables(&tt, &t5) != cudaSuccess) rc = COR_ERR_CUDA;
         if (rc != COR_OK) break;
@@ -340,12 +346,12 @@ extern "C" int cor_ctx_destroy(cor_ctx* ctx) {
                       &ctx->status, &ctx->records, &ctx->park[0], &ctx->park[1]};
     if (ctx->gen) cudaFree(ctx->gen);
     if (ctx->park_count_host) cudaFreeHost(ctx->park_count_host);
+    if (ctx->launches_host) cudaFreeHost(ctx->launches_host);
     for (DevBuf* b : bufs)
         if (b->p) cudaFree(b->p);
     if (ctx->queue) cudaFree(ctx->queue);
     if (ctx->counters) cudaFree(ctx->counters);
-    if (ctx->crust_g) cudaFree((void*)ctx->crust_g);
-    if (ctx->crust_h) cudaFree((void*)ctx->crust_h);
+    if (ctx->crust) cudaFree(ctx->crust);
     if (ctx->stream) cudaStreamDestroy(ctx->stream);
     delete ctx;
     return COR_OK;
@@ -437,13 +443,14 @@ static bool model_set_ok(const cor_model_set& m) {
     const bool in_ok = m.internal_model == COR_INTERNAL_NONE || m.internal_model == COR_INTERNAL_SH;
     const bool ex_ok = m.external_model == COR_EXTERNAL_NONE || m.external_model == COR_EXTERNAL_T96 ||
                        m.external_model == COR_EXTERNAL_TS05;
-    const bool cr_ok = m.crustal_model == COR_CRUSTAL_NONE;
+    const bool cr_ok = m.crustal_model == COR_CRUSTAL_NONE || m.crustal_model == COR_CRUSTAL_CHAOS;
     const bool any = m.internal_model || m.external_model || m.crustal_model;
     return in_ok && ex_ok && cr_ok && any && m.reserved == 0;
 }
 
 // The compile-time model set matching m (model_set_ok(m) must hold).
 static const ModelOps* find_ops(const cor_model_set& m) {
+    if (m.crustal_model != COR_CRUSTAL_NONE) return &ops_crustal;
     const int key = m.internal_model * 100 + m.external_model * 10 + m.crustal_model;
     static const ModelOps* const all[] = {&ops_igrf, &ops_igrf_t96, &ops_t96, &ops_igrf_ts05, &ops_ts05};
     for (const ModelOps* o : all)
@@ -509,13 +516,105 @@ static int launch_scan(cor_ctx* ctx, const TraceArgs& a, cor_model_set models, c
         const int rc = launch_trace(ctx, ops, a, s);
         if (rc != COR_OK) return rc;
     }
+    unsigned long long launches = a.n_traj > 0 ? (unsigned long long)ctx->generations : 0ull;
     if (a.n_jobs > 0) {
         const int threads = 256;
         const int blocks = (int)(((int64_t)a.n_jobs * 32 + threads - 1) / threads);
         reduce_kernel<<<blocks, threads, 0, s>>>(a.jobs, a.offsets, a.n_jobs, a.status, sites);
         CUDA_TRY(ctx, cudaGetLastError());
+        launches += 1;
     }
+    // the pinned staging value is read by the copy before the next call can
+    // change it: every call on a context synchronises its stream first
+    CUDA_TRY(ctx, cudaStreamSynchronize(s));
+    *ctx->launches_host = launches;
+    CUDA_TRY(ctx, cudaMemcpyAsync(&a.counters->kernel_launches, ctx->launches_host, sizeof(unsigned long long),
+                                  cudaMemcpyHostToDevice, s));
     return COR_OK;
+}
+
+// ---- crustal model tables --------------------------------------------------
+// One device block: g, h, k1, k2 (packed lower triangles of nmax(nmax+1)/2
+// entries each), then kd (nmax entries).  k1, k2 and kd are the recursion
+// factors of lib/chaos/chaos.c:163-180, computed with its expressions.
+static int upload_crustal(cor_ctx* ctx, const double* g, const double* h, int32_t nmax) {
+    if (nmax < 2 || nmax > kChaosMaxN)
+        return fail(ctx, COR_ERR_RANGE, "crustal table nmax %d outside [2, %d]", nmax, kChaosMaxN);
+    const size_t nt = (size_t)nmax * (size_t)(nmax + 1) / 2;
+    const size_t total = 4 * nt + (size_t)nmax;
+    double* host = (double*)calloc(total, sizeof(double));
+    if (!host) return fail(ctx, COR_ERR_NOMEM, "host allocation");
+    double* hk1 = host + 2 * nt;
+    double* hk2 = host + 3 * nt;
+    double* hkd = host + 4 * nt;
+    memcpy(host, g, sizeof(double) * nt);
+    memcpy(host + nt, h, sizeof(double) * nt);
+    int n_first = nmax;
+    for (int n = 0; n < nmax && n_first == nmax; n++)
+        for (int m = 0; m <= n; m++)
+            if (g[n * (n + 1) / 2 + m] != 0. || h[n * (n + 1) / 2 + m] != 0.) {
+                n_first = n;
+                break;
+            }
+    for (int n = 2; n < nmax; n++) {
+        const double n2 = n * 2;
+        const double n21 = n2 - 1;
+        const int n1 = n - 1;
+        hkd[n] = sqrt(n21 / n2);
+        const double nn = (double)n * n;
+        for (int m = 0; m < n; m++) {
+            const double mm = m * m;
+            const double nnmm = nn - mm;
+            hk1[n * (n + 1) / 2 + m] = n21 / sqrt(nnmm);
+            hk2[n * (n + 1) / 2 + m] = sqrt((n1 * n1 - mm) / nnmm);
+        }
+    }
+    int rc = COR_OK;
+    double* dev = nullptr;
+    do {
+        cudaError_t e = cudaSetDevice(ctx->device);
+        if (e == cudaSuccess) e = cudaMalloc(&dev, sizeof(double) * total);
+        if (e != cudaSuccess) { rc = fail(ctx, COR_ERR_NOMEM, "crustal table: %s", cudaGetErrorString(e)); break; }
+        e = cudaMemcpyAsync(dev, host, sizeof(double) * total, cudaMemcpyHostToDevice, ctx->stream);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
+        if (e != cudaSuccess) { rc = fail(ctx, COR_ERR_CUDA, "crustal table: %s", cudaGetErrorString(e)); break; }
+        if (ctx->crust) cudaFree(ctx->crust);
+        ctx->crust = dev;
+        dev = nullptr;
+        ctx->crust_nmax = nmax;
+        ctx->crust_n_first = n_first;
+    } while (0);
+    if (dev) cudaFree(dev);
+    free(host);
+    return rc;
+}
+
+// The crustal tables for a launch of model set m; the first launch with the
+// crustal model uploads the CHAOS-7.16 table unless cor_upload_crustal gave one.
+static int crustal_tables(cor_ctx* ctx, const cor_model_set& m, CrustalTables* t) {
+    memset(t, 0, sizeof *t);
+    if (m.crustal_model == COR_CRUSTAL_NONE) return COR_OK;
+    if (!ctx->crust) {
+        const int rc = upload_crustal(ctx, cor_chaos716.g, cor_chaos716.h, cor_chaos716.nmax);
+        if (rc != COR_OK) return rc;
+    }
+    const size_t nt = (size_t)ctx->crust_nmax * (size_t)(ctx->crust_nmax + 1) / 2;
+    t->g = ctx->crust;
+    t->h = ctx->crust + nt;
+    t->k1 = ctx->crust + 2 * nt;
+    t->k2 = ctx->crust + 3 * nt;
+    t->kd = ctx->crust + 4 * nt;
+    t->nmax = ctx->crust_nmax;
+    t->n_first = ctx->crust_n_first;
+    t->internal = m.internal_model;
+    t->external = m.external_model;
+    return COR_OK;
+}
+
+extern "C" int cor_upload_crustal(cor_ctx* ctx, const double* g, const double* h, int32_t nmax) {
+    if (!ctx) return COR_ERR_INVALID;
+    if (!g || !h) return fail(ctx, COR_ERR_INVALID, "null crustal table");
+    return upload_crustal(ctx, g, h, nmax);
 }
 
 extern "C" int cor_upload_params(cor_ctx* ctx, const cor_model_params* params, int32_t n_params) {
@@ -584,7 +683,10 @@ extern "C" int cor_trace_batch_device(cor_ctx* ctx, const cor_scan_job* jobs_dev
     a.records = records_dev;
     a.queue = ctx->queue;
     a.counters = counters_dev ? counters_dev : ctx->counters;
-    a.crust = CrustalTables{ctx->crust_g, ctx->crust_h, ctx->crust_nmax};
+    {
+        const int rc = crustal_tables(ctx, models, &a.crust);
+        if (rc != COR_OK) return rc;
+    }
     a.rig_major = ((flags & COR_FLAG_UNIFORM_GRID) && a.n_rig > 0) ? 1 : 0;
     return launch_scan(ctx, a, models, sites_dev, (cudaStream_t)stream);
 }
@@ -689,7 +791,8 @@ extern "C" int cor_field_batch(cor_ctx* ctx, cor_model_set models, const cor_mod
         free(hp);
         cudaMemcpyAsync(dpos, gsm_pos, sizeof(double) * 3 * (size_t)n, cudaMemcpyHostToDevice, s);
         if (param_index) cudaMemcpyAsync(didx, param_index, sizeof(int32_t) * (size_t)n, cudaMemcpyHostToDevice, s);
-        const CrustalTables crust{ctx->crust_g, ctx->crust_h, ctx->crust_nmax};
+        CrustalTables crust;
+        if ((rc = crustal_tables(ctx, models, &crust)) != COR_OK) break;
         find_ops(models)->launch_field((const DevParams*)dp, n_params, (const int32_t*)didx, (const double*)dpos, n,
                                        (double*)dout, crust, s);
         cudaMemcpyAsync(geo_field, dout, sizeof(double) * 3 * (size_t)n, cudaMemcpyDeviceToHost, s);

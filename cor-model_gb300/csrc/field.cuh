@@ -3,6 +3,7 @@
 #pragma once
 
 #include "cor_device.cuh"
+#include "chaos.cuh"
 #include "t96.cuh"
 #include "ts05.cuh"
 
@@ -10,7 +11,11 @@ namespace cor {
 
 // Compile-time model set: internal (0/1), external (0 none, 1 T96, 2 TS05),
 // crustal (0/1).  The kernels are instantiated per set so the step loop
-// carries no model dispatch.
+// carries no model dispatch.  kModelAtRunTime for internal or external reads
+// the choice from the crustal tables' internal/external members instead (the
+// one instantiation that serves every set with a crustal model).
+constexpr int kModelAtRunTime = -1;
+
 template <int INTERNAL, int EXTERNAL, int CRUSTAL>
 struct ModelSet {
     static constexpr int internal = INTERNAL;
@@ -26,16 +31,6 @@ struct DevParams {
     TS05Cond ts05;
 };
 
-// Device tables of the crustal model (packed lower triangle) and its
-// per-degree recursion factors; set by the context before a crustal launch.
-struct CrustalTables {
-    const double* g;
-    const double* h;
-    int nmax;
-};
-
-__device__ Vec3 chaos_geo(const Vec3 x, const CrustalTables& t);
-
 // GSM position in metres -> GEO field in nT.
 template <class MS>
 __device__ __forceinline__ Vec3 calculate_field(const Vec3 gsm_pos, const DevParams* __restrict__ dp,
@@ -43,7 +38,9 @@ __device__ __forceinline__ Vec3 calculate_field(const Vec3 gsm_pos, const DevPar
     const cor_model_params* __restrict__ p = &dp->p;
     const Vec3 pos = {DIVRE(gsm_pos.x), DIVRE(gsm_pos.y), DIVRE(gsm_pos.z)};
     Vec3 tot = {0., 0., 0.};
-    if (MS::internal) {
+    const bool internal = MS::internal == kModelAtRunTime ? crust.internal != 0 : MS::internal != 0;
+    const int external = MS::external == kModelAtRunTime ? crust.external : MS::external;
+    if (internal) {
         // internal_calc, src/models.c:146-160
         const Vec3 geo = gsm_to_geo(pos, p);
         const Vec3 bg = internal_geo(geo, p);
@@ -52,12 +49,12 @@ __device__ __forceinline__ Vec3 calculate_field(const Vec3 gsm_pos, const DevPar
         tot.y += bs.y;
         tot.z += bs.z;
     }
-    if (MS::external == COR_EXTERNAL_T96) {
+    if (external == COR_EXTERNAL_T96) {
         const Vec3 b = t96_field(dp->t96, pos);  // t96_calc, src/models.c:171-177
         tot.x += b.x;
         tot.y += b.y;
         tot.z += b.z;
-    } else if (MS::external == COR_EXTERNAL_TS05) {
+    } else if (external == COR_EXTERNAL_TS05) {
         const Vec3 b = ts05_field(dp->ts05, pos);  // ts05_calc, src/models.c:162-169
         tot.x += b.x;
         tot.y += b.y;

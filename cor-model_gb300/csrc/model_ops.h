@@ -11,7 +11,7 @@
 namespace cor {
 
 struct ModelOps {
-    int key;  // internal*100 + external*10 + crustal
+    int key;  // internal*100 + external*10 + crustal (negative for run-time choices)
     cudaError_t (*occupancy)(int* blocks_per_sm);
     cudaError_t (*launch_generation)(const TraceArgs& a, unsigned blocks, cudaStream_t s);
     cudaError_t (*launch_field)(const DevParams* params, int n_params, const int32_t* pidx, const double* pos,
@@ -20,6 +20,6 @@ struct ModelOps {
     cudaError_t (*upload_tables)(const T96Tables* t96, const TS05Tables* ts05);
 };
 
-extern const ModelOps ops_igrf, ops_igrf_t96, ops_t96, ops_igrf_ts05, ops_ts05;
+extern const ModelOps ops_igrf, ops_igrf_t96, ops_t96, ops_igrf_ts05, ops_ts05, ops_crustal;
 
 }  // namespace cor

@@ -134,7 +134,7 @@ typedef struct {
     uint64_t trials;          /* RK trials (accepted + rejected)           */
     uint64_t trajectories;
     uint64_t watchdog;        /* trajectories that ended COR_TRAJ_WATCHDOG */
-    uint64_t turn_fallbacks;  /* turn-angle decisions that needed atan2    */
+    uint64_t kernel_launches; /* kernels this call launched (generations + reduction) */
 } cor_counters;
 
 typedef struct {
@@ -195,6 +195,15 @@ int cor_trace_batch(cor_ctx *ctx, const cor_batch_req *req, cor_batch_result *ou
  * Per-condition constants of the external models are derived here on the
  * host. */
 int cor_upload_params(cor_ctx *ctx, const cor_model_params *params, int32_t n_params);
+
+/* Replaces the crustal model's coefficient table on this context: G and H as
+ * packed lower triangles (index n*(n+1)/2 + m, degrees n = 0 .. nmax-1), the
+ * layout of lib/chaos/coefs/chaos_7_16.h read by chaos_geo
+ * (lib/chaos/chaos.c:120-226).  Without this call the first scan or field
+ * batch with COR_CRUSTAL_CHAOS uploads the built-in CHAOS-7.16 table
+ * (nmax 186).  nmax outside [2, 192] gives COR_ERR_RANGE.  The reference
+ * has no counterpart: its table is a compile-time constant. */
+int cor_upload_crustal(cor_ctx *ctx, const double *g, const double *h, int32_t nmax);
 
 /* Same scan with every buffer already in device memory (jobs, trig from
  * cor_prepare_trig, offsets from cor_batch_count, sites, status, records) and

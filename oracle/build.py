@@ -64,6 +64,19 @@ def build_port(force: bool = False) -> str:
     return out
 
 
+def build_nudge(force: bool = False) -> str:
+    """The oracle with every libm transcendental moved by one ulp (nudge/)."""
+    out = os.path.join(HERE, "liboracle_nudge.so")
+    srcs = port_sources()
+    nudge_dir = os.path.join(HERE, "nudge")
+    extra = [os.path.join(nudge_dir, "nudge.c"), os.path.join(nudge_dir, "nudge.h")]
+    if force or _stale(out, srcs + extra):
+        cmd = ["gcc", "-std=gnu17", "-fPIC", "-shared", "-pthread", *FP_FLAGS, "-include",
+               os.path.join(nudge_dir, "nudge.h"), *srcs, os.path.join(nudge_dir, "nudge.c"), "-o", out, "-lm"]
+        _run(cmd)
+    return out
+
+
 def ref_available() -> bool:
     return os.path.isfile(os.path.join(REF_ROOT, "src", "trajectory.c"))
 

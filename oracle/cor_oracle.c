@@ -32,11 +32,13 @@
 
 /* ---- geometry: src/utils.c:28-101 ------------------------------------- */
 static void o_sph_to_car(double r, double theta, double phi, double car[3]) {
-    /* src/utils.c:28-41 */
-    const double sq = r * sin(theta);
-    car[0] = sq * cos(phi);
-    car[1] = sq * sin(phi);
-    car[2] = r * cos(theta);
+    /* src/utils.c:28-41.  The parenthesised names keep these calls out of the
+     * one-ulp libm perturbation build (nudge/), as the device takes them from
+     * the host C library. */
+    const double sq = r * (sin)(theta);
+    car[0] = sq * (cos)(phi);
+    car[1] = sq * (sin)(phi);
+    car[2] = r * (cos)(theta);
 }
 
 static void o_car_to_sph(const double car[3], double sph[3]) {

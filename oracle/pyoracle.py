@@ -46,8 +46,65 @@ def load() -> C.CDLL:
     return _lib
 
 
+_nudge = None
+
+
+def load_nudge() -> C.CDLL:
+    """The oracle built with every libm transcendental moved by one ulp."""
+    global _nudge
+    if _nudge is None:
+        lib = C.CDLL(obuild.build_nudge())
+        vp, dbl = C.c_void_p, C.c_double
+        lib.orc_ts05_gsm.argtypes = [vp, dbl, dbl, dbl, vp, vp, vp]
+        lib.orc_t96_gsm.argtypes = [vp, dbl, dbl, dbl, vp, vp, vp]
+        lib.orc_scan_batch.argtypes = [C.POINTER(ct.BatchReq), vp, C.c_int, vp, vp, vp, vp]
+        lib.orc_nudge_seed.argtypes = [C.c_uint64]
+        lib.orc_chaos_geo.argtypes = [dbl, dbl, dbl, vp, vp, C.c_int, vp, vp, vp]
+        lib.orc_set_crustal_table.argtypes = [vp, vp, C.c_int]
+        lib.orc_calculate_field.argtypes = [vp, ct.ModelSet, vp, vp]
+        _nudge = lib
+    return _nudge
+
+
+def scan_batch_nudged(jobs, params, models, seed: int, threads=8):
+    """orc_scan_batch of the one-ulp-perturbed oracle (each thread reseeds
+    from `seed` and the job order, so the result is reproducible only per
+    job; the statistics, not the bits, are what matter)."""
+    lib = load_nudge()
+    jobs = np.ascontiguousarray(jobs, ct.JOB_DTYPE)
+    params = np.ascontiguousarray(params, ct.PARAMS_DTYPE)
+    n, off = ct.batch_offsets(jobs)
+    sites = np.zeros(len(jobs), ct.SITE_DTYPE)
+    status = np.zeros(n, np.uint8)
+    req = ct.BatchReq(_p(jobs), len(jobs), len(params), _p(params), models, 25000, 0.01, ct.DEF_HM0_P)
+    cnt = ct.Counters()
+    _crustal(lib, models)
+    lib.orc_nudge_seed(seed)
+    rc = lib.orc_scan_batch(C.byref(req), _p(off), threads, _p(sites), _p(status), None, C.byref(cnt))
+    if rc != 0:
+        raise RuntimeError(f"nudged scan failed: {rc}")
+    return ct.ScanResult(sites, status, None, off, cnt.as_dict())
+
+
+def calculate_field_nudged(gsm_m: np.ndarray, params: np.ndarray, models) -> np.ndarray:
+    """calculate_field of the one-ulp-perturbed oracle (seed it first)."""
+    return calculate_field(gsm_m, params, models, lib=load_nudge())
+
+
 def _p(a):
     return None if a is None else a.ctypes.data
+
+
+_crust_keep = {}
+
+
+def _crustal(lib, models) -> None:
+    """Give `lib` the dense CHAOS-7.16 table when `models` has the crustal model."""
+    if models is None or models.crustal_model == ct.CRUSTAL_NONE or id(lib) in _crust_keep:
+        return
+    G, H, nmax = ct.chaos_dense()
+    _crust_keep[id(lib)] = (G, H)
+    lib.orc_set_crustal_table(G.ctypes.data, H.ctypes.data, nmax)
 
 
 def internal_geo(xyz: np.ndarray, params: np.ndarray) -> np.ndarray:
@@ -63,12 +120,13 @@ def internal_geo(xyz: np.ndarray, params: np.ndarray) -> np.ndarray:
     return out
 
 
-def calculate_field(gsm_m: np.ndarray, params: np.ndarray, models=None) -> np.ndarray:
-    lib = load()
+def calculate_field(gsm_m: np.ndarray, params: np.ndarray, models=None, lib=None) -> np.ndarray:
+    lib = lib or load()
     pos = np.asarray(gsm_m, np.float64).reshape(-1, 3)
     p = np.ascontiguousarray(params, ct.PARAMS_DTYPE).reshape(-1)[:1]
     out = np.zeros_like(pos)
     m = models or ct.model_set()
+    _crustal(lib, m)
     for i in range(len(pos)):
         x = np.ascontiguousarray(pos[i])
         o = np.zeros(3)
@@ -90,6 +148,7 @@ def scan_batch(jobs: np.ndarray, params: np.ndarray, models=None, step_limit=250
     req = ct.BatchReq(_p(jobs), len(jobs), len(params), _p(params), models or ct.model_set(), step_limit,
                       tu_angle, particle_mass)
     cnt = ct.Counters()
+    _crustal(lib, req.models)
     rc = lib.orc_scan_batch(C.byref(req), _p(off), threads, _p(sites), _p(status), _p(records), C.byref(cnt))
     if rc != 0:
         raise RuntimeError(f"oracle scan failed: {rc}")

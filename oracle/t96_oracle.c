@@ -284,7 +284,7 @@ static void t_circle(double x, double y, double z, double rl, double b[3]) {
 }
 
 static void t_crosslp(double x, double y, double z, double b[3], double xc, double rl, double al) {
-    const double cal = cos(al), sal = sin(al);
+    const double cal = (cos)(al), sal = (sin)(al);
     const double y1 = y * cal - z * sal, z1 = y * sal + z * cal;
     const double y2 = y * cal + z * sal, z2 = -y * sal + z * cal;
     double b1[3], b2[3];
@@ -661,7 +661,7 @@ static void t_dipdistr(double x, double y, double z, double b[3], int mode) {
 
 static void t_loops4(double x, double y, double z, double b[3], double xc, double yc, double zc, double R,
                      double theta, double phi) {
-    const double st = sin(theta), ct = cos(theta), sp = sin(phi), cp = cos(phi);
+    const double st = (sin)(theta), ct = (cos)(theta), sp = (sin)(phi), cp = (cos)(phi);
     double xs, yss, zs, xss, zss, bxs, q[3];
     xs = (x - xc) * cp + (y - yc) * sp;
     yss = (y - yc) * cp - (x - xc) * sp;
@@ -770,17 +770,17 @@ static void t_r2sheet(double x, double y, double z, double b[3]) {
     const double px72 = 0.396953e-01 * 0.396953e-01;
     const double qx = sqrt(xks2 + px72);
     const double t2x = (px72 * 0.396953e-01) / (qx * qx * qx);
-    const double t3x = xks / pow(sqrt(xks2 + 0.579023e-01 * 0.579023e-01), 5) * 3.493856 * pow(0.579023e-01, 4);
+    const double t3x = xks / pow(sqrt(xks2 + 0.579023e-01 * 0.579023e-01), 5) * 3.493856 * (pow)(0.579023e-01, 4);
     const double t1y = xks / sqrt(xks2 + 0.478750e-01 * 0.478750e-01);
     const double py72 = 0.363750e-01 * 0.363750e-01;
     const double qy = sqrt(xks2 + py72);
     const double t2y = (py72 * 0.363750e-01) / (qy * qy * qy);
-    const double t3y = xks / pow(sqrt(xks2 + 0.567500e-01 * 0.567500e-01), 5) * 3.493856 * pow(0.567500e-01, 4);
+    const double t3y = xks / pow(sqrt(xks2 + 0.567500e-01 * 0.567500e-01), 5) * 3.493856 * (pow)(0.567500e-01, 4);
     const double t1z = xks / sqrt(xks2 + 0.355625e-01 * 0.355625e-01);
     const double pz72 = 0.318750e-01 * 0.318750e-01;
     const double qz = sqrt(xks2 + pz72);
     const double t2z = (pz72 * 0.318750e-01) / (qz * qz * qz);
-    const double t3z = xks / pow(sqrt(xks2 + 0.538750e-01 * 0.538750e-01), 5) * 3.493856 * pow(0.538750e-01, 4);
+    const double t3z = xks / pow(sqrt(xks2 + 0.538750e-01 * 0.538750e-01), 5) * 3.493856 * (pow)(0.538750e-01, 4);
     const double rho2 = x * x + y * y;
     const double r = sqrt(rho2 + z * z);
     const double rho = sqrt(rho2);
@@ -896,16 +896,16 @@ void orc_t96_gsm(const double *parmod, double x, double y, double z, double *bxo
     const double bt = sqrt(byimf * byimf + bzimf * bzimf);
     double theta = 0.0;
     if (byimf != 0.0 || bzimf != 0.0) {
-        theta = atan2(byimf, bzimf);
+        theta = (atan2)(byimf, bzimf);
         if (theta <= 0.0) theta += 6.2831853;
     }
-    const double ct = cos(theta), st = sin(theta);
-    const double eps = 718.5 * sqrt(pdyn) * bt * sin(theta / 2.);
+    const double ct = (cos)(theta), st = (sin)(theta);
+    const double eps = 718.5 * sqrt(pdyn) * bt * (sin)(theta / 2.);
     const double ys = y * ct - z * st, zs = z * ct + y * st;
     const double ysd = ys / 10.0;
     const double factimf = exp(x / 20.0 - ysd * ysd);
     const double oimfy = 0.7850 * byimf * factimf, oimfz = 0.7850 * bzimf * factimf;
-    const double xappa = pow(pdyn / 2.0, 0.14);
+    const double xappa = (pow)(pdyn / 2.0, 0.14);
     const double xappa3 = xappa * xappa * xappa;
     const double am = 70.0 / xappa;
     const double rho2 = y * y + z * z;

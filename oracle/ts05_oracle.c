@@ -676,7 +676,7 @@ static void s_full_rc(double x, double y, double z, double phi, double scsy, dou
     double bs[3], bas[3], bq[3];
     s_symm(s_ap, 0, xts, yts, zts, bs);
     s_symm(s_apprc, 1, xta, yta, zta, bas);
-    const double cp = cos(phi), sp = sin(phi);
+    const double cp = (cos)(phi), sp = (sin)(phi);
     const double xr = xta * cp - yta * sp, yr = xta * sp + yta * cp;
     s_prc_quad(xr, yr, zta, bq);
     const double bxq = bq[0] * cp + bq[1] * sp;
@@ -752,7 +752,7 @@ void orc_ts05_gsm(const double *parmod, double x, double y, double z, double *bx
     const double dst = parmod[1] * 0.8 - 13. * sqrt(pdyn);
     const double byimf = parmod[2], bzimf = parmod[3];
     const double w1 = parmod[4], w2 = parmod[5], w3 = parmod[6], w4 = parmod[7], w5 = parmod[8], w6 = parmod[9];
-    const double xappa = pow((pdyn / 2.), A[22]);
+    const double xappa = (pow)((pdyn / 2.), A[22]);
     const double xappa3 = xappa * xappa * xappa;
     const double xx = x * xappa, yy = y * xappa, zz = z * xappa;
     const double am = 34.586 / xappa;
@@ -779,16 +779,16 @@ void orc_ts05_gsm(const double *parmod, double x, double y, double z, double *bx
     const double bxcf = cf[0] * xappa3, bycf = cf[1] * xappa3, bzcf = cf[2] * xappa3;
     double dstt = -20.;
     if (dst < dstt) dstt = dst;
-    double znam = pow(fabs(dstt), 0.37);
+    double znam = (pow)(fabs(dstt), 0.37);
     const double dx1 = A[23] - A[24] / znam;
     const double dx2 = A[25] - A[26] / znam;
-    const double d = A[35] * exp(-w1 / A[36]) + A[68];
+    const double d = A[35] * (exp)(-w1 / A[36]) + A[68];
     double t1[3], t2[3];
     s_warped(xx, yy, zz, dx1, dx2, d, t1, t2);
     znam = fabs(dst);
     if (dst >= -20.) znam = 20.;
-    const double xk1 = A[31] * pow(znam / 20., A[32]);
-    const double xk2 = A[33] * pow(znam / 20., A[34]);
+    const double xk1 = A[31] * (pow)(znam / 20., A[32]);
+    const double xk2 = A[33] * (pow)(znam / 20., A[34]);
     /* birk_tot (birk_tot.c:4-123), R11 and R21 only */
     double f[3], h[3], r11[3], r21[3];
     s_birk_1n2(1, xx, yy, zz, xk1, f);
@@ -800,13 +800,13 @@ void orc_ts05_gsm(const double *parmod, double x, double y, double z, double *bx
     const double phi = A[37];
     znam = fabs(dst);
     if (dst >= -20.) znam = 20.;
-    const double scsy = A[27] * pow((20. / znam), A[28]) * xappa;
-    const double scpr = A[29] * pow((20. / znam), A[30]) * xappa;
+    const double scsy = A[27] * (pow)((20. / znam), A[28]) * xappa;
+    const double scpr = A[29] * (pow)((20. / znam), A[30]) * xappa;
     double src[3], prc[3];
     s_full_rc(xx, yy, zz, phi, scsy, scpr, src, prc);
     const double himf[3] = { 0., byimf, bzimf };
-    const double dlp1 = pow((pdyn / 2.), A[20]);
-    const double dlp2 = pow((pdyn / 2.), A[21]);
+    const double dlp1 = (pow)((pdyn / 2.), A[20]);
+    const double dlp2 = (pow)((pdyn / 2.), A[21]);
     const double tamp1 = A[1] + A[2] * dlp1 + A[3] * (A[38] * w1) / sqrt(w1 * w1 + A[38] * A[38]);
     const double tamp2 = A[5] + A[6] * dlp2 + A[7] * (A[39] * w2) / sqrt(w2 * w2 + A[39] * A[39]);
     const double a_src = A[9] + A[10] * (A[40] * w3) / sqrt(w3 * w3 + A[40] * A[40]) + A[11] * dst;

@@ -5,11 +5,11 @@ and driven two ways:
   * through its library functions (internal_recalc, internal_geo, t96_gsm,
     ts05_gsm, chaos_geo, calculate_field) via ctypes, giving field vectors and
     set-up blocks as exact hex floats;
-  * through its `cor` binary (`cor -p -i igrf14 [-e t96|ts05] INFILE`),
+  * through its `cor` binary (`cor -i igrf14 [-e t96|ts05] [-c chaos7.16] INFILE`),
     giving the printed rows and the CUTOFF line of whole rigidity scans.
 
 Run here (where the reference tree exists):  python tests/golden/make_golden.py [section ...]
-Sections: setup field scan0 scan_t96 scan_ts05.  The fixtures are small JSON
+Sections: setup field scan0 scan_t96 scan_ts05 scan_chaos nudge nudge_extra.  The fixtures are small JSON
 files; nothing on the GPU side reads the reference.
 """
 from __future__ import annotations
@@ -153,7 +153,9 @@ def make_field(lib) -> dict:
     pts = field_points(rng, 200, 1.0, 25.0) * ct.DEF_RE
     combos = {"igrf14": ("igrf14", None, None, None),
               "igrf14+t96": ("igrf14", "t96", None, T96_PARMOD),
-              "igrf14+ts05": ("igrf14", "ts05", None, TS05_PARMOD)}
+              "igrf14+ts05": ("igrf14", "ts05", None, TS05_PARMOD),
+              "igrf14+chaos7.16": ("igrf14", None, "chaos7.16", None),
+              "igrf14+t96+chaos7.16": ("igrf14", "t96", "chaos7.16", T96_PARMOD)}
     out["calculate_field"] = {"time": [2020, 6, 21, 173, 12, 0, 0], "points_m": hx(pts), "cases": {}}
     for key, (imod, emod, cmod, pm) in combos.items():
         pp = p1.copy()
@@ -164,6 +166,8 @@ def make_field(lib) -> dict:
         models[k] = lib.get_model(sym(lib, "internal_models"), imod.encode()); k += 1
         if emod:
             models[k] = lib.get_model(sym(lib, "external_models"), emod.encode()); k += 1
+        if cmod:
+            models[k] = lib.get_model(sym(lib, "crustal_models"), cmod.encode()); k += 1
         vals = []
         o = Vector()
         for x, y, z in pts:
@@ -248,6 +252,133 @@ def make_scan_ext(kind: str, n_sites: int = 200, rig: float = 0.05, dele: float 
             "parmod": pm, "sites": recs}
 
 
+def make_scan_chaos(n_sites: int = 12) -> dict:
+    """IGRF-14 + the CHAOS-7.16 crustal field on a coarse rigidity grid (each
+    field call costs the reference ~0.4 ms, so the set is kept small)."""
+    rng = np.random.default_rng(13)
+    lats = rng.choice(np.arange(-85, 86, 5), n_sites)
+    lons = rng.choice(np.arange(0, 360, 5), n_sites)
+    sites = [(float(a), float(o), float(a), float(o)) for a, o in zip(lats, lons)]
+    t7 = [2020, 1, 1, 1, 0, 0, 0]
+    recs = run_scan_set(sites, 0.5, 20.0, 0.5, t7, ["-i", "igrf14", "-c", "chaos7.16"], keep_text={0})
+    return {"config": "IGRF-14 + CHAOS-7.16 crustal at 2020-01-01, vertical, 20 km, 20 -> 0.5 GV by 0.5",
+            "rig": 0.5, "rk": 20.0, "del": 0.5, "time": t7, "model": "igrf14", "crustal": "chaos7.16",
+            "sites": recs}
+
+
+# ---- the reference's own sensitivity to a one-ulp libm change ------------------
+def _scan_agreement(g, res):
+    """Flag agreement and sites within one step of a scan result vs a golden set."""
+    d = g["del"]
+    n_traj = n_agree = ok = 0
+    for j, s in enumerate(g["sites"]):
+        st = res.status[res.offsets[j]:res.offsets[j + 1]]
+        mine = st == ct.TRAJ_ALLOWED
+        ref = np.zeros(len(st), bool)
+        ref[s["allowed"]] = True
+        n_traj += len(st)
+        n_agree += int(np.sum(mine == ref))
+        mine3 = [res.sites[j]["r_lower"], res.sites[j]["r_upper"], res.sites[j]["r_cutoff"]]
+        ok += all(abs(a - float(b)) <= d * 1.0000001 for a, b in zip(mine3, s["cutoff"]))
+    return n_agree / n_traj, ok / len(g["sites"])
+
+
+def make_nudge() -> dict:
+    """Runs the oracle whose libm results are each moved by one ulp (random
+    sign) on the golden scan sets and field points: how far the reference's
+    own results move under a one-ulp change of its math library."""
+    out = {"seeds": [1, 2, 3], "scans": {}, "fields": {}}
+    for name, ext in (("scan_t96.json", ct.EXTERNAL_T96), ("scan_ts05.json", ct.EXTERNAL_TS05)):
+        with open(os.path.join(HERE, name)) as f:
+            g = json.load(f)
+        p = ct.internal_setup(g["model"], g["time"], parmod=g["parmod"])
+        jobs = np.concatenate([ct.make_job(s["lat"], s["lon"], rig=g["rig"], rk=g["rk"], dele=g["del"],
+                                           the1=s["the1"], fi1=s["fi1"]) for s in g["sites"]])
+        stats = []
+        for seed in out["seeds"]:
+            res = pyoracle.scan_batch_nudged(jobs, p, ct.model_set(ct.INTERNAL_SH, ext), seed)
+            stats.append(_scan_agreement(g, res))
+        out["scans"][name] = {"flag_agreement": [a for a, _ in stats], "sites_within_one_step": [b for _, b in stats]}
+        print(name, stats)
+    with open(os.path.join(HERE, "field_kats.json")) as f:
+        kats = json.load(f)
+    lib = pyoracle.load_nudge()
+    for name, fn in (("t96_gsm", lib.orc_t96_gsm), ("ts05_gsm", lib.orc_ts05_gsm)):
+        g = kats[name]
+        pm = np.array([float.fromhex(v) for v in g["parmod"]])
+        pts = np.array([float.fromhex(v) for v in g["points"]]).reshape(-1, 3)
+        want = np.array([float.fromhex(v) for v in g["b"]]).reshape(-1, 3)
+        b = np.zeros(3)
+        worst = np.zeros(len(pts))
+        for seed in range(1, 9):
+            lib.orc_nudge_seed(seed)
+            for i, (x, y, z) in enumerate(pts):
+                fn(pm.ctypes.data, x, y, z, b[0:].ctypes.data, b[1:].ctypes.data, b[2:].ctypes.data)
+                rel = np.linalg.norm(b - want[i]) / max(np.linalg.norm(want[i]), 1e-300)
+                worst[i] = max(worst[i], rel)
+        out["fields"][name] = {"max_rel_dev": hx(worst)}
+        print(name, "median", np.median(worst), "max", worst.max())
+    return out
+
+
+def make_nudge_extra() -> dict:
+    """The CHAOS scan and field and the calculate_field cases of
+    nudge_sensitivity.json (kept apart from `nudge`: each nudged crustal scan
+    costs as much as the reference's)."""
+    path = os.path.join(HERE, "nudge_sensitivity.json")
+    with open(path) as f:
+        out = json.load(f)
+    with open(os.path.join(HERE, "scan_chaos.json")) as f:
+        g = json.load(f)
+    p = ct.internal_setup(g["model"], g["time"])
+    jobs = np.concatenate([ct.make_job(s["lat"], s["lon"], rig=g["rig"], rk=g["rk"], dele=g["del"],
+                                       the1=s["the1"], fi1=s["fi1"]) for s in g["sites"]])
+    stats = []
+    for seed in out["seeds"]:
+        res = pyoracle.scan_batch_nudged(jobs, p, ct.model_set(ct.INTERNAL_SH, ct.EXTERNAL_NONE, ct.CRUSTAL_CHAOS),
+                                         seed)
+        stats.append(_scan_agreement(g, res))
+    out["scans"]["scan_chaos.json"] = {"flag_agreement": [a for a, _ in stats],
+                                       "sites_within_one_step": [b for _, b in stats]}
+    print("scan_chaos.json", stats)
+    with open(os.path.join(HERE, "field_kats.json")) as f:
+        kat = json.load(f)["chaos_geo"]
+    lib = pyoracle.load_nudge()
+    G, H, nmax = ct.chaos_dense()
+    pts = np.array([float.fromhex(v) for v in kat["points"]]).reshape(-1, 3)
+    want = np.array([float.fromhex(v) for v in kat["b"]]).reshape(-1, 3)
+    b = np.zeros(3)
+    worst = np.zeros(len(pts))
+    for seed in range(1, 9):
+        lib.orc_nudge_seed(seed)
+        for i, (x, y, z) in enumerate(pts):
+            lib.orc_chaos_geo(x, y, z, G.ctypes.data, H.ctypes.data, nmax, b[0:].ctypes.data, b[1:].ctypes.data,
+                              b[2:].ctypes.data)
+            worst[i] = max(worst[i], np.linalg.norm(b - want[i]) / max(np.linalg.norm(want[i]), 1e-300))
+    out["fields"]["chaos_geo"] = {"max_rel_dev": hx(worst)}
+    print("chaos_geo", "median", np.median(worst), "max", worst.max())
+    with open(os.path.join(HERE, "field_kats.json")) as f:
+        cf = json.load(f)["calculate_field"]
+    pts = np.array([float.fromhex(v) for v in cf["points_m"]]).reshape(-1, 3)
+    out["calculate_field"] = {}
+    sets = {"igrf14+t96": (ct.EXTERNAL_T96, ct.CRUSTAL_NONE), "igrf14+ts05": (ct.EXTERNAL_TS05, ct.CRUSTAL_NONE),
+            "igrf14+chaos7.16": (ct.EXTERNAL_NONE, ct.CRUSTAL_CHAOS),
+            "igrf14+t96+chaos7.16": (ct.EXTERNAL_T96, ct.CRUSTAL_CHAOS)}
+    for key, (ext, crust) in sets.items():
+        case = cf["cases"][key]
+        p = ct.internal_setup("igrf14", cf["time"], parmod=[float.fromhex(v) for v in case["parmod"]])
+        want = np.array([float.fromhex(v) for v in case["b"]]).reshape(-1, 3)
+        models = ct.model_set(ct.INTERNAL_SH, ext, crust)
+        worst = np.zeros(len(pts))
+        for seed in range(1, 9):
+            lib.orc_nudge_seed(seed)
+            got = pyoracle.calculate_field_nudged(pts, p, models)
+            worst = np.maximum(worst, np.linalg.norm(got - want, axis=1) / np.linalg.norm(want, axis=1))
+        out["calculate_field"][key] = {"max_rel_dev": hx(worst)}
+        print(key, "median", np.median(worst), "max", worst.max())
+    return out
+
+
 def main(sections):
     lib = ref_lib()
     todo = {
@@ -256,6 +387,9 @@ def main(sections):
         "scan0": ("scan_config0.json", make_scan0),
         "scan_t96": ("scan_t96.json", lambda: make_scan_ext("t96")),
         "scan_ts05": ("scan_ts05.json", lambda: make_scan_ext("ts05")),
+        "scan_chaos": ("scan_chaos.json", make_scan_chaos),
+        "nudge": ("nudge_sensitivity.json", make_nudge),
+        "nudge_extra": ("nudge_sensitivity.json", make_nudge_extra),
     }
     for s in sections or list(todo):
         fn, mk = todo[s]

@@ -158,43 +158,58 @@ def _scan_golden(name, models):
     return g, p, jobs
 
 
-def test_scan_t96_matches_reference(ctx):
-    """IGRF-14 + T96, 200 sites x 400 rigidities against the reference's own scans:
-    allowed/forbidden flags agree on >= 99.9% of trajectories, every
-    disagreement lies inside the scan's penumbra [P(S), P(C)], and P(S), P(C),
-    P(M) agree within one rigidity step at >= 99.5% of sites."""
-    models = ct.model_set(ct.INTERNAL_SH, ct.EXTERNAL_T96)
-    g, p, jobs = _scan_golden("scan_t96.json", models)
-    res = ctx.trace_batch(jobs, p, models=models)
-    n_traj = n_agree = 0
-    sites_ok = 0
-    outside = []
-    off_sites = []
+# ---- scans with the external and crustal fields ------------------------------
+# These fields call the C library's exp/log/sin/cos/atan/pow, which the device
+# evaluates with CUDA's own functions; trajectories near the cutoff are
+# chaotic, so a last-bit difference can flip an allowed/forbidden flag.  The
+# bar is the reference's own: nudge_sensitivity.json holds how well the
+# reference agrees with itself when every libm result is moved by one ulp
+# (three seeds).  The GPU must do at least NUDGE_FACTOR times as well on both
+# counts (flags that differ; sites whose P(S), P(C) or P(M) is off by more than
+# one rigidity step), and every flag that differs must lie inside the scan's
+# penumbra [P(S), P(C)] widened by one step.
+NUDGE_FACTOR = 2.0
+
+
+def _scan_vs_reference(name, res, label):
+    g = golden(name)
+    nudge = golden("nudge_sensitivity.json")["scans"][name]
     d = g["del"]
+    n_traj = n_diff = sites_off = 0
+    outside, off = [], []
     for j, s in enumerate(g["sites"]):
         st = res.status[res.offsets[j]:res.offsets[j + 1]]
         mine = st == ct.TRAJ_ALLOWED
         ref = np.zeros(len(st), bool)
         ref[s["allowed"]] = True
         n_traj += len(st)
-        n_agree += int(np.sum(mine == ref))
+        n_diff += int(np.sum(mine != ref))
         lo = min(float(s["cutoff"][0]), res.sites[j]["r_lower"]) - d
         hi = max(float(s["cutoff"][1]), res.sites[j]["r_upper"]) + d
         rig = g["rig"] + np.arange(len(st)) * d
-        bad = np.nonzero(mine != ref)[0]
-        outside += [(j, float(rig[i])) for i in bad if not (lo <= rig[i] <= hi)]
+        outside += [(j, float(rig[i])) for i in np.nonzero(mine != ref)[0] if not (lo <= rig[i] <= hi)]
         mine3 = [res.sites[j]["r_lower"], res.sites[j]["r_upper"], res.sites[j]["r_cutoff"]]
-        if all(abs(a - float(b)) <= d * 1.0000001 for a, b in zip(mine3, s["cutoff"])):
-            sites_ok += 1
-        else:
-            off_sites.append((s["lat"], s["lon"], [round(float(v), 3) for v in mine3], s["cutoff"],
-                              int(np.sum(mine != ref))))
-    print(f"T96 scan: flag agreement {n_agree / n_traj:.5f}, sites within one step {sites_ok}/{len(g['sites'])}")
-    for o in off_sites:
-        print("  site off by more than one step (lat, lon, gpu, reference, flipped):", o)
-    assert n_agree / n_traj >= 0.999
+        if not all(abs(a - float(b)) <= d * 1.0000001 for a, b in zip(mine3, s["cutoff"])):
+            sites_off += 1
+            off.append((s["lat"], s["lon"], [round(float(v), 3) for v in mine3], s["cutoff"]))
+    n_sites = len(g["sites"])
+    ref_diff = max(1.0 - a for a in nudge["flag_agreement"]) * n_traj
+    ref_off = max(1.0 - a for a in nudge["sites_within_one_step"]) * n_sites
+    print(f"{label}: flags differing {n_diff}/{n_traj} (reference vs itself, one-ulp libm: up to "
+          f"{ref_diff:.0f}), sites off by more than one step {sites_off}/{n_sites} (reference vs itself: "
+          f"up to {ref_off:.0f})")
+    for o in off:
+        print("  site off by more than one step (lat, lon, gpu, reference):", o)
     assert not outside, outside[:10]
-    assert sites_ok / len(g["sites"]) >= 0.995
+    assert n_diff <= NUDGE_FACTOR * ref_diff + 1
+    assert sites_off <= NUDGE_FACTOR * ref_off + 1
+
+
+def test_scan_t96_matches_reference(ctx):
+    """IGRF-14 + T96, 200 sites x 400 rigidities against the reference's own scans."""
+    models = ct.model_set(ct.INTERNAL_SH, ct.EXTERNAL_T96)
+    g, p, jobs = _scan_golden("scan_t96.json", models)
+    _scan_vs_reference("scan_t96.json", ctx.trace_batch(jobs, p, models=models), "T96 scan")
 
 
 def test_scan_t96_equals_oracle_statistics(ctx):
@@ -215,10 +230,14 @@ def test_scan_t96_equals_oracle_statistics(ctx):
 # ---- TS05 -----------------------------------------------------------------
 # TS05 takes central differences with steps of 1e-6 and 1e-4 (birk_tot.c:267-275,
 # full_rc.c:119-146), which turn one ulp of difference in a transcendental into
-# up to ~1e-8 of relative change in the field.  Its tolerance is therefore the
-# point's own conditioning: TS05_RTOL_K times the relative change the oracle
-# shows for a one-ulp nudge of the position, and at least FIELD_RTOL.
+# up to ~1e-8 of relative change in the field.  Its tolerance per point is
+# therefore the point's own conditioning, whichever is larger of
+# TS05_RTOL_K times the relative change the oracle shows for a one-ulp nudge
+# of the position and NUDGE_RTOL_K times the largest change the reference
+# shows when every libm result is moved by one ulp (nudge_sensitivity.json),
+# and at least FIELD_RTOL.
 TS05_RTOL_K = 64.0
+NUDGE_RTOL_K = 16.0
 
 
 def _ts05_sensitivity(pts, pm):
@@ -247,7 +266,8 @@ def test_field_ts05_kats(ctx):
     got = ctx.field_batch(pts * ct.DEF_RE, p, models=ct.model_set(ct.INTERNAL_NONE, ct.EXTERNAL_TS05))
     exact = np.all(((pts * ct.DEF_RE) / ct.DEF_RE) == pts, axis=1)
     err = _rel_err(got[exact], want[exact])
-    tol = np.maximum(FIELD_RTOL, TS05_RTOL_K * _ts05_sensitivity(pts[exact], pm))
+    nudge = unhex(golden("nudge_sensitivity.json")["fields"]["ts05_gsm"]["max_rel_dev"])[exact]
+    tol = np.maximum(FIELD_RTOL, np.maximum(TS05_RTOL_K * _ts05_sensitivity(pts[exact], pm), NUDGE_RTOL_K * nudge))
     print(f"ts05 KAT: {exact.sum()} points, max rel err {err.max():.3e}, median {np.median(err):.3e}, "
           f"points above 1e-12: {np.sum(err > FIELD_RTOL)}, max err/tol {np.max(err / tol):.3f}")
     assert np.all(err <= tol)
@@ -262,34 +282,87 @@ def test_field_igrf_ts05_calculate_field(ctx):
     want = unhex(case["b"]).reshape(-1, 3)
     got = ctx.field_batch(pts, p, models=ct.model_set(ct.INTERNAL_SH, ct.EXTERNAL_TS05))
     err = _rel_err(got, want)
-    print(f"igrf14+ts05 calculate_field: max rel err {err.max():.3e}")
-    assert err.max() <= 1e-9
+    nudge = unhex(golden("nudge_sensitivity.json")["calculate_field"]["igrf14+ts05"]["max_rel_dev"])
+    tol = np.maximum(FIELD_RTOL, NUDGE_RTOL_K * nudge)
+    print(f"igrf14+ts05 calculate_field: max rel err {err.max():.3e}, max err/tol {np.max(err / tol):.3f}")
+    assert np.all(err <= tol)
 
 
 def test_scan_ts05_matches_reference(ctx):
-    """IGRF-14 + TS05 scans against the reference's: flag agreement >= 99.9%,
-    disagreements inside the penumbra, cutoffs within one step at >= 99.5%."""
+    """IGRF-14 + TS05, 200 sites x 400 rigidities against the reference's own scans."""
     models = ct.model_set(ct.INTERNAL_SH, ct.EXTERNAL_TS05)
     g, p, jobs = _scan_golden("scan_ts05.json", models)
-    res = ctx.trace_batch(jobs, p, models=models)
-    n_traj = n_agree = sites_ok = 0
-    outside = []
-    d = g["del"]
-    for j, s in enumerate(g["sites"]):
-        st = res.status[res.offsets[j]:res.offsets[j + 1]]
-        mine = st == ct.TRAJ_ALLOWED
-        ref = np.zeros(len(st), bool)
-        ref[s["allowed"]] = True
-        n_traj += len(st)
-        n_agree += int(np.sum(mine == ref))
-        lo = min(float(s["cutoff"][0]), res.sites[j]["r_lower"]) - d
-        hi = max(float(s["cutoff"][1]), res.sites[j]["r_upper"]) + d
-        rig = g["rig"] + np.arange(len(st)) * d
-        outside += [(j, float(rig[i])) for i in np.nonzero(mine != ref)[0] if not (lo <= rig[i] <= hi)]
-        mine3 = [res.sites[j]["r_lower"], res.sites[j]["r_upper"], res.sites[j]["r_cutoff"]]
-        if all(abs(a - float(b)) <= d * 1.0000001 for a, b in zip(mine3, s["cutoff"])):
-            sites_ok += 1
-    print(f"TS05 scan: flag agreement {n_agree / n_traj:.5f}, sites within one step {sites_ok}/{len(g['sites'])}")
-    assert n_agree / n_traj >= 0.999
-    assert not outside, outside[:10]
-    assert sites_ok / len(g["sites"]) >= 0.995
+    _scan_vs_reference("scan_ts05.json", ctx.trace_batch(jobs, p, models=models), "TS05 scan")
+
+
+# ---- CHAOS-7.16 crustal field ------------------------------------------------
+# The device sums the reference's terms in the reference's order; its atan2,
+# sin and cos are not glibc's.  The bound per point is NUDGE_RTOL_K times the
+# largest relative change the reference itself shows when every libm result
+# is moved by one ulp (nudge_sensitivity.json), and at least FIELD_RTOL.
+
+
+def _identity_rotation(p):
+    p["a1"][0], p["a2"][0], p["a3"][0] = [1, 0, 0], [0, 1, 0], [0, 0, 1]
+    return p
+
+
+def test_field_chaos_kats(ctx):
+    g = golden("field_kats.json")["chaos_geo"]
+    dev = unhex(golden("nudge_sensitivity.json")["fields"]["chaos_geo"]["max_rel_dev"])
+    p = _identity_rotation(ct.internal_setup("igrf14", [2020, 1, 1, 1, 0, 0, 0]))
+    pts = unhex(g["points"]).reshape(-1, 3)
+    want = unhex(g["b"]).reshape(-1, 3)
+    got = ctx.field_batch(pts * ct.DEF_RE, p,
+                          models=ct.model_set(ct.INTERNAL_NONE, ct.EXTERNAL_NONE, ct.CRUSTAL_CHAOS))
+    exact = np.all(((pts * ct.DEF_RE) / ct.DEF_RE) == pts, axis=1)
+    err = _rel_err(got[exact], want[exact])
+    tol = np.maximum(FIELD_RTOL, NUDGE_RTOL_K * dev[exact])
+    print(f"chaos KAT: {exact.sum()} points, max rel err {err.max():.3e}, median {np.median(err):.3e}, "
+          f"max err/tol {np.max(err / tol):.3f}")
+    assert exact.sum() >= len(pts) // 2
+    assert np.all(err <= tol)
+
+
+@pytest.mark.parametrize("key,ext", [("igrf14+chaos7.16", ct.EXTERNAL_NONE),
+                                     ("igrf14+t96+chaos7.16", ct.EXTERNAL_T96)])
+def test_field_crustal_calculate_field(ctx, key, ext):
+    g = golden("field_kats.json")["calculate_field"]
+    case = g["cases"][key]
+    p = ct.internal_setup("igrf14", g["time"], parmod=unhex(case["parmod"]))
+    pts = unhex(g["points_m"]).reshape(-1, 3)
+    want = unhex(case["b"]).reshape(-1, 3)
+    got = ctx.field_batch(pts, p, models=ct.model_set(ct.INTERNAL_SH, ext, ct.CRUSTAL_CHAOS))
+    err = _rel_err(got, want)
+    print(f"{key} calculate_field: max rel err {err.max():.3e}")
+    assert err.max() <= FIELD_RTOL
+
+
+def test_crustal_table_upload(ctx):
+    """An all-zero crustal table adds exactly nothing: the run-time-dispatch
+    kernel then gives the IGRF field bit for bit.  Out-of-range sizes fail."""
+    g = golden("field_kats.json")["calculate_field"]
+    p = ct.internal_setup("igrf14", g["time"])
+    pts = unhex(g["points_m"]).reshape(-1, 3)
+    nmax = 30
+    zero = np.zeros(nmax * (nmax + 1) // 2)
+    c2 = ct.Context(0)
+    try:
+        c2.upload_crustal(zero, zero, nmax)
+        got = c2.field_batch(pts, p, models=ct.model_set(ct.INTERNAL_SH, ct.EXTERNAL_NONE, ct.CRUSTAL_CHAOS))
+        want = c2.field_batch(pts, p, models=ct.model_set(ct.INTERNAL_SH))
+        assert np.array_equal(got.view(np.uint64), want.view(np.uint64))
+        with pytest.raises(ct.CorError) as e:
+            c2.upload_crustal(np.zeros(193 * 194 // 2), np.zeros(193 * 194 // 2), 193)
+        assert e.value.code == -7  # COR_ERR_RANGE
+    finally:
+        c2.close()
+
+
+def test_scan_chaos_matches_reference(ctx):
+    """IGRF-14 + CHAOS-7.16, 12 sites x 40 rigidities against the reference's scans."""
+    models = ct.model_set(ct.INTERNAL_SH, ct.EXTERNAL_NONE, ct.CRUSTAL_CHAOS)
+    g = golden("scan_chaos.json")
+    p = ct.internal_setup(g["model"], g["time"])
+    jobs = config0_jobs(g["sites"], g["rig"], g["rk"], g["del"])
+    _scan_vs_reference("scan_chaos.json", ctx.trace_batch(jobs, p, models=models), "CHAOS scan")

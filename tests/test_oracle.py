@@ -120,3 +120,16 @@ def test_oracle_calculate_field_external_bit_exact():
         want = unhex(case["b"]).reshape(-1, 3)
         got = pyoracle.calculate_field(pts, p, models=ct.model_set(ct.INTERNAL_SH, ext))
         assert np.array_equal(got.view(np.uint64), want.view(np.uint64)), key
+
+
+def test_oracle_calculate_field_crustal_bit_exact():
+    """calculate_field with the CHAOS-7.16 crustal model (chaos_7_16_calc,
+    src/models.c:179-192), alone with IGRF-14 and together with T96."""
+    g = golden("field_kats.json")["calculate_field"]
+    pts = unhex(g["points_m"]).reshape(-1, 3)
+    for key, ext in (("igrf14+chaos7.16", ct.EXTERNAL_NONE), ("igrf14+t96+chaos7.16", ct.EXTERNAL_T96)):
+        case = g["cases"][key]
+        p = ct.internal_setup("igrf14", g["time"], parmod=unhex(case["parmod"]))
+        want = unhex(case["b"]).reshape(-1, 3)
+        got = pyoracle.calculate_field(pts, p, models=ct.model_set(ct.INTERNAL_SH, ext, ct.CRUSTAL_CHAOS))
+        assert np.array_equal(got.view(np.uint64), want.view(np.uint64)), key
