@@ -22,7 +22,7 @@ int main(int argc, char** argv) {
     if (fread(jobs, sizeof(cor_scan_job), nj, fj) != (size_t)nj) return 4;
     if (fread(&params, sizeof params, 1, fp) != 1) return 5;
     cor_model_set ms = {atoi(argv[3]), atoi(argv[4]), atoi(argv[5]), 0};
-    uint64_t steps = 0, trials = 0, ops = 0, trans = 0;
+    uint64_t steps = 0, trials = 0, ops = 0, trans = 0, by_class[FC_N] = {0};
     for (long j = 0; j < nj; j++) {
         cor_counters c;
         memset(&c, 0, sizeof c);
@@ -33,9 +33,15 @@ int main(int argc, char** argv) {
         trials += c.trials;
         ops += g_tally.ops;
         trans += g_tally.trans;
+        for (int k = 0; k < FC_N; k++) by_class[k] += g_tally.by_class[k];
     }
-    printf("{\"scans\": %ld, \"accepted_steps\": %llu, \"trials\": %llu, \"ops\": %llu, \"transcendentals\": %llu}\n",
+    static const char* names[FC_N] = {"add", "mul", "div", "sqrt", "exp", "log", "sin", "cos", "tan", "atan", "asin",
+                                      "atan2", "pow", "fmod"};
+    printf("{\"scans\": %ld, \"accepted_steps\": %llu, \"trials\": %llu, \"ops\": %llu, \"transcendentals\": %llu",
            nj, (unsigned long long)steps, (unsigned long long)trials, (unsigned long long)ops,
            (unsigned long long)trans);
+    printf(", \"by_class\": {");
+    for (int k = 0; k < FC_N; k++) printf("%s\"%s\": %llu", k ? ", " : "", names[k], (unsigned long long)by_class[k]);
+    printf("}}\n");
     return 0;
 }

@@ -75,6 +75,7 @@ def main(name: str) -> dict:
         "flops_per_step": flops / c["accepted_steps"],
         "flops_per_rejected_trial": 0.0,
         "trials_per_step": c["trials"] / c["accepted_steps"],
+        "per_step_by_class": {k: v / c["accepted_steps"] for k, v in c["by_class"].items()},
         "source": "op-counting build of the oracle on a seeded sample (rejected trials included per step)",
     }
     with open(os.path.join(ORACLE, f"work_model_{name}.json"), "w") as f:

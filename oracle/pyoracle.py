@@ -66,7 +66,7 @@ def load_nudge() -> C.CDLL:
     return _nudge
 
 
-def scan_batch_nudged(jobs, params, models, seed: int, threads=8):
+def scan_batch_nudged(jobs, params, models, seed: int, threads=8, step_limit=25000):
     """orc_scan_batch of the one-ulp-perturbed oracle (each thread reseeds
     from `seed` and the job order, so the result is reproducible only per
     job; the statistics, not the bits, are what matter)."""
@@ -76,7 +76,7 @@ def scan_batch_nudged(jobs, params, models, seed: int, threads=8):
     n, off = ct.batch_offsets(jobs)
     sites = np.zeros(len(jobs), ct.SITE_DTYPE)
     status = np.zeros(n, np.uint8)
-    req = ct.BatchReq(_p(jobs), len(jobs), len(params), _p(params), models, 25000, 0.01, ct.DEF_HM0_P)
+    req = ct.BatchReq(_p(jobs), len(jobs), len(params), _p(params), models, step_limit, 0.01, ct.DEF_HM0_P)
     cnt = ct.Counters()
     _crustal(lib, models)
     lib.orc_nudge_seed(seed)

@@ -253,17 +253,20 @@ def make_scan_ext(kind: str, n_sites: int = 200, rig: float = 0.05, dele: float 
 
 
 def make_scan_chaos(n_sites: int = 12) -> dict:
-    """IGRF-14 + the CHAOS-7.16 crustal field on a coarse rigidity grid (each
-    field call costs the reference ~0.4 ms, so the set is kept small)."""
+    """IGRF-14 + the CHAOS-7.16 crustal field on a coarse rigidity grid with
+    the reference's -s option lowering the step limit to 2000 (each field call
+    costs the reference ~0.4 ms, so the set is kept small)."""
     rng = np.random.default_rng(13)
     lats = rng.choice(np.arange(-85, 86, 5), n_sites)
     lons = rng.choice(np.arange(0, 360, 5), n_sites)
     sites = [(float(a), float(o), float(a), float(o)) for a, o in zip(lats, lons)]
     t7 = [2020, 1, 1, 1, 0, 0, 0]
-    recs = run_scan_set(sites, 0.5, 20.0, 0.5, t7, ["-i", "igrf14", "-c", "chaos7.16"], keep_text={0})
-    return {"config": "IGRF-14 + CHAOS-7.16 crustal at 2020-01-01, vertical, 20 km, 20 -> 0.5 GV by 0.5",
+    recs = run_scan_set(sites, 0.5, 20.0, 0.5, t7, ["-i", "igrf14", "-c", "chaos7.16", "-s", "2000"],
+                        keep_text={0})
+    return {"config": "IGRF-14 + CHAOS-7.16 crustal at 2020-01-01, vertical, 20 km, 20 -> 0.5 GV by 0.5, "
+                      "2000-step limit (-s 2000)",
             "rig": 0.5, "rk": 20.0, "del": 0.5, "time": t7, "model": "igrf14", "crustal": "chaos7.16",
-            "sites": recs}
+            "step_limit": 2000, "sites": recs}
 
 
 # ---- the reference's own sensitivity to a one-ulp libm change ------------------
@@ -336,7 +339,7 @@ def make_nudge_extra() -> dict:
     stats = []
     for seed in out["seeds"]:
         res = pyoracle.scan_batch_nudged(jobs, p, ct.model_set(ct.INTERNAL_SH, ct.EXTERNAL_NONE, ct.CRUSTAL_CHAOS),
-                                         seed)
+                                         seed, step_limit=g["step_limit"])
         stats.append(_scan_agreement(g, res))
     out["scans"]["scan_chaos.json"] = {"flag_agreement": [a for a, _ in stats],
                                        "sites_within_one_step": [b for _, b in stats]}

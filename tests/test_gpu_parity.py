@@ -360,9 +360,11 @@ def test_crustal_table_upload(ctx):
 
 
 def test_scan_chaos_matches_reference(ctx):
-    """IGRF-14 + CHAOS-7.16, 12 sites x 40 rigidities against the reference's scans."""
+    """IGRF-14 + CHAOS-7.16, 12 sites x 40 rigidities with a 2000-step limit
+    (the reference's -s 2000) against the reference's scans."""
     models = ct.model_set(ct.INTERNAL_SH, ct.EXTERNAL_NONE, ct.CRUSTAL_CHAOS)
     g = golden("scan_chaos.json")
     p = ct.internal_setup(g["model"], g["time"])
     jobs = config0_jobs(g["sites"], g["rig"], g["rk"], g["del"])
-    _scan_vs_reference("scan_chaos.json", ctx.trace_batch(jobs, p, models=models), "CHAOS scan")
+    res = ctx.trace_batch(jobs, p, models=models, step_limit=g["step_limit"])
+    _scan_vs_reference("scan_chaos.json", res, "CHAOS scan")
