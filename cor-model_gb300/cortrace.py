@@ -83,7 +83,9 @@ EXPORTS = [
     "cor_ctx_create", "cor_ctx_destroy", "cor_last_error_string", "cor_abi_version", "cor_batch_count",
     "cor_prepare_trig", "cor_trace_batch", "cor_trace_batch_device", "cor_upload_params", "cor_field_batch",
     "cor_internal_setup", "cor_gsm_setup", "cor_probe_fp64_peak", "cor_upload_crustal",
+    "cor_trace_batch_device_noalloc",
 ]
+NOALLOC_MAX_TRAJ = 1048576  # COR_NOALLOC_MAX_TRAJ
 
 _lib = None
 
@@ -109,6 +111,8 @@ def load(path: str = LIB_PATH) -> C.CDLL:
                                            vp, vp, vp, vp, C.c_uint32, vp]
     lib.cor_upload_params.argtypes = [vp, vp, i32]
     lib.cor_upload_crustal.argtypes = [vp, vp, vp, i32]
+    lib.cor_trace_batch_device_noalloc.argtypes = [vp, vp, vp, i32, vp, u64, ModelSet, u64, dbl, dbl,
+                                                   vp, vp, vp, C.c_uint32, vp]
     lib.cor_probe_fp64_peak.argtypes = [vp, C.POINTER(C.c_double)]
     lib.cor_field_batch.argtypes = [vp, ModelSet, vp, i32, vp, vp, i64, vp]
     lib.cor_internal_setup.argtypes = [C.c_char_p, vp, vp]

@@ -3,6 +3,7 @@
 #include <cuda_runtime.h>
 
 #include <math.h>
+#include <mutex>
 #include <stdarg.h>
 #include <stdio.h>
 #include <stdlib.h>
@@ -849,5 +850,129 @@ extern "C" int cor_probe_fp64_peak(cor_ctx* ctx, double* flops_per_s) {
     cudaFree(out);
     if (e != cudaSuccess) return fail(ctx, COR_ERR_CUDA, "fp64 probe: %s", cudaGetErrorString(e));
     *flops_per_s = 2.0 * 8.0 * iters * (double)blocks * threads / (best * 1e-3);
+    return COR_OK;
+}
+
+// ---- scan without allocation ------------------------------------------------
+// cor_trace_batch_device_noalloc keeps its scratch in one file-scope device
+// array instead of context buffers: the work-queue counter, the generation
+// counters and the counters block (first 256 bytes), then the per-trajectory
+// termination classes the reduction reads (COR_NOALLOC_MAX_TRAJ bytes).  It
+// runs the scan as a single generation (no park buffers: those scale with the
+// resident threads, ~25 MB) and never calls cudaMalloc or cudaFree.  Every call
+// on every context of a device shares the array, so calls that overlap on the
+// GPU race on it.
+struct NoAllocHead {
+    unsigned long long queue;
+    unsigned long long pad0[7];
+    GenCounters gen;
+    unsigned long long pad1[6];
+    cor_counters counters;
+};
+static_assert(sizeof(NoAllocHead) <= 256, "no-alloc scratch header exceeds 256 bytes");
+constexpr size_t kNoAllocHead = 256;
+static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocHead + COR_NOALLOC_MAX_TRAJ];
+
+constexpr int kNoAllocMaxDevices = 64;
+static std::mutex g_noalloc_mu;
+static unsigned char* g_noalloc_ptr[kNoAllocMaxDevices];
+
+// Device address of the scratch array on ctx's device (current); looked up once
+// per device, which also loads this library's device code there.
+static int noalloc_scratch(cor_ctx* ctx, unsigned char** out) {
+    if (ctx->device < 0 || ctx->device >= kNoAllocMaxDevices)
+        return fail(ctx, COR_ERR_RANGE, "device %d beyond the %d the no-alloc path tracks", ctx->device,
+                    kNoAllocMaxDevices);
+    std::lock_guard<std::mutex> lock(g_noalloc_mu);
+    if (!g_noalloc_ptr[ctx->device]) {
+        void* p = nullptr;
+        const cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+        if (e != cudaSuccess)
+            return fail(ctx, COR_ERR_CUDA, "cudaGetSymbolAddress(no-alloc scratch): %s", cudaGetErrorString(e));
+        g_noalloc_ptr[ctx->device] = (unsigned char*)p;
+    }
+    *out = g_noalloc_ptr[ctx->device];
+    return COR_OK;
+}
+
+__global__ void noalloc_launches_kernel(cor_counters* c, unsigned long long launches) { c->kernel_launches = launches; }
+
+extern "C" int cor_trace_batch_device_noalloc(cor_ctx* ctx, const cor_scan_job* jobs_dev, const cor_job_trig* trig_dev,
+                                              int32_t n_jobs, const uint64_t* offsets_dev, uint64_t n_traj,
+                                              cor_model_set models, uint64_t step_limit, double tu_angle,
+                                              double particle_mass, cor_site_result* sites_dev,
+                                              cor_traj_record* records_dev, cor_counters* counters_dev,
+                                              uint32_t flags, void* stream) {
+    if (!ctx) return COR_ERR_INVALID;
+    int rc = check_req(ctx, models, ctx->n_params, step_limit, tu_angle, particle_mass);
+    if (rc != COR_OK) return rc;
+    if (n_traj > (uint64_t)COR_NOALLOC_MAX_TRAJ)
+        return fail(ctx, COR_ERR_RANGE, "%llu trajectories exceed the no-alloc maximum of %d per call",
+                    (unsigned long long)n_traj, COR_NOALLOC_MAX_TRAJ);
+    if (n_jobs < 0 || (n_jobs > 0 && (!jobs_dev || !trig_dev || !offsets_dev || !sites_dev)))
+        return fail(ctx, COR_ERR_INVALID, "missing device buffer");
+    if (models.crustal_model != COR_CRUSTAL_NONE && !ctx->crust)
+        return fail(ctx, COR_ERR_INVALID, "crustal table not resident: call cor_upload_crustal first");
+    CUDA_TRY(ctx, cudaSetDevice(ctx->device));
+    unsigned char* scratch = nullptr;
+    if ((rc = noalloc_scratch(ctx, &scratch)) != COR_OK) return rc;
+    NoAllocHead* head = (NoAllocHead*)scratch;
+    uint8_t* status = scratch + kNoAllocHead;
+    cudaStream_t s = (cudaStream_t)stream;
+
+    TraceArgs a;
+    memset(&a, 0, sizeof a);
+    a.jobs = jobs_dev;
+    a.trig = reinterpret_cast<const JobTrig*>(trig_dev);
+    a.offsets = offsets_dev;
+    a.n_jobs = n_jobs;
+    a.n_traj = n_traj;
+    a.params = (const DevParams*)ctx->params.p;
+    a.step_limit = step_limit;
+    a.tu_angle = tu_angle;
+    a.gc_reject = 0.;
+    a.turn_exact = find_turn_threshold(tu_angle, &a.gc_reject) ? 1 : 0;
+    a.n_rig = 0;
+    if (n_jobs > 0 && n_traj % (uint64_t)n_jobs == 0) a.n_rig = (uint32_t)(n_traj / (uint64_t)n_jobs);
+    a.rig_major = ((flags & COR_FLAG_UNIFORM_GRID) && a.n_rig > 0) ? 1 : 0;
+    a.mass = particle_mass;
+    a.status = status;
+    a.records = records_dev;
+    a.queue = &head->queue;
+    a.counters = counters_dev ? counters_dev : &head->counters;
+    a.gen = &head->gen;
+    if ((rc = crustal_tables(ctx, models, &a.crust)) != COR_OK) return rc;
+    a.restore = nullptr;
+    a.n_restore = 0;
+    a.park = nullptr;
+    a.allow_park = 0;
+    a.park_below = 0;
+
+    // the header keeps the previous call's values: clear it
+    CUDA_TRY(ctx, cudaMemsetAsync(scratch, 0, kNoAllocHead, s));
+    if (counters_dev) CUDA_TRY(ctx, cudaMemsetAsync(counters_dev, 0, sizeof(cor_counters), s));
+    unsigned long long launches = 0;
+    if (n_traj > 0) {
+        const ModelOps* ops = find_ops(models);
+        if (!ops) return fail(ctx, COR_ERR_UNSUPPORTED, "model set not available");
+        int per_sm = 0;
+        CUDA_TRY(ctx, ops->occupancy(&per_sm));
+        if (per_sm < 1) per_sm = 1;
+        uint64_t blocks = (n_traj + 127) / 128;
+        const uint64_t cap = (uint64_t)ctx->sms * (uint64_t)per_sm;
+        if (blocks > cap) blocks = cap;
+        a.launched_warps = (uint32_t)(blocks * 4);
+        CUDA_TRY(ctx, ops->launch_generation(a, (unsigned)blocks, s));
+        launches++;
+    }
+    if (n_jobs > 0) {
+        const int threads = 256;
+        const int blocks = (int)(((int64_t)n_jobs * 32 + threads - 1) / threads);
+        reduce_kernel<<<blocks, threads, 0, s>>>(jobs_dev, offsets_dev, n_jobs, status, sites_dev);
+        CUDA_TRY(ctx, cudaGetLastError());
+        launches++;
+    }
+    noalloc_launches_kernel<<<1, 1, 0, s>>>(a.counters, launches + 1);
+    CUDA_TRY(ctx, cudaGetLastError());
     return COR_OK;
 }

@@ -223,6 +223,38 @@ int cor_trace_batch_device(cor_ctx *ctx,
                            cor_traj_record *records_dev, cor_counters *counters_dev,
                            uint32_t flags, void *stream);
 
+/* Largest n_trajectories one cor_trace_batch_device_noalloc call accepts. */
+#define COR_NOALLOC_MAX_TRAJ 1048576
+
+/* The scan of cor_trace_batch_device without any device allocation: it calls
+ * no cudaMalloc, cudaFree or other allocating routine.  It has no counterpart
+ * in the reference.  Its scratch is one file-scope device array of
+ * 256 + COR_NOALLOC_MAX_TRAJ bytes (the work-queue counter, the generation and
+ * counter blocks, and the per-trajectory termination classes the reduction
+ * reads), so the per-trajectory classes are not returned (there is no
+ * status_dev); n_trajectories above COR_NOALLOC_MAX_TRAJ gives COR_ERR_RANGE
+ * before any GPU work.  It runs the scan as one kernel generation (no
+ * regrouping, whose park buffers would need memory), then the reduction, and
+ * returns with both queued on `stream` without synchronising it.  Results
+ * (sites, records, counters) are identical to cor_trace_batch_device's.
+ * Preconditions: the parameter blocks are resident (cor_upload_params) and,
+ * for a model set with the crustal model, so is its table (cor_upload_crustal)
+ * -- otherwise COR_ERR_INVALID.
+ * The first call on a device looks up the array's device address there
+ * (cudaGetSymbolAddress, which may load this library's device code onto that
+ * device); make that first call before any stream capture on the device.
+ * Every call, on every context of the device, shares the array and finds the
+ * previous call's contents in it (the call clears what must start at zero):
+ * calls whose work overlaps on the GPU race on it and must be serialised by
+ * the caller, e.g. by issuing them all on one stream. */
+int cor_trace_batch_device_noalloc(cor_ctx *ctx,
+                                   const cor_scan_job *jobs_dev, const cor_job_trig *trig_dev,
+                                   int32_t n_jobs, const uint64_t *offsets_dev, uint64_t n_trajectories,
+                                   cor_model_set models, uint64_t step_limit,
+                                   double tu_angle, double particle_mass,
+                                   cor_site_result *sites_dev, cor_traj_record *records_dev,
+                                   cor_counters *counters_dev, uint32_t flags, void *stream);
+
 /* ---- field ------------------------------------------------------------ */
 /* calculate_field (src/models.c:194-207) at n points: gsm_pos is n x 3 GSM
  * positions in metres; geo_field gets n x 3 GEO field components in nT.
