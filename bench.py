@@ -32,12 +32,24 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, os.path.join(ROOT, "cor-model_gb300"))
 
 import cortrace as ct  # noqa: E402
+import window  # noqa: E402
 
 WORKLOAD = "igrf14+t96 5x5deg global grid, vertical, 20 km, 20->0.01 GV by 0.01 (2664 sites x 2000)"
 TIME7 = [2020, 6, 21, 173, 12, 0, 0]
 PARMOD = [2.0, -20.0, 0.0, -1.0]
 N_RIG = 2000
 METRIC = "site cutoffs/s"
+WINDOW_FILE = os.path.join(ROOT, "cor-model_gb300", "window_t96.npz")
+TUNING_FILE = os.path.join(ROOT, "cor-model_gb300", "tuning.json")
+
+
+def tuning() -> dict:
+    """The autotuner's choice (cor-model_gb300/autotune.py), else the defaults."""
+    if os.path.exists(TUNING_FILE):
+        with open(TUNING_FILE) as f:
+            t = json.load(f)
+        return {k: t[k] for k in ("inflight", "park_below", "max_generations", "min_park")} | {"source": "autotune"}
+    return {"inflight": 3, "park_below": 16, "max_generations": 48, "min_park": 256, "source": "defaults"}
 
 
 def grid_sites() -> list[tuple[float, float]]:
@@ -164,10 +176,12 @@ class Lane:
     buffers.  Batches on different slots overlap on the GPU, so one batch's
     tail of long trajectories runs beside the next batch's bulk."""
 
-    def __init__(self, dev: int, p):
+    def __init__(self, dev: int, p, tune: dict | None = None):
         import torch
         self.torch = torch
         self.ctx = ct.Context(dev)
+        if tune:
+            self.ctx.set_regroup(tune["park_below"], tune["max_generations"], tune["min_park"])
         self.stream = torch.cuda.Stream(device=dev)
         rc = self.ctx.lib.cor_upload_params(self.ctx.h, p.ctypes.data, len(p))
         if rc != 0:
@@ -222,12 +236,76 @@ def run_batches(slots, bufs, order) -> None:
         raise errors[0]
 
 
+def site_features(latlon) -> np.ndarray:
+    """The window network's inputs for vertical incidence at this workload's
+    condition (IGRF-14 + T96 at 2020-06-21 12 UT)."""
+    p = params()
+    tilt, ep = window.dipole_tilt(p), window.decimal_epoch(TIME7)
+    return np.array([window.features(lat, lon, 0.0, 0.0, ep, PARMOD, tilt) for lat, lon in latlon])
+
+
+def measure_window(args, slots, bufs, p, plain_e2e: float) -> dict:
+    """The learned window on the timed batches: predicted windows traced
+    through cor_trace_batch (host buffers, like e2e), full-scan fallback on
+    an edge hit, R_C compared with the plain scan of the same sites."""
+    import queue
+    wm = window.WindowModel(args.window)
+    timed = list(range(args.warmup, args.warmup + args.steps))
+    feats = {i: site_features(bufs[i]["latlon"]) for i in timed}
+    wm.windows(feats[timed[0]])                     # load the network's kernels before timing
+    q = queue.Queue()
+    for i in timed:
+        q.put(i)
+    out = {}
+
+    def worker(slot):
+        while True:
+            try:
+                i = q.get_nowait()
+            except queue.Empty:
+                return
+            i_lo, i_hi = wm.windows(feats[i])
+            out[i] = window.trace_windows(slot.ctx, bufs[i]["host_jobs"], p, models(), i_lo, i_hi)
+
+    t0 = time.perf_counter()
+    ths = [threading.Thread(target=worker, args=(s,)) for s in slots]
+    for t in ths:
+        t.start()
+    for t in ths:
+        t.join()
+    wall = time.perf_counter() - t0
+    n_sites = agree = fallback = traced = 0
+    full_traj = 0
+    worst = 0.0
+    for i in timed:
+        full = bufs[i]["sites"].cpu().numpy().view(ct.SITE_DTYPE)
+        sites, fb, tr, _ = out[i]
+        d = np.abs(sites["r_cutoff"] - full["r_cutoff"])
+        agree += int(np.sum(d <= 0.01 + 1e-9))
+        worst = max(worst, float(d.max()))
+        n_sites += len(full)
+        fallback += int(fb.sum())
+        traced += tr
+        full_traj += bufs[i]["n"]
+    wm.close()
+    v = n_sites / wall
+    return {"value": v, "unit": METRIC, "speedup_vs_plain_e2e": v / plain_e2e if plain_e2e else None,
+            "sites": n_sites, "agree_frac_dRc_le_0.01GV": agree / n_sites, "max_abs_dRc_GV": worst,
+            "fallback_frac": fallback / n_sites, "trajectories_frac_of_full_scan": traced / full_traj,
+            "model": json.loads(wm.info) if wm.info.startswith("{") else wm.info,
+            "how": "predicted window +-3 sigma on the 0.01 GV grid, full scan on an edge hit; host buffers through "
+                   "cor_trace_batch, network inference on the tensor cores inside the timed region"}
+
+
 def run_ours(args, rank: int, world: int, dist) -> dict | None:
     import torch
     dev = int(os.environ.get("LOCAL_RANK", "0"))
     torch.cuda.set_device(dev)
     p = params()
-    slots = [Lane(dev, p) for _ in range(args.inflight)]
+    tune = tuning()
+    if args.inflight is None:
+        args.inflight = tune["inflight"]
+    slots = [Lane(dev, p, tune) for _ in range(args.inflight)]
     mine = rank_batches(rank, world, args.batches)
     n_steps = args.warmup + args.steps
     bufs = []
@@ -241,7 +319,7 @@ def run_ours(args, rank: int, world: int, dist) -> dict | None:
             "n_jobs": len(jobs), "n": n, "jobs": t(jobs), "trig": t(trig), "off": t(off),
             "sites": torch.zeros(len(jobs) * ct.SITE_DTYPE.itemsize, dtype=torch.uint8, device=f"cuda:{dev}"),
             "status": torch.zeros(n, dtype=torch.uint8, device=f"cuda:{dev}"),
-            "host_jobs": jobs,
+            "host_jobs": jobs, "latlon": batch_sites(b, args.batches),
         })
     peak = C.c_double(0.0)
     slots[0].ctx.lib.cor_probe_fp64_peak(slots[0].ctx.h, C.byref(peak))
@@ -305,6 +383,9 @@ def run_ours(args, rank: int, world: int, dist) -> dict | None:
         t = torch.tensor([e2e_s], dtype=torch.float64, device=f"cuda:{dev}")
         tdist.all_reduce(t, op=tdist.ReduceOp.MAX)
         e2e_s = float(t.item())
+    learned = None
+    if args.window and os.path.exists(args.window) and world == 1:
+        learned = measure_window(args, slots, bufs, p, sites_done / e2e_s)
     for s in slots:
         s.ctx.close()
     if rank != 0:
@@ -320,7 +401,7 @@ def run_ours(args, rank: int, world: int, dist) -> dict | None:
         "data": "synthetic grid of sites (the configuration's own sites; no dataset)",
         "config": {"workload": WORKLOAD, "sites_per_step": sites_done // max(1, args.steps * world),
                    "trajectories_per_step": traj_done // max(1, args.steps * world),
-                   "batches": args.batches, "inflight": args.inflight,
+                   "batches": args.batches, "inflight": args.inflight, "tuning": tune,
                    "l2": "no L2 flush: the kernel is FP64-bound and its state lives in registers; inputs and "
                          "outputs are MB-sized", "parallelism": f"sites split over {world} GPU(s)"},
         "trajectories_per_s": traj_done / dev_s, "steps_per_s": steps_acc / dev_s,
@@ -335,6 +416,8 @@ def run_ours(args, rank: int, world: int, dist) -> dict | None:
         "gpu_launches": sum(int(b["counters"][4]) for b in timed),
         "clocks": clocks.summary(),
     }
+    if learned is not None:
+        out["learned_window"] = learned
     if world == 1 and not args.no_cpu_baseline:
         out["cpu_baseline"] = cpu_baseline(args.batches)
     return out
@@ -412,9 +495,12 @@ def main():
     ap.add_argument("--steps", type=int, default=4)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--batches", type=int, default=16)
-    ap.add_argument("--inflight", type=int, default=3, help="batches in flight at once (one stream each)")
+    ap.add_argument("--inflight", type=int, default=None,
+                    help="batches in flight at once (one stream each; default: the autotuner's choice, else 3)")
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--window", default=WINDOW_FILE, help="trained window model for the learned-window line "
+                    "(train_window.py output); skipped when the file is absent")
     ap.add_argument("--profile-case", action="store_true",
                     help="run only the small profiling case of the scan kernel (prints its own JSON, not a bench line)")
     args = ap.parse_args()

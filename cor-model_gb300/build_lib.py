@@ -30,10 +30,10 @@ CC_FLAGS = ["-O2", "-std=gnu17", "-fPIC", "-ffp-contract=off", "-fno-math-errno"
 
 # Sources of the shared library.
 CU_SOURCES = ["cortrace.cu", "inst_igrf.cu", "inst_igrf_t96.cu", "inst_t96.cu", "inst_igrf_ts05.cu",
-              "inst_ts05.cu", "inst_crustal.cu"]
+              "inst_ts05.cu", "inst_crustal.cu", "mlp.cu"]
 LIB_C_SOURCES = ["setup.c", "coef_tables.c"]
 # Sources of the drop-in CLI (linked against the library).
-CLI_C_SOURCES = ["cli_main.c", "cli_io.c", "cli_models.c", "cli_scan.c"]
+CLI_C_SOURCES = ["cli_main.c", "cli_io.c", "cli_models.c", "cli_scan.c", "cli_field.c"]
 
 
 def nvcc() -> str:

@@ -39,7 +39,7 @@ SH = 105
 JOB_DTYPE = np.dtype([
     ("r0", "f8"), ("the0", "f8"), ("fi0", "f8"), ("the1", "f8"), ("fi1", "f8"),
     ("rig", "f8"), ("del", "f8"), ("rk", "f8"), ("zn", "f8"),
-    ("nk1", "i4"), ("param_index", "i4")], align=True)
+    ("nk1", "i4"), ("param_index", "i4"), ("i_first", "i4"), ("i_count", "i4")], align=True)
 PARAMS_DTYPE = np.dtype([
     ("parmod", "f8", (10,)), ("g", "f8", (SH,)), ("h", "f8", (SH,)), ("rec", "f8", (SH,)),
     ("a1", "f8", (3,)), ("a2", "f8", (3,)), ("a3", "f8", (3,))], align=True)
@@ -51,7 +51,7 @@ SITE_DTYPE = np.dtype([
     ("n_forbidden", "i4"), ("n_traj", "i4")], align=True)
 TRIG_DTYPE = np.dtype([(k, "f8") for k in ("st0", "ct0", "sp0", "cp0", "st1", "ct1", "sp1", "cp1")], align=True)
 
-assert JOB_DTYPE.itemsize == 80 and PARAMS_DTYPE.itemsize == 2672
+assert JOB_DTYPE.itemsize == 88 and PARAMS_DTYPE.itemsize == 2672
 assert RECORD_DTYPE.itemsize == 88 and SITE_DTYPE.itemsize == 32
 
 
@@ -83,7 +83,7 @@ EXPORTS = [
     "cor_ctx_create", "cor_ctx_destroy", "cor_last_error_string", "cor_abi_version", "cor_batch_count",
     "cor_prepare_trig", "cor_trace_batch", "cor_trace_batch_device", "cor_upload_params", "cor_field_batch",
     "cor_internal_setup", "cor_gsm_setup", "cor_probe_fp64_peak", "cor_upload_crustal",
-    "cor_trace_batch_device_noalloc",
+    "cor_trace_batch_device_noalloc", "cor_ctx_set_regroup", "cor_trace_steps",
 ]
 NOALLOC_MAX_TRAJ = 1048576  # COR_NOALLOC_MAX_TRAJ
 
@@ -111,6 +111,8 @@ def load(path: str = LIB_PATH) -> C.CDLL:
                                            vp, vp, vp, vp, C.c_uint32, vp]
     lib.cor_upload_params.argtypes = [vp, vp, i32]
     lib.cor_upload_crustal.argtypes = [vp, vp, vp, i32]
+    lib.cor_ctx_set_regroup.argtypes = [vp, i32, i32, i64]
+    lib.cor_trace_steps.argtypes = [vp, C.POINTER(BatchReq), C.POINTER(BatchResult), vp, C.c_uint32]
     lib.cor_trace_batch_device_noalloc.argtypes = [vp, vp, vp, i32, vp, u64, ModelSet, u64, dbl, dbl,
                                                    vp, vp, vp, C.c_uint32, vp]
     lib.cor_probe_fp64_peak.argtypes = [vp, C.POINTER(C.c_double)]
@@ -228,6 +230,10 @@ class Context:
         self._check(self.lib.cor_trace_batch(self.h, C.byref(req), C.byref(res)), "trace_batch")
         return ScanResult(sites, status, records, off, res.counters.as_dict())
 
+    def set_regroup(self, park_below: int = 16, max_generations: int = 48, min_park: int = 256) -> None:
+        """cor_ctx_set_regroup: the scan kernel's regrouping knobs."""
+        self._check(self.lib.cor_ctx_set_regroup(self.h, park_below, max_generations, min_park), "cor_ctx_set_regroup")
+
     def upload_crustal(self, g: np.ndarray, h: np.ndarray, nmax: int) -> None:
         """cor_upload_crustal: packed lower-triangle G, H (index n(n+1)/2 + m)."""
         g = np.ascontiguousarray(g, np.float64)
@@ -250,14 +256,17 @@ class Context:
 
 
 def make_job(lat, lon, rig=0.05, rk=20.0, dele=0.05, r0=1.0031391260673028, the1=None, fi1=None,
-             zn=1.0, nk1=100, param_index=0) -> np.ndarray:
-    """One scan (INFILE) as a JOB_DTYPE record; vertical incidence by default."""
+             zn=1.0, nk1=100, param_index=0, i_first=0, i_last=None) -> np.ndarray:
+    """One scan (INFILE) as a JOB_DTYPE record; vertical incidence by default.
+    i_first / i_last (inclusive) trace only a window of the scan's grid."""
     j = np.zeros(1, JOB_DTYPE)
     j["r0"], j["the0"], j["fi0"] = r0, lat, lon
     j["the1"] = lat if the1 is None else the1
     j["fi1"] = lon if fi1 is None else fi1
     j["rig"], j["del"], j["rk"], j["zn"] = rig, dele, rk, zn
     j["nk1"], j["param_index"] = nk1, param_index
+    j["i_first"] = i_first
+    j["i_count"] = 0 if i_last is None else i_last - i_first + 1
     return j
 
 

@@ -75,6 +75,34 @@ __device__ __forceinline__ Vec3 gsm_to_geo(const Vec3 s, const cor_model_params*
     return g;
 }
 
+// Out-of-line C-library functions for the field models.  The inline
+// expansion of a CUDA double-precision function is tens to hundreds of
+// instructions, and the T96/TS05 models call them at many sites inside
+// unrolled loops; calling one out-of-line copy instead keeps each kernel's
+// field code small enough for the instruction caches.  Same functions, same
+// results.
+struct SinCos {
+    double s, c;
+};
+static __device__ __noinline__ double ol_exp(const double x) { return exp(x); }
+static __device__ __noinline__ double ol_log(const double x) { return log(x); }
+static __device__ __noinline__ double ol_sin(const double x) { return sin(x); }
+static __device__ __noinline__ double ol_cos(const double x) { return cos(x); }
+static __device__ __noinline__ double ol_atan(const double x) { return atan(x); }
+static __device__ __noinline__ double ol_asin(const double x) { return asin(x); }
+static __device__ __noinline__ double ol_atan2(const double y, const double x) { return atan2(y, x); }
+static __device__ __noinline__ double ol_pow(const double x, const double y) { return pow(x, y); }
+static __device__ __noinline__ SinCos ol_sincos_v(const double x) {
+    SinCos r;
+    sincos(x, &r.s, &r.c);
+    return r;
+}
+__device__ __forceinline__ void ol_sincos(const double x, double* s, double* c) {
+    const SinCos r = ol_sincos_v(x);
+    *s = r.s;
+    *c = r.c;
+}
+
 // Spherical-harmonic internal field, internal_geo (lib/internal/internal.c:182-275).
 // Degree truncated by radius, NM = min(13, 3 + 30/((int)R + 2)) (:201-205).
 // The (m, n) double loop is unrolled with compile-time indices so the

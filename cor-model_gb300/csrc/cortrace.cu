@@ -48,6 +48,12 @@ struct cor_ctx {
     double* crust = nullptr;              // crustal tables: g, h, k1, k2 (packed), kd
     int crust_nmax = 0;
     int crust_n_first = 0;
+    int park_below = 16;                  // regroup settings (cor_ctx_set_regroup)
+    int max_generations = 48;
+    uint64_t min_park = 256;
+    DevBuf steps;                         // trajectory dump: per-step records (cor_trace_steps)
+    cor_step_record* step_dev = nullptr;  // set only while cor_trace_steps runs
+    uint32_t step_cap = 0;
 };
 
 extern "C" {
@@ -344,7 +350,7 @@ extern "C" int cor_ctx_destroy(cor_ctx* ctx) {
     cudaSetDevice(ctx->device);
     if (ctx->stream) cudaStreamSynchronize(ctx->stream);
     DevBuf* bufs[] = {&ctx->jobs,   &ctx->trig,    &ctx->offsets, &ctx->params,  &ctx->sites,
-                      &ctx->status, &ctx->records, &ctx->park[0], &ctx->park[1]};
+                      &ctx->status, &ctx->records, &ctx->park[0], &ctx->park[1], &ctx->steps};
     if (ctx->gen) cudaFree(ctx->gen);
     if (ctx->park_count_host) cudaFreeHost(ctx->park_count_host);
     if (ctx->launches_host) cudaFreeHost(ctx->launches_host);
@@ -367,8 +373,13 @@ extern "C" int cor_batch_count(const cor_scan_job* jobs, int32_t n_jobs, uint64_
         // src/trajectory.c:7,12: i = 0 .. (int)round((rk-rig)/del)
         const double nr = round((jb.rk - jb.rig) / jb.del);
         if (!(nr >= 0.) || nr > 1e8) return COR_ERR_INVALID;
+        const int64_t n_grid = (int64_t)((int)nr) + 1;
+        // a window of the grid: indices i_first .. i_first + i_count - 1
+        if (jb.i_first < 0 || jb.i_count < 0 || jb.i_first >= n_grid) return COR_ERR_INVALID;
+        const int64_t n = jb.i_count ? (int64_t)jb.i_count : n_grid - jb.i_first;
+        if ((int64_t)jb.i_first + n > n_grid) return COR_ERR_INVALID;
         if (offsets) offsets[j] = tot;
-        tot += (uint64_t)((int)nr) + 1;
+        tot += (uint64_t)n;
     }
     if (offsets) offsets[n_jobs] = tot;
     if (n_traj) *n_traj = tot;
@@ -462,21 +473,19 @@ static const ModelOps* find_ops(const cor_model_set& m) {
 // Generations of the scan kernel.  Generation 0 drains the work queue; every
 // later one restores the trajectories the previous one parked, in a grid
 // sized to their count, so the survivors run in full warps.  Each live
-// trajectory count at least halves per generation (a warp parks with fewer
-// than half its lanes live, or when half the warps have parked), so the loop
-// is short; the last generations (or the 48th) run without parking.  The host
+// trajectory count at least halves per generation (a block parks with fewer
+// than park_below lanes per warp live, or when half the warps have parked), so the loop
+// is short; the last generation (the context's max_generations-th, or one
+// with at most min_park live trajectories) runs without parking.  The host
 // reads the parked count between generations, so this call synchronises the
 // stream once per generation.
-constexpr int kParkBelow = 16;
-constexpr int kMaxGenerations = 48;
-constexpr uint64_t kMinPark = 256;
 
 static int launch_trace(cor_ctx* ctx, const ModelOps* ops, TraceArgs a, cudaStream_t s) {
     int per_sm = 0;
     CUDA_TRY(ctx, ops->occupancy(&per_sm));
     if (per_sm < 1) per_sm = 1;
     const uint64_t cap_blocks = (uint64_t)ctx->sms * (uint64_t)per_sm;
-    const size_t park_bytes = sizeof(ParkedLane) * (size_t)cap_blocks * 128;
+    const size_t park_bytes = sizeof(ParkedLane) * (size_t)cap_blocks * kTraceThreads;
     int rc;
     if ((rc = ensure(ctx, ctx->park[0], park_bytes)) != COR_OK) return rc;
     if ((rc = ensure(ctx, ctx->park[1], park_bytes)) != COR_OK) return rc;
@@ -484,16 +493,16 @@ static int launch_trace(cor_ctx* ctx, const ModelOps* ops, TraceArgs a, cudaStre
     uint32_t n_restore = 0;
     int cur = 0;
     ctx->generations = 0;
-    for (int g = 0; g < kMaxGenerations && live > 0; g++) {
-        uint64_t blocks = (live + 127) / 128;
+    for (int g = 0; g < ctx->max_generations && live > 0; g++) {
+        uint64_t blocks = (live + kTraceThreads - 1) / kTraceThreads;
         if (blocks > cap_blocks) blocks = cap_blocks;
         a.restore = g == 0 ? nullptr : (const ParkedLane*)ctx->park[cur ^ 1].p;
         a.n_restore = n_restore;
         a.park = (ParkedLane*)ctx->park[cur].p;
         a.gen = ctx->gen;
-        a.allow_park = (g + 1 < kMaxGenerations && live > kMinPark) ? 1 : 0;
-        a.park_below = kParkBelow;
-        a.launched_warps = (uint32_t)(blocks * 4);
+        a.allow_park = (g + 1 < ctx->max_generations && live > ctx->min_park) ? 1 : 0;
+        a.park_below = ctx->park_below;
+        a.launched_warps = (uint32_t)(blocks * kTraceWarps);
         CUDA_TRY(ctx, cudaMemsetAsync(ctx->gen, 0, sizeof(GenCounters), s));
         CUDA_TRY(ctx, ops->launch_generation(a, (unsigned)blocks, s));
         ctx->generations = g + 1;
@@ -618,6 +627,16 @@ extern "C" int cor_upload_crustal(cor_ctx* ctx, const double* g, const double* h
     return upload_crustal(ctx, g, h, nmax);
 }
 
+extern "C" int cor_ctx_set_regroup(cor_ctx* ctx, int32_t park_below, int32_t max_generations, int64_t min_park) {
+    if (!ctx) return COR_ERR_INVALID;
+    if (park_below < 0 || park_below > 32 || max_generations < 1 || max_generations > 1024 || min_park < 0)
+        return fail(ctx, COR_ERR_INVALID, "regroup settings out of range");
+    ctx->park_below = park_below;
+    ctx->max_generations = max_generations;
+    ctx->min_park = (uint64_t)min_park;
+    return COR_OK;
+}
+
 extern "C" int cor_upload_params(cor_ctx* ctx, const cor_model_params* params, int32_t n_params) {
     if (!ctx) return COR_ERR_INVALID;
     if (n_params < 1 || !params) return fail(ctx, COR_ERR_INVALID, "no parameter block");
@@ -662,6 +681,9 @@ extern "C" int cor_trace_batch_device(cor_ctx* ctx, const cor_scan_job* jobs_dev
         return fail(ctx, COR_ERR_INVALID, "missing device buffer (status is required on the device path)");
     CUDA_TRY(ctx, cudaSetDevice(ctx->device));
     TraceArgs a;
+    memset(&a, 0, sizeof a);
+    a.step_records = ctx->step_dev;
+    a.step_cap = ctx->step_cap;
     a.jobs = jobs_dev;
     a.trig = reinterpret_cast<const JobTrig*>(trig_dev);
     a.offsets = offsets_dev;
@@ -758,6 +780,28 @@ extern "C" int cor_trace_batch(cor_ctx* ctx, const cor_batch_req* req, cor_batch
     free(offsets);
     free(trig);
     return rc;
+}
+
+extern "C" int cor_trace_steps(cor_ctx* ctx, const cor_batch_req* req, cor_batch_result* out, cor_step_record* steps,
+                               uint32_t step_capacity) {
+    if (!ctx || !req || !out) return COR_ERR_INVALID;
+    if (!steps || step_capacity == 0) return fail(ctx, COR_ERR_INVALID, "no step record buffer");
+    uint64_t n_traj = 0;
+    if (cor_batch_count(req->jobs, req->n_jobs, &n_traj, nullptr) != COR_OK)
+        return fail(ctx, COR_ERR_INVALID, "invalid rigidity grid in a job");
+    const size_t bytes = sizeof(cor_step_record) * (size_t)n_traj * step_capacity;
+    CUDA_TRY(ctx, cudaSetDevice(ctx->device));
+    int rc = ensure(ctx, ctx->steps, bytes ? bytes : 1);
+    if (rc != COR_OK) return rc;
+    CUDA_TRY(ctx, cudaMemsetAsync(ctx->steps.p, 0, bytes, ctx->stream));
+    ctx->step_dev = (cor_step_record*)ctx->steps.p;
+    ctx->step_cap = step_capacity;
+    rc = cor_trace_batch(ctx, req, out);
+    ctx->step_dev = nullptr;
+    ctx->step_cap = 0;
+    if (rc != COR_OK) return rc;
+    CUDA_TRY(ctx, cudaMemcpy(steps, ctx->steps.p, bytes, cudaMemcpyDeviceToHost));
+    return COR_OK;
 }
 
 extern "C" int cor_field_batch(cor_ctx* ctx, cor_model_set models, const cor_model_params* params, int32_t n_params,
@@ -958,10 +1002,10 @@ extern "C" int cor_trace_batch_device_noalloc(cor_ctx* ctx, const cor_scan_job* 
         int per_sm = 0;
         CUDA_TRY(ctx, ops->occupancy(&per_sm));
         if (per_sm < 1) per_sm = 1;
-        uint64_t blocks = (n_traj + 127) / 128;
+        uint64_t blocks = (n_traj + kTraceThreads - 1) / kTraceThreads;
         const uint64_t cap = (uint64_t)ctx->sms * (uint64_t)per_sm;
         if (blocks > cap) blocks = cap;
-        a.launched_warps = (uint32_t)(blocks * 4);
+        a.launched_warps = (uint32_t)(blocks * kTraceWarps);
         CUDA_TRY(ctx, ops->launch_generation(a, (unsigned)blocks, s));
         launches++;
     }

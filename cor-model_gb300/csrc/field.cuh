@@ -31,45 +31,55 @@ struct DevParams {
     TS05Cond ts05;
 };
 
-// GSM position in metres -> GEO field in nT.
+// GSM position in metres -> GEO field in nT, for the lanes with `want` set
+// (the others get zeros and never read dp).  With the crustal model every
+// lane of the warp must make the call together, converged: the crustal sum
+// is evaluated by the whole warp (chaos_geo_warp).  Without it, a caller may
+// call for its wanting lanes alone.
 template <class MS>
-__device__ __forceinline__ Vec3 calculate_field(const Vec3 gsm_pos, const DevParams* __restrict__ dp,
+__device__ __forceinline__ Vec3 calculate_field(const bool want, const Vec3 gsm_pos, const DevParams* __restrict__ dp,
                                                 const CrustalTables& crust) {
-    const cor_model_params* __restrict__ p = &dp->p;
-    const Vec3 pos = {DIVRE(gsm_pos.x), DIVRE(gsm_pos.y), DIVRE(gsm_pos.z)};
     Vec3 tot = {0., 0., 0.};
-    const bool internal = MS::internal == kModelAtRunTime ? crust.internal != 0 : MS::internal != 0;
-    const int external = MS::external == kModelAtRunTime ? crust.external : MS::external;
-    if (internal) {
-        // internal_calc, src/models.c:146-160
-        const Vec3 geo = gsm_to_geo(pos, p);
-        const Vec3 bg = internal_geo(geo, p);
-        const Vec3 bs = geo_to_gsm(bg, p);
-        tot.x += bs.x;
-        tot.y += bs.y;
-        tot.z += bs.z;
+    Vec3 pos = {0., 0., 0.};
+    const cor_model_params* __restrict__ p = nullptr;
+    if (want) {
+        p = &dp->p;
+        pos = {DIVRE(gsm_pos.x), DIVRE(gsm_pos.y), DIVRE(gsm_pos.z)};
+        const bool internal = MS::internal == kModelAtRunTime ? crust.internal != 0 : MS::internal != 0;
+        const int external = MS::external == kModelAtRunTime ? crust.external : MS::external;
+        if (internal) {
+            // internal_calc, src/models.c:146-160
+            const Vec3 geo = gsm_to_geo(pos, p);
+            const Vec3 bg = internal_geo(geo, p);
+            const Vec3 bs = geo_to_gsm(bg, p);
+            tot.x += bs.x;
+            tot.y += bs.y;
+            tot.z += bs.z;
+        }
+        if (external == COR_EXTERNAL_T96) {
+            const Vec3 b = t96_field(dp->t96, pos);  // t96_calc, src/models.c:171-177
+            tot.x += b.x;
+            tot.y += b.y;
+            tot.z += b.z;
+        } else if (external == COR_EXTERNAL_TS05) {
+            const Vec3 b = ts05_field(dp->ts05, pos);  // ts05_calc, src/models.c:162-169
+            tot.x += b.x;
+            tot.y += b.y;
+            tot.z += b.z;
+        }
     }
-    if (external == COR_EXTERNAL_T96) {
-        const Vec3 b = t96_field(dp->t96, pos);  // t96_calc, src/models.c:171-177
-        tot.x += b.x;
-        tot.y += b.y;
-        tot.z += b.z;
-    } else if (external == COR_EXTERNAL_TS05) {
-        const Vec3 b = ts05_field(dp->ts05, pos);  // ts05_calc, src/models.c:162-169
-        tot.x += b.x;
-        tot.y += b.y;
-        tot.z += b.z;
-    }
-    if (MS::crustal) {
+    if constexpr (MS::crustal != 0) {
         // chaos_7_16_calc, src/models.c:179-192
-        const Vec3 geo = gsm_to_geo(pos, p);
-        const Vec3 bg = chaos_geo(geo, crust);
-        const Vec3 bs = geo_to_gsm(bg, p);
-        tot.x += bs.x;
-        tot.y += bs.y;
-        tot.z += bs.z;
+        const Vec3 geo = want ? gsm_to_geo(pos, p) : Vec3{0., 0., 0.};
+        const Vec3 bg = chaos_geo_warp(want, geo, crust);
+        if (want) {
+            const Vec3 bs = geo_to_gsm(bg, p);
+            tot.x += bs.x;
+            tot.y += bs.y;
+            tot.z += bs.z;
+        }
     }
-    return gsm_to_geo(tot, p);
+    return want ? gsm_to_geo(tot, p) : tot;
 }
 
 }  // namespace cor

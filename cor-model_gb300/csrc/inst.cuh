@@ -7,10 +7,10 @@
     namespace cor {                                                                                        \
     using MS_##NAME = ModelSet<I, E, C>;                                                                   \
     static cudaError_t occ_##NAME(int* n) {                                                                \
-        return cudaOccupancyMaxActiveBlocksPerMultiprocessor(n, trace_kernel<MS_##NAME>, 128, 0);          \
+        return cudaOccupancyMaxActiveBlocksPerMultiprocessor(n, trace_kernel<MS_##NAME>, kTraceThreads, 0);          \
     }                                                                                                      \
     static cudaError_t gen_##NAME(const TraceArgs& a, unsigned blocks, cudaStream_t s) {                   \
-        trace_kernel<MS_##NAME><<<blocks, 128, 0, s>>>(a);                                                 \
+        trace_kernel<MS_##NAME><<<blocks, kTraceThreads, 0, s>>>(a);                                                 \
         return cudaGetLastError();                                                                         \
     }                                                                                                      \
     static cudaError_t field_##NAME(const DevParams* p, int np, const int32_t* idx, const double* pos,     \

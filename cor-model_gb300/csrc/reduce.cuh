@@ -8,7 +8,9 @@ namespace cor {
 // Per-scan reduction, src/trajectory.c:156-160, one warp per scan.  The
 // reference's fmin/fmax over thread_rig = rig + i*del are taken through the
 // extreme indices (thread_rig increases with i), so the result does not
-// depend on the order in which trajectories finished.
+// depend on the order in which trajectories finished.  For a window of the
+// grid (i_first > 0 or i_count > 0) the indices are the grid's and the
+// untraced indices below the window count as forbidden.
 __global__ void reduce_kernel(const cor_scan_job* __restrict__ jobs, const uint64_t* __restrict__ off,
                               int n_jobs, const uint8_t* __restrict__ status, cor_site_result* __restrict__ out) {
     const int w = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
@@ -16,8 +18,9 @@ __global__ void reduce_kernel(const cor_scan_job* __restrict__ jobs, const uint6
     if (w >= n_jobs) return;
     const uint64_t b = off[w], e = off[w + 1];
     int imin_allowed = 0x7fffffff, imax1 = -1, imax2 = -1, nza = 0;
+    const int i0 = jobs[w].i_first;  // grid index of the first traced trajectory
     for (uint64_t t = b + lane; t < e; t += 32) {
-        const int i = (int)(t - b);
+        const int i = i0 + (int)(t - b);
         const int st = status[t];
         if (st == COR_TRAJ_ALLOWED) {
             imin_allowed = min(imin_allowed, i);
@@ -43,6 +46,8 @@ __global__ void reduce_kernel(const cor_scan_job* __restrict__ jobs, const uint6
         if (imax1 >= 0) rmx1 = fmax(rmx1, job.rig + imax1 * job.del);
         if (imax2 >= 0) rmx2 = fmax(rmx2, job.rig + imax2 * job.del);
         double rmx = fmax(rmx1, rmx2);
+        // the untraced indices below a window count as forbidden
+        nza += job.i_first;
         const double zan = nza - (rmi - job.rig) / job.del;
         const double rms = rmi + zan * job.del;
         rmx = rmx + job.del;

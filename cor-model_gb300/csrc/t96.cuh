@@ -73,7 +73,7 @@ __device__ __forceinline__ double bes_poly0(double x32) {
 
 // J0 and J1 polynomial/asymptotic approximations (bes0/bes1, :211-234),
 // computed together: they share x/3 or 3/x and sqrt(x).
-__device__ __forceinline__ void t96_bes01(const double x, double& j0, double& j1) {
+static __device__ __noinline__ void t96_bes01(const double x, double& j0, double& j1) {
     if (fabs(x) < 3.0) {
         const double x3 = DIV3(x);
         const double x32 = x3 * x3;
@@ -88,12 +88,12 @@ __device__ __forceinline__ void t96_bes01(const double x, double& j0, double& j1
     const double t0 = x - 0.78539816 - xd3 * (0.04166397 + xd3 * (0.00003954 - xd3 * (0.00262573 - xd3 * (0.00054125 + xd3 * (0.00029333 - xd3 * 0.00013558)))));
     const double f1 = 0.79788456 + xd3 * (0.00000156 + xd3 * (0.01659667 + xd3 * (0.00017105 - xd3 * (0.00249511 - xd3 * (0.00113653 - xd3 * 0.00020033)))));
     const double t1 = x - 2.35619449 + xd3 * (0.12499612 + xd3 * (0.0000565 - xd3 * (0.00637879 - xd3 * (0.00074348 + xd3 * (0.00079824 - xd3 * 0.00029166)))));
-    j0 = f0 / sx * cos(t0);
-    j1 = f1 / sx * cos(t1);
+    j0 = f0 / sx * ol_cos(t0);
+    j1 = f1 / sx * ol_cos(t1);
 }
 
 // cylharm, :113-163
-__device__ __forceinline__ Vec3 t96_cylharm(const double x, const double y, const double z) {
+static __device__ __noinline__ Vec3 t96_cylharm(const double x, const double y, const double z) {
     constexpr double A[12] = {0.24777, -27.003, -0.46815, 7.0637, -1.5918, -0.90317E-01,
                               57.522, 13.757, 2.0100, 10.458, 4.5798, 2.1695};
     double rho = sqrt(y * y + z * z), sf, cf;
@@ -114,7 +114,7 @@ __device__ __forceinline__ Vec3 t96_cylharm(const double x, const double y, cons
         const double dz = div_c(rho, A[i + 6], 1.0 / A[i + 6]);
         double j0, j1;
         t96_bes01(dz, j0, j1);
-        const double e = exp(div_c(x, A[i + 6], 1.0 / A[i + 6]));
+        const double e = ol_exp(div_c(x, A[i + 6], 1.0 / A[i + 6]));
         const double j1dz = j1 / dz;
         bx -= A[i] * j1 * e * sf;
         by += A[i] * (2.0 * j1 / dz - j0) * e * sf * cf;
@@ -126,7 +126,7 @@ __device__ __forceinline__ Vec3 t96_cylharm(const double x, const double y, cons
         const double xk = div_c(x, A[i + 6], 1.0 / A[i + 6]);
         double j0, j1;
         t96_bes01(dz, j0, j1);
-        const double e = exp(xk);
+        const double e = ol_exp(xk);
         const double brho = (xk * j0 - (dz * dz + xk - 1.0) * j1 / dz) * e * sf;
         const double bphi = (j0 + j1 / dz * (xk - 1.0)) * e * cf;
         bx += A[i] * (dz * j0 + xk * j1) * e * sf;
@@ -137,23 +137,23 @@ __device__ __forceinline__ Vec3 t96_cylharm(const double x, const double y, cons
 }
 
 // intercon, :236-271
-__device__ __forceinline__ Vec3 t96_intercon(const double x, const double y, const double z) {
+static __device__ __noinline__ Vec3 t96_intercon(const double x, const double y, const double z) {
     constexpr double A[9] = {-8.411078731, 5932254.951, -9073284.93, -11.68794634, 6027598.824,
                              -9218378.368, -6.508798398, -11824.42793, 18015.66212};
     constexpr double RP[3] = {0.12503844191332988, 0.071597395204476152, 0.011080976889832743};
     constexpr double RR[3] = {0.059675527522452816, 0.00098459526668325296, 0.00064371058922777988};
     double sz[3], cz[3];
 #pragma unroll
-    for (int k = 0; k < 3; k++) sincos(z * RR[k], &sz[k], &cz[k]);
+    for (int k = 0; k < 3; k++) ol_sincos(z * RR[k], &sz[k], &cz[k]);
     double bx = 0.0, by = 0.0, bz = 0.0;
 #pragma unroll
     for (int i = 0; i < 3; i++) {
         double sy, cy;
-        sincos(y * RP[i], &sy, &cy);
+        ol_sincos(y * RP[i], &sy, &cy);
 #pragma unroll
         for (int k = 0; k < 3; k++) {
             const double sq = c_t96.ic_sq[3 * i + k];
-            const double e = exp(x * sq);
+            const double e = ol_exp(x * sq);
             bx += A[3 * i + k] * (-sq * e * cy * sz[k]);
             by += A[3 * i + k] * (RP[i] * e * sy * sz[k]);
             bz += A[3 * i + k] * (-RR[k] * e * cy * cz[k]);
@@ -163,20 +163,20 @@ __device__ __forceinline__ Vec3 t96_intercon(const double x, const double y, con
 }
 
 // shlcar3x3_t96, :500-617, for shield table t (0 ARC, 1 ATAIL2, 2 ATAIL3)
-__device__ __forceinline__ Vec3 t96_shlcar3x3(const int t, const double x, const double y, const double z) {
+static __device__ __noinline__ Vec3 t96_shlcar3x3(const int t, const double x, const double y, const double z) {
     double sz[3], cz[3];
 #pragma unroll
-    for (int k = 0; k < 3; k++) sincos(div_c(z, c_shl_r[t][k], c_shl_rr[t][k]), &sz[k], &cz[k]);
+    for (int k = 0; k < 3; k++) ol_sincos(div_c(z, c_shl_r[t][k], c_shl_rr[t][k]), &sz[k], &cz[k]);
     double hx = 0.0, hy = 0.0, hz = 0.0;
 #pragma unroll
     for (int i = 0; i < 3; i++) {
         const double p = c_shl_p[t][i], rp = c_shl_rp[t][i];
         double sy, cy;
-        sincos(div_c(y, p, rp), &sy, &cy);
+        ol_sincos(div_c(y, p, rp), &sy, &cy);
 #pragma unroll
         for (int k = 0; k < 3; k++) {
             const double sq = c_t96.shl_sq[t][3 * i + k];
-            const double e = exp(x * sq);
+            const double e = ol_exp(x * sq);
             const double amp = c_shl_a[t][2 * (3 * i + k)] + c_shl_a[t][2 * (3 * i + k) + 1];
             hx += (-sq * e * cy * sz[k]) * amp;
             hy += (div_c(e, p, rp) * sy * sz[k]) * amp;
@@ -187,7 +187,7 @@ __device__ __forceinline__ Vec3 t96_shlcar3x3(const int t, const double x, const
 }
 
 // ringcurr_96, :323-381
-__device__ __forceinline__ Vec3 t96_ringcurr(const double x, const double y, const double z) {
+static __device__ __noinline__ Vec3 t96_ringcurr(const double x, const double y, const double z) {
     constexpr double F[2] = {569.895366, -1603.386993};
     constexpr double BETA[2] = {2.722188, 3.766875};
     const double dzs = sqrt(z * z + 4.0);
@@ -228,7 +228,7 @@ __device__ __forceinline__ Vec3 t96_ringcurr(const double x, const double y, con
 }
 
 // taildisk_t96, :383-443
-__device__ __forceinline__ Vec3 t96_taildisk(const double x, const double y, const double z) {
+static __device__ __noinline__ Vec3 t96_taildisk(const double x, const double y, const double z) {
     constexpr double F[4] = {-745796.7338, 1176470.141, -444610.529, -57508.01028};
     constexpr double BETA[4] = {7.9250000, 8.0850000, 8.4712500, 27.89500};
     const double y20 = div_c(y, 20.0, 1.0 / 20.0);
@@ -286,10 +286,10 @@ __device__ __forceinline__ T87Line t96_tail87_line(const double b2, const double
     const double xa2 = 1. / (xc22 + b2);
     const double xna = xnx2 + b2;
     const double f = b2 - xc22;
-    const double xln1 = log(76.37 / xna);
+    const double xln1 = ol_log(76.37 / xna);
     const double xln2 = xln1 + 0.13238005;
     const double rb = 1. / b;
-    const double s0 = div_r(atan(div_r(xnx, b, rb)) + 1.5707963, b, rb);
+    const double s0 = div_r(ol_atan(div_r(xnx, b, rb)) + 1.5707963, b, rb);
     const double rxa1 = 1. / xa1;
     o.s0 = s0;
     o.s1 = div_r(xln1 * .5 + xc1 * s0, xa1, rxa1);
@@ -300,7 +300,7 @@ __device__ __forceinline__ T87Line t96_tail87_line(const double b2, const double
     return o;
 }
 
-__device__ __forceinline__ void t96_tail87(const double x, const double z, double& bxo, double& bzo) {
+static __device__ __noinline__ void t96_tail87(const double x, const double z, double& bxo, double& bzo) {
     const double zp = z - 40.0, zm = z + 40.0;
     const double xnx = -10.0 - x;
     const double xnx2 = xnx * xnx;
@@ -319,7 +319,7 @@ __device__ __forceinline__ void t96_tail87(const double x, const double z, doubl
 }
 
 // circle, :857-887
-__device__ __forceinline__ Vec3 t96_circle(const double x, const double y, const double z, const double rl) {
+static __device__ __noinline__ Vec3 t96_circle(const double x, const double y, const double z, const double rl) {
     const double rho2 = x * x + y * y;
     const double rho = sqrt(rho2);
     const double rr = rho + rl;
@@ -329,7 +329,7 @@ __device__ __forceinline__ Vec3 t96_circle(const double x, const double y, const
     const double r32 = 0.5 * (r12 + r22);
     const double xk2 = 1.0 - r12 / r22;
     const double xk2s = 1.0 - xk2;
-    const double dl = log(1.0 / xk2s);
+    const double dl = ol_log(1.0 / xk2s);
     const double K = 1.38629436112 + xk2s * (0.09666344259 + xk2s * (0.03590092383 + xk2s * (0.03742563713 + xk2s * 0.01451196212))) +
                      dl * (0.5 + xk2s * (0.12498593597 + xk2s * (0.06880248576 + xk2s * (0.03328355346 + xk2s * 0.00441787012))));
     const double E = 1.0 + xk2s * (0.44325141463 + xk2s * (0.0626060122 + xk2s * (0.04757383546 + xk2s * 0.01736506451))) +
@@ -342,7 +342,7 @@ __device__ __forceinline__ Vec3 t96_circle(const double x, const double y, const
 }
 
 // crosslp, :889-905, tilt index it into c_t96.cross_cs
-__device__ __forceinline__ Vec3 t96_crosslp(const double x, const double y, const double z, const double xc,
+static __device__ __noinline__ Vec3 t96_crosslp(const double x, const double y, const double z, const double xc,
                                            const double rl, const int it) {
     const double cal = c_t96.cross_cs[it][0], sal = c_t96.cross_cs[it][1];
     const double y1 = y * cal - z * sal, z1 = y * sal + z * cal;
@@ -357,7 +357,7 @@ struct Dip3 {
     Vec3 dx, dy, dz;
 };
 
-__device__ __forceinline__ Dip3 t96_dipxyz(const double x, const double y, const double z) {
+static __device__ __noinline__ Dip3 t96_dipxyz(const double x, const double y, const double z) {
     const double x2 = x * x, y2 = y * y, z2 = z * z;
     const double r2 = x2 + y2 + z2;
     const double xmr5 = 30574.0 / (r2 * r2 * sqrt(r2));
@@ -377,7 +377,7 @@ __device__ __forceinline__ Dip3 t96_dipxyz(const double x, const double y, const
 
 // Region-1 "dipole loops" basis contracted with its coefficients
 // (diploop1 :809-855 summed with C1 as in birk1tot_02 :702-707).
-__device__ __forceinline__ Vec3 t96_r1_loops(const double x, const double y, const double z) {
+static __device__ __noinline__ Vec3 t96_r1_loops(const double x, const double y, const double z) {
     constexpr double XX[12] = {-11.0, -7.0, -7.0, -3.0, -3.0, 1.0, 1.0, 1.0, 5.0, 5.0, 9.0, 9.0};
     constexpr double YY[12] = {2.0, 0.0, 4.0, 2.0, 6.0, 0.0, 4.0, 8.0, 2.0, 6.0, 0.0, 4.0};
     constexpr double C1[14] = {-0.911582E-03, -0.376654E-02, -0.727423E-02, -0.270084E-02, -0.123899E-02,
@@ -422,7 +422,7 @@ __device__ __forceinline__ Vec3 t96_r1_loops(const double x, const double y, con
 
 // Region-1 "conical harmonics + dipole pairs" basis contracted with C2
 // (condip1 :930-1028 summed as in birk1tot_02 :710-715).
-__device__ __forceinline__ Vec3 t96_r1_condip(const double x, const double y, const double z) {
+static __device__ __noinline__ Vec3 t96_r1_condip(const double x, const double y, const double z) {
     constexpr double XX[9] = {-10.0, -7.0, -4.0, -4.0, 0.0, 4.0, 4.0, 7.0, 10.0};
     constexpr double YY[9] = {3.0, 6.0, 3.0, 9.0, 6.0, 3.0, 9.0, 6.0, 3.0};
     constexpr double ZZ[14] = {20.0, 20.0, 4.0, 20.0, 4.0, 4.0, 20.0, 20.0, 20.0, 2.0, 3.0, 4.50, 7.0, 10.0};
@@ -505,7 +505,7 @@ __device__ __forceinline__ Vec3 t96_r1_condip(const double x, const double y, co
 }
 
 // birk1shld, :1030-1194
-__device__ __forceinline__ Vec3 t96_birk1shld(const double x, const double y, const double z) {
+static __device__ __noinline__ Vec3 t96_birk1shld(const double x, const double y, const double z) {
     constexpr double RPI[4] = {1.0 / 5.303648988, 1.0 / 10.40368955, 1.0 / 69.65230348, 1.0 / 466.5099509};
     constexpr double RK[4] = {1.0 / 1.645049286, 1.0 / 3.825838190, 1.0 / 11.66675599, 1.0 / 558.9781177};
     constexpr double AA[16] = {
@@ -515,16 +515,16 @@ __device__ __forceinline__ Vec3 t96_birk1shld(const double x, const double y, co
         -773.7002492 + 957.0094135, -1824.143669 + 520.7994379, 1192.484774 + -1192.184565, 89.15537624 + -98.52042999};
     double szk[4], czk[4];
 #pragma unroll
-    for (int k = 0; k < 4; k++) sincos(z * RK[k], &szk[k], &czk[k]);
+    for (int k = 0; k < 4; k++) ol_sincos(z * RK[k], &szk[k], &czk[k]);
     double bx = 0.0, by = 0.0, bz = 0.0;
 #pragma unroll
     for (int i = 0; i < 4; i++) {
         double sy, cy;
-        sincos(RPI[i] * y, &sy, &cy);
+        ol_sincos(RPI[i] * y, &sy, &cy);
 #pragma unroll
         for (int k = 0; k < 4; k++) {
             const double sq = c_t96.b1s_sq[4 * i + k];
-            const double e = exp(x * sq);
+            const double e = ol_exp(x * sq);
             bx += (-sq * e * cy * szk[k]) * AA[4 * i + k];
             by += (RPI[i] * e * sy * szk[k]) * AA[4 * i + k];
             bz += (-RK[k] * e * cy * czk[k]) * AA[4 * i + k];
@@ -534,14 +534,14 @@ __device__ __forceinline__ Vec3 t96_birk1shld(const double x, const double y, co
 }
 
 // birk1tot_02 (:619-807): the Region-1 field with its blend zones and shield.
-__device__ __forceinline__ Vec3 t96_birk1_blend(const double x, const double y, const double z, const double r,
+static __device__ __noinline__ Vec3 t96_birk1_blend(const double x, const double y, const double z, const double r,
                                                const double r3, const double cpas, const double spas, const double t1,
                                                const double t2, const bool south) {
     const double sqr = sqrt(r);
-    const double s1 = sin(t1);
-    const double st01 = sqr / pow(r3 + 1.0 / (s1 * s1 * s1 * s1 * s1 * s1) - 1.0, 0.1666666667);
-    const double s2 = sin(t2);
-    const double st02 = sqr / pow(r3 + 1.0 / (s2 * s2 * s2 * s2 * s2 * s2) - 1.0, 0.1666666667);
+    const double s1 = ol_sin(t1);
+    const double st01 = sqr / ol_pow(r3 + 1.0 / (s1 * s1 * s1 * s1 * s1 * s1) - 1.0, 0.1666666667);
+    const double s2 = ol_sin(t2);
+    const double st02 = sqr / ol_pow(r3 + 1.0 / (s2 * s2 * s2 * s2 * s2 * s2) - 1.0, 0.1666666667);
     double ct01 = sqrt(1.0 - st01 * st01), ct02 = sqrt(1.0 - st02 * st02);
     if (south) {
         ct01 = -ct01;
@@ -559,19 +559,19 @@ __device__ __forceinline__ Vec3 t96_birk1_blend(const double x, const double y, 
     return {b1.x * (1.0 - frac) + b2.x * frac, b1.y * (1.0 - frac) + b2.y * frac, b1.z * (1.0 - frac) + b2.z * frac};
 }
 
-__device__ __forceinline__ Vec3 t96_birk1tot(const double x, const double y, const double z) {
+static __device__ __noinline__ Vec3 t96_birk1tot(const double x, const double y, const double z) {
     const double tnoonn = 12.0 * 0.01745329;
     const double tnoons = 3.141592654 - tnoonn;
     const double r2 = x * x + y * y + z * z;
     const double r = sqrt(r2);
     const double r3 = r * r2;
     double pas = 0.0;
-    if (x != 0.0 || y != 0.0) pas = atan2(y, x);
-    const double tas = atan2(sqrt(x * x + y * y), z);
-    const double stas = sin(tas);
-    double tet0 = asin(stas / pow((stas * stas * stas * stas * stas * stas) * (1.0 - r3) + r3, 0.1666666667));
+    if (x != 0.0 || y != 0.0) pas = ol_atan2(y, x);
+    const double tas = ol_atan2(sqrt(x * x + y * y), z);
+    const double stas = ol_sin(tas);
+    double tet0 = ol_asin(stas / ol_pow((stas * stas * stas * stas * stas * stas) * (1.0 - r3) + r3, 0.1666666667));
     if (tas > 1.5707963) tet0 = 3.141592654 - tet0;
-    const double sh = sin(pas * 0.5);
+    const double sh = ol_sin(pas * 0.5);
     const double dtet = (8.0 * 0.01745329) * (sh * sh);
     const double tr1n = tnoonn + dtet, tr1s = tnoons - dtet;
     const double t01n = tr1n - 0.034906, t01s = tr1s - 0.034906;
@@ -591,7 +591,7 @@ __device__ __forceinline__ Vec3 t96_birk1tot(const double x, const double y, con
     }
     if ((tet0 >= t01n && tet0 <= t02n) || (tet0 >= t01s && tet0 <= t02s)) {
         double spas, cpas;
-        sincos(pas, &spas, &cpas);
+        ol_sincos(pas, &spas, &cpas);
         const bool south = tet0 >= t01s;
         b = t96_birk1_blend(x, y, z, r, r3, cpas, spas, south ? t01s : t01n, south ? t02s : t02n, south);
     }
@@ -600,23 +600,23 @@ __device__ __forceinline__ Vec3 t96_birk1tot(const double x, const double y, con
 }
 
 // birk2shl, :1196-1263
-__device__ __forceinline__ Vec3 t96_birk2shl(const double x, const double y, const double z) {
+static __device__ __noinline__ Vec3 t96_birk2shl(const double x, const double y, const double z) {
     constexpr double AI[2] = {13.85650567, 14.90554500};
     constexpr double AK[2] = {10.21914434, 10.09021632};
     constexpr double AS[4] = {-111.6371348 + 124.5402702, 110.3735178 + -122.0095905, 111.9448247 + -129.1957743,
                               -110.7586562 + 126.5649012};
     double szk[2], czk[2];
 #pragma unroll
-    for (int k = 0; k < 2; k++) sincos(div_c(z, AK[k], 1.0 / AK[k]), &szk[k], &czk[k]);
+    for (int k = 0; k < 2; k++) ol_sincos(div_c(z, AK[k], 1.0 / AK[k]), &szk[k], &czk[k]);
     double hx = 0.0, hy = 0.0, hz = 0.0;
 #pragma unroll
     for (int i = 0; i < 2; i++) {
         double sy, cy;
-        sincos(div_c(y, AI[i], 1.0 / AI[i]), &sy, &cy);
+        ol_sincos(div_c(y, AI[i], 1.0 / AI[i]), &sy, &cy);
 #pragma unroll
         for (int k = 0; k < 2; k++) {
             const double sq = c_t96.b2s_sq[2 * i + k];
-            const double e = exp(x * sq);
+            const double e = ol_exp(x * sq);
             hx += (-sq * e * cy * szk[k]) * AS[2 * i + k];
             hy += (div_c(e, AI[i], 1.0 / AI[i]) * sy * szk[k]) * AS[2 * i + k];
             hz += (div_c(-e, AK[k], 1.0 / AK[k]) * cy * czk[k]) * AS[2 * i + k];
@@ -646,7 +646,7 @@ __device__ __forceinline__ double t96_xksi(const double x, const double y, const
     const double fgh32 = sq * sq * sq;
     const double fg2 = (f * f) + g2;
     if (fg2 < 1.0e-5) return -1.0;
-    const double th = sin(0.3665191 + 0.5 * 0.09599309 * (1.0 - f / sqrt(fg2)));
+    const double th = ol_sin(0.3665191 + 0.5 * 0.09599309 * (1.0 - f / sqrt(fg2)));
     return (fg2 / fgh32) - (th * th);
 }
 
@@ -665,7 +665,7 @@ __device__ __forceinline__ double t96_tksi(const double xk, const double x0, con
 }
 
 // loops4, :1445-1509, fixed tilt index il into c_t96.loop_cs
-__device__ __forceinline__ Vec3 t96_loops4(const double x, const double y, const double z, const double xc,
+static __device__ __noinline__ Vec3 t96_loops4(const double x, const double y, const double z, const double xc,
                                           const double yc, const double zc, const double R, const int il) {
     const double st = c_t96.loop_cs[il][0], ct = c_t96.loop_cs[il][1];
     const double sp = c_t96.loop_cs[il][2], cp = c_t96.loop_cs[il][3];
@@ -712,7 +712,7 @@ __device__ __forceinline__ Vec3 t96_loops4(const double x, const double y, const
 }
 
 // r2inner (:1316-1334) with bconic (:1336-1372) and dipdistr (:1374-1392)
-__device__ __forceinline__ Vec3 t96_r2inner(const double x, const double y, const double z) {
+static __device__ __noinline__ Vec3 t96_r2inner(const double x, const double y, const double z) {
     constexpr double CB[5] = {154.185, -2.12446, 0.601735E-01, -.153954E-02, .355077E-04};
     const double ro2 = x * x + y * y;
     const double ro = sqrt(ro2);
@@ -779,7 +779,7 @@ __device__ __forceinline__ Vec3 t96_r2inner(const double x, const double y, cons
 }
 
 // r2outer, :1394-1414
-__device__ __forceinline__ Vec3 t96_r2outer(const double x, const double y, const double z) {
+static __device__ __noinline__ Vec3 t96_r2outer(const double x, const double y, const double z) {
     const Vec3 d1 = t96_crosslp(x, y, z, 0.55, 0.694, 1);
     const Vec3 d2 = t96_crosslp(x, y, z, 1.55, 2.8, 2);
     const Vec3 d3 = t96_crosslp(x, y, z, -0.7, 0.2, 3);
@@ -792,7 +792,7 @@ __device__ __forceinline__ Vec3 t96_r2outer(const double x, const double y, cons
 
 // r2sheet, :1511-1593, with xksi passed in (the reference evaluates the same
 // xksi(X, Y, Z) again).
-__device__ __forceinline__ Vec3 t96_r2sheet(const double x, const double y, const double z, const double xks) {
+static __device__ __noinline__ Vec3 t96_r2sheet(const double x, const double y, const double z, const double xks) {
     constexpr double CX[5][4][4] = {
         {{8.07190, -7.39582, -7.62341, 0.684671}, {-13.5672, 11.6681, 13.1154, -0.890217},
          {7.78726, -5.38346, -8.08738, 0.609385}, {-2.70410, 3.53741, 3.15549, -1.11069}},
@@ -859,11 +859,11 @@ __device__ __forceinline__ Vec3 t96_r2sheet(const double x, const double y, cons
     const double ct2 = ct * ct;
     const double ct2m1 = ct2 - 1.0;
     double s[5];
-    s[0] = c_t96.r2s_k[0] * ct * exp(-19.0969 * ct2);
-    s[1] = c_t96.r2s_k[1] * ct * exp(-9.28828 * ct2);
-    s[2] = c_t96.r2s_k[2] * ct * exp(-0.129687 * ct2);
-    s[3] = ct * exp(5.58594 * ct2m1);
-    s[4] = ct * exp(22.5055 * ct2m1);
+    s[0] = c_t96.r2s_k[0] * ct * ol_exp(-19.0969 * ct2);
+    s[1] = c_t96.r2s_k[1] * ct * ol_exp(-9.28828 * ct2);
+    s[2] = c_t96.r2s_k[2] * ct * ol_exp(-0.129687 * ct2);
+    s[3] = ct * ol_exp(5.58594 * ct2m1);
+    s[4] = ct * ol_exp(22.5055 * ct2m1);
     double acc = 0.0;
 #pragma unroll
     for (int l = 0; l < 5; l++) {
@@ -874,11 +874,11 @@ __device__ __forceinline__ Vec3 t96_r2sheet(const double x, const double y, cons
         acc = (l == 0) ? s[l] * term : acc + s[l] * term;
     }
     const double bx = acc;
-    s[0] = c_t96.r2s_k[3] * ct * exp(-13.6750 * ct2);
-    s[1] = c_t96.r2s_k[4] * ct * exp(-6.70625 * ct2);
-    s[2] = ct * exp(2.31875 * ct2m1);
-    s[3] = ct * exp(11.4062 * ct2m1);
-    s[4] = ct * exp(20.4562 * ct2m1);
+    s[0] = c_t96.r2s_k[3] * ct * ol_exp(-13.6750 * ct2);
+    s[1] = c_t96.r2s_k[4] * ct * ol_exp(-6.70625 * ct2);
+    s[2] = ct * ol_exp(2.31875 * ct2m1);
+    s[3] = ct * ol_exp(11.4062 * ct2m1);
+    s[4] = ct * ol_exp(20.4562 * ct2m1);
     acc = 0.0;
 #pragma unroll
     for (int l = 0; l < 5; l++) {
@@ -889,11 +889,11 @@ __device__ __forceinline__ Vec3 t96_r2sheet(const double x, const double y, cons
         acc = (l == 0) ? s[l] * term : acc + s[l] * term;
     }
     const double by = acc;
-    s[0] = exp(-16.7125 * ct2);
-    s[1] = exp(-16.4625 * ct2);
-    s[2] = exp(-0.1625 * ct2);
-    s[3] = exp(5.1 * (ct2 - 1.0));
-    s[4] = exp(23.7125 * (ct2 - 1.0));
+    s[0] = ol_exp(-16.7125 * ct2);
+    s[1] = ol_exp(-16.4625 * ct2);
+    s[2] = ol_exp(-0.1625 * ct2);
+    s[3] = ol_exp(5.1 * (ct2 - 1.0));
+    s[4] = ol_exp(23.7125 * (ct2 - 1.0));
     acc = 0.0;
 #pragma unroll
     for (int l = 0; l < 5; l++) {
@@ -907,7 +907,7 @@ __device__ __forceinline__ Vec3 t96_r2sheet(const double x, const double y, cons
 }
 
 // r2_birk, :1265-1314
-__device__ __forceinline__ Vec3 t96_r2birk(const double x, const double y, const double z) {
+static __device__ __noinline__ Vec3 t96_r2birk(const double x, const double y, const double z) {
     const double dl = 0.03, dl1 = 0.015;
     const double xks = t96_xksi(x, y, z);
     if (xks < -(dl + dl1)) {
@@ -945,11 +945,11 @@ __device__ __forceinline__ Vec3 t96_dipole(const double x, const double y, const
 }
 
 // t96_gsm, :4-111.  x = GSM position [R_E]; c = per-condition block.
-__device__ __forceinline__ Vec3 t96_field(const T96Cond& c, const Vec3 X) {
+static __device__ __noinline__ Vec3 t96_field(const T96Cond& c, const Vec3 X) {
     const double x = X.x, y = X.y, z = X.z;
     const double ys = y * c.ct - z * c.st, zs = z * c.ct + y * c.st;
     const double ysd = div_c(ys, 10.0, 1.0 / 10.0);
-    const double factimf = exp(div_c(x, 20.0, 1.0 / 20.0) - ysd * ysd);
+    const double factimf = ol_exp(div_c(x, 20.0, 1.0 / 20.0) - ysd * ysd);
     const double oimfy = c.kimfy * factimf, oimfz = c.kimfz * factimf;
     const double rho2 = y * y + z * z;
     double xmxm = c.am + x - c.c548;

@@ -32,6 +32,7 @@ struct ParkedLane {
     int32_t job;
     uint32_t step, trials;
     int32_t nk0;
+    int32_t need_field;   // parked right after a step or its start: the field at pos is still to be evaluated
 };
 
 // Per-generation scratch counters (zeroed before each generation).
@@ -68,6 +69,10 @@ struct TraceArgs {
     int allow_park;                // 0 in the last generation
     int park_below;                // a warp parks when fewer lanes than this are live
     uint32_t launched_warps;
+    // trajectory dump: every accepted step of trajectory t goes to
+    // step_records[t * step_cap + step - 1] (null: not recorded)
+    cor_step_record* step_records;
+    uint32_t step_cap;
 };
 
 __device__ __forceinline__ int find_job(const uint64_t* __restrict__ off, int n_jobs, uint64_t t) {
@@ -92,7 +97,7 @@ struct Lane {
     int32_t job_index;
 };
 
-__device__ __forceinline__ void lane_park(const Lane& L, ParkedLane& o) {
+__device__ __forceinline__ void lane_park(const Lane& L, bool need_field, ParkedLane& o) {
     o.pos[0] = L.pos.x; o.pos[1] = L.pos.y; o.pos[2] = L.pos.z;
     o.vel[0] = L.vel.x; o.vel[1] = L.vel.y; o.vel[2] = L.vel.z;
     o.field[0] = L.field.x; o.field[1] = L.field.y; o.field[2] = L.field.z;
@@ -101,9 +106,11 @@ __device__ __forceinline__ void lane_park(const Lane& L, ParkedLane& o) {
     o.traj = L.traj;
     o.job = L.job_index;
     o.step = L.step; o.trials = L.trials; o.nk0 = L.nk0;
+    o.need_field = need_field ? 1 : 0;
 }
 
-__device__ __forceinline__ void lane_restore(Lane& L, const ParkedLane& o, const cor_scan_job* jobs,
+// Returns whether the restored trajectory still needs its field evaluated.
+__device__ __forceinline__ bool lane_restore(Lane& L, const ParkedLane& o, const cor_scan_job* jobs,
                                              const DevParams* params) {
     L.pos = {o.pos[0], o.pos[1], o.pos[2]};
     L.vel = {o.vel[0], o.vel[1], o.vel[2]};
@@ -115,6 +122,7 @@ __device__ __forceinline__ void lane_restore(Lane& L, const ParkedLane& o, const
     L.job = jobs + o.job;
     L.par = params + L.job->param_index;
     L.step = o.step; L.trials = o.trials; L.nk0 = o.nk0;
+    return o.need_field != 0;
 }
 
 // Claims the next index of a queue for every lane in `want` with one atomic
@@ -154,7 +162,7 @@ __device__ __forceinline__ void lane_init(Lane& L, const TraceArgs& a, uint64_t 
     L.job_index = j;
     L.par = a.params + job->param_index;
     L.traj = a.offsets[j] + i;
-    const double rig = job->rig + (int)i * job->del;
+    const double rig = job->rig + (int)(i + (uint64_t)job->i_first) * job->del;  // :14, absolute grid index
     L.rig = rig;
     L.nk0 = job->nk1;
     L.time = 0.;
@@ -277,16 +285,25 @@ __device__ __forceinline__ void warp_add_u64(unsigned long long* dst, unsigned l
     if ((threadIdx.x & 31) == 0 && v) atomicAdd(dst, v);
 }
 
-// One generation of the scan.  All 32 lanes of a warp stay in the loop
-// until the warp leaves it as a whole (every exit below is warp-uniform).
+// Threads of a scan block: one block of 8 warps per SM (the kernels of the
+// external-field sets need ~255 registers a thread, so 8 warps is also the
+// register file's limit).
+constexpr int kTraceThreads = 256;
+constexpr int kTraceWarps = kTraceThreads / 32;
+
+// One generation of the scan.  Every thread of a block stays in the loop
+// until the block leaves it as a whole: the exit and park decisions are
+// block-wide (__syncthreads_count / _or), which also lines the block's warps
+// up before each field evaluation, so they run through the field models'
+// instructions together and share the instruction-cache fills.
 // A lane with no trajectory takes the next parked one, else the next queue
-// index.  Once the queue is drained, a warp whose live lanes fall below
-// park_below -- or any warp, once half of the generation's warps have
-// parked -- writes its live trajectories to the park list and leaves; the
-// host then launches the next generation sized to the parked count, which
-// restores them densely (the regroup step).
+// index.  Once the queue is drained, a block whose live lanes fall below
+// park_below per warp -- or any block, once half of the generation's warps
+// have parked -- writes its live trajectories to the park list and leaves;
+// the host then launches the next generation sized to the parked count,
+// which restores them densely (the regroup step).
 template <class MS>
-__global__ void __launch_bounds__(128) trace_kernel(const TraceArgs a) {
+__global__ void __launch_bounds__(kTraceThreads, 1) trace_kernel(const TraceArgs a) {
     Lane L;
     bool has = false, done = false;
     unsigned long long n_steps = 0, n_trials = 0, n_traj = 0, n_wd = 0;
@@ -297,6 +314,17 @@ __global__ void __launch_bounds__(128) trace_kernel(const TraceArgs a) {
             const int st = lane_advance(L, a);
             if (st == 0) {
                 need_field = true;
+                if (a.step_records && L.step <= a.step_cap) {
+                    cor_step_record r;
+                    r.gsm[0] = L.gsm.x; r.gsm[1] = L.gsm.y; r.gsm[2] = L.gsm.z;
+                    r.pos[0] = L.pos.x; r.pos[1] = L.pos.y; r.pos[2] = L.pos.z;
+                    r.v = L.v;
+                    r.time = L.time;
+                    r.length = L.alength;
+                    r.step = L.step;
+                    r.reserved = 0;
+                    a.step_records[L.traj * a.step_cap + (L.step - 1)] = r;
+                }
             } else {
                 lane_finish(L, a, st);
                 n_steps += (st == COR_TRAJ_ALLOWED) ? L.step - 1 : L.step;
@@ -311,7 +339,7 @@ __global__ void __launch_bounds__(128) trace_kernel(const TraceArgs a) {
         if (a.n_restore) {
             const uint64_t r = queue_pop(&a.gen->restore_cursor, want);
             if (want && r < a.n_restore) {
-                lane_restore(L, a.restore[r], a.jobs, a.params);
+                need_field = lane_restore(L, a.restore[r], a.jobs, a.params);
                 has = true;
                 want = false;
             }
@@ -326,36 +354,38 @@ __global__ void __launch_bounds__(128) trace_kernel(const TraceArgs a) {
                 done = true;
             }
         }
-        if (__all_sync(0xffffffffu, done)) break;
-        if (a.allow_park && __any_sync(0xffffffffu, done)) {
-            const unsigned live = __ballot_sync(0xffffffffu, has);
-            bool park = __popc(live) < a.park_below;
-            if (!park) {
-                unsigned pw = 0;
-                if (lane == 0) pw = *((volatile unsigned int*)&a.gen->parked_warps);
-                pw = __shfl_sync(0xffffffffu, pw, 0);
-                park = 2u * pw >= a.launched_warps;
-            }
-            if (park) {
-                // need_field lanes were just initialised or advanced: their
-                // field is evaluated by the next generation's first pass.
+        // block-wide decisions: every thread of the block takes the same branch
+        const int n_done = __syncthreads_count(done);
+        if (n_done == kTraceThreads) break;
+        if (a.allow_park && n_done > 0) {
+            const int n_live = __syncthreads_count(has);
+            unsigned pw = 0;
+            if (threadIdx.x == 0) pw = *((volatile unsigned int*)&a.gen->parked_warps);
+            const int half = __syncthreads_or(threadIdx.x == 0 && 2u * pw >= a.launched_warps);
+            if (n_live < a.park_below * kTraceWarps || half) {
+                // need_field lanes were just initialised or advanced: the
+                // generation that restores them evaluates their field (the
+                // loop keeps a single calculate_field call site, so the field
+                // models are inlined once).
+                const unsigned live = __ballot_sync(0xffffffffu, has);
                 const int leader = __ffs(live) - 1;
                 unsigned base = 0;
                 if (live && lane == leader) base = atomicAdd(&a.gen->park_count, (unsigned)__popc(live));
                 base = __shfl_sync(0xffffffffu, base, live ? leader : 0);
-                if (has) {
-                    if (need_field) {
-                        L.field = calculate_field<MS>(L.gsm, L.par, a.crust);
-                        L.b = 1.E-09 * sqrt(L.field.x * L.field.x + L.field.y * L.field.y + L.field.z * L.field.z);
-                    }
-                    lane_park(L, a.park[base + __popc(live & ((1u << lane) - 1u))]);
-                }
+                if (has) lane_park(L, need_field, a.park[base + __popc(live & ((1u << lane) - 1u))]);
                 if (lane == 0) atomicAdd(&a.gen->parked_warps, 1u);
                 break;
             }
         }
-        if (need_field) {
-            L.field = calculate_field<MS>(L.gsm, L.par, a.crust);
+        if constexpr (MS::crustal != 0) {
+            // the crustal sum is evaluated by the whole (converged) warp
+            const Vec3 f = calculate_field<MS>(need_field, L.gsm, L.par, a.crust);
+            if (need_field) {
+                L.field = f;
+                L.b = 1.E-09 * sqrt(L.field.x * L.field.x + L.field.y * L.field.y + L.field.z * L.field.z);
+            }
+        } else if (need_field) {
+            L.field = calculate_field<MS>(true, L.gsm, L.par, a.crust);
             L.b = 1.E-09 * sqrt(L.field.x * L.field.x + L.field.y * L.field.y + L.field.z * L.field.z);
         }
     }
@@ -370,11 +400,17 @@ __global__ void field_kernel(const DevParams* __restrict__ params, int n_params,
                              const int32_t* __restrict__ pidx, const double* __restrict__ pos, int64_t n,
                              double* __restrict__ out, CrustalTables crust) {
     const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
-    int k = pidx ? pidx[i] : 0;
-    if (k < 0 || k >= n_params) k = 0;
-    const Vec3 x = {pos[3 * i], pos[3 * i + 1], pos[3 * i + 2]};
-    const Vec3 b = calculate_field<MS>(x, params + k, crust);
+    const bool want = i < n;
+    if (MS::crustal == 0 && !want) return;   // with the crustal model every lane takes part
+    int k = 0;
+    Vec3 x = {0., 0., 0.};
+    if (want) {
+        k = pidx ? pidx[i] : 0;
+        if (k < 0 || k >= n_params) k = 0;
+        x = {pos[3 * i], pos[3 * i + 1], pos[3 * i + 2]};
+    }
+    const Vec3 b = calculate_field<MS>(want, x, params + k, crust);
+    if (!want) return;
     out[3 * i] = b.x;
     out[3 * i + 1] = b.y;
     out[3 * i + 2] = b.z;

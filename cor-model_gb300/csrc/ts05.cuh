@@ -55,7 +55,7 @@ static __constant__ double c_ts05_a21[31] = {
     1.779933730, 1.102649543, .8867880020};
 
 // ---- deformed.c ------------------------------------------------------------
-__device__ __forceinline__ Vec3 ts05_taildisk(const double D0, const double DELTADX, const double x, const double y,
+static __device__ __noinline__ Vec3 ts05_taildisk(const double D0, const double DELTADX, const double x, const double y,
                                              const double z) {
     constexpr double F[5] = {-71.09346626, -1014.308601, -1272.939359, -3224.935936, -44546.86232};
     constexpr double B[5] = {10.90101242, 12.68393898, 13.51791954, 14.86775017, 15.12306404};
@@ -63,7 +63,7 @@ __device__ __forceinline__ Vec3 ts05_taildisk(const double D0, const double DELT
     const double rho = sqrt(x * x + y * y);
     const double rr = 1. / rho;
     const double drhodx = div_r(x, rho, rr), drhody = div_r(y, rho, rr);
-    const double dex = exp(div_c(x, 7., 1. / 7.));
+    const double dex = ol_exp(div_c(x, 7., 1. / 7.));
     const double y20 = div_c(y, 20., 1. / 20.);
     const double d = D0 + 4.7 * y20 * y20 + DELTADX * dex;
     const double dddy = 4.7 * y * 0.005;
@@ -105,22 +105,22 @@ __device__ __forceinline__ Vec3 ts05_taildisk(const double D0, const double DELT
 }
 
 // shlcar5x5, deformed.c:169-208, table t (0: A1 of unwarped, 1: A2)
-__device__ __forceinline__ Vec3 ts05_shlcar5x5(const int t, const double* __restrict__ coef, const double x,
+static __device__ __noinline__ Vec3 ts05_shlcar5x5(const int t, const double* __restrict__ coef, const double x,
                                               const double y, const double z) {
     double szk[5], czk[5];
 #pragma unroll
-    for (int k = 0; k < 5; k++) sincos(z * c_ts05.s5_rr[t][k], &szk[k], &czk[k]);
+    for (int k = 0; k < 5; k++) ol_sincos(z * c_ts05.s5_rr[t][k], &szk[k], &czk[k]);
     double hx = 0., hy = 0., hz = 0.;
 #pragma unroll
     for (int i = 0; i < 5; i++) {
         const double rp = c_ts05.s5_rp[t][i];
         double sy, cy;
-        sincos(y * rp, &sy, &cy);
+        ol_sincos(y * rp, &sy, &cy);
 #pragma unroll
         for (int k = 0; k < 5; k++) {
             const double rr = c_ts05.s5_rr[t][k];
             const double sq = c_ts05.s5_sq[t][5 * i + k];
-            const double e = exp(x * sq);
+            const double e = ol_exp(x * sq);
             const double c = coef[5 * i + k];
             hx = hx + c * (-sq * e * cy * szk[k]);
             hy = hy + c * (rp * e * sy * szk[k]);
@@ -131,19 +131,19 @@ __device__ __forceinline__ Vec3 ts05_shlcar5x5(const int t, const double* __rest
 }
 
 // warped + unwarped, deformed.c:4-92
-__device__ __forceinline__ void ts05_warped(const TS05Cond& c, const double x, const double y, const double z, Vec3& b1,
+static __device__ __noinline__ void ts05_warped(const TS05Cond& c, const double x, const double y, const double z, Vec3& b1,
                                             Vec3& b2) {
     const double rho2 = y * y + z * z;
     const double rho = sqrt(rho2);
     double phi = 0., cphi = 1., sphi = 0.;
     if (y != 0. || z != 0.) {
-        phi = atan2(z, y);
+        phi = ol_atan2(z, y);
         const double rr = 1. / rho;
         cphi = div_r(y, rho, rr);
         sphi = div_r(z, rho, rr);
     }
     double sf, cf;
-    sincos(phi, &sf, &cf);
+    ol_sincos(phi, &sf, &cf);
     const double yy = rho * cf, zz = rho * sf;
     const Vec3 f1 = ts05_taildisk(c.d * 1.1, 1., (x - 6. - c.dx1) * 1.1 + 1.2, yy * 1.1, zz * 1.1);
     const Vec3 h1 = ts05_shlcar5x5(0, c.coef1, x, yy, zz);
@@ -181,10 +181,10 @@ __device__ __forceinline__ double ts05_theta_s(const double* __restrict__ A, con
 }
 
 // fialcos, birk_tot.c:311-372, MODE = 1
-__device__ __forceinline__ void ts05_fialcos1(const double R, const double TH, const double sf, const double cfi,
+static __device__ __noinline__ void ts05_fialcos1(const double R, const double TH, const double sf, const double cfi,
                                               const double th0, const double dt, double& bt, double& bp) {
     double st, ctt;
-    sincos(TH, &st, &ctt);
+    ol_sincos(TH, &st, &ctt);
     const double ro = R * st;
     const double tg = st / (1. + ctt);
     const double ctg = st / (1. - ctt);
@@ -223,40 +223,40 @@ __device__ __forceinline__ void ts05_fialcos1(const double R, const double TH, c
 }
 
 // one_cone, birk_tot.c:248-291 (MODE 1)
-__device__ __forceinline__ Vec3 ts05_one_cone(const double* __restrict__ A, const double* __restrict__ q,
+static __device__ __noinline__ Vec3 ts05_one_cone(const double* __restrict__ A, const double* __restrict__ q,
                                              const double x, const double y, const double z, const double dth) {
     const double th0 = A[30];
     const double rho2 = x * x + y * y;
     const double rho = sqrt(rho2);
     const double R = sqrt(rho2 + z * z);
-    const double TH = atan2(rho, z);
-    const double PHI = atan2(y, x);
+    const double TH = ol_atan2(rho, z);
+    const double PHI = ol_atan2(y, x);
     double sth, cth, s2, c2, s3;
-    sincos(TH, &sth, &cth);
-    sincos(2. * TH, &s2, &c2);
-    s3 = sin(3. * TH);
+    ol_sincos(TH, &sth, &cth);
+    ol_sincos(2. * TH, &s2, &c2);
+    s3 = ol_sin(3. * TH);
     const double rs = ts05_r_s(A, q, R, cth, c2);
     const double ths = ts05_theta_s(A, q, R, TH, sth, s2, s3);
     double sf, cfi;
-    sincos(PHI, &sf, &cfi);
+    ol_sincos(PHI, &sf, &cfi);
     double btast, bfast;
     ts05_fialcos1(rs, ths, sf, cfi, th0, dth, btast, bfast);
     const double rr = 1. / R;
     const double rsr = div_r(rs, R, rr);
-    const double stsst = sin(ths) / sth;
+    const double stsst = ol_sin(ths) / sth;
     const double rdp = R + 1E-6, rdm = R - 1E-6;
     const double drsdr = div_c(ts05_r_s(A, q, rdp, cth, c2) - ts05_r_s(A, q, rdm, cth, c2), 2E-6, 1. / 2E-6);
     const double tdp = TH + 1E-6, tdm = TH - 1E-6;
     double sp, cp, sm, cm, s2p, c2p, s2m, c2m;
-    sincos(tdp, &sp, &cp);
-    sincos(tdm, &sm, &cm);
-    sincos(2. * tdp, &s2p, &c2p);
-    sincos(2. * tdm, &s2m, &c2m);
+    ol_sincos(tdp, &sp, &cp);
+    ol_sincos(tdm, &sm, &cm);
+    ol_sincos(2. * tdp, &s2p, &c2p);
+    ol_sincos(2. * tdm, &s2m, &c2m);
     const double drsdt = div_c(ts05_r_s(A, q, R, cp, c2p) - ts05_r_s(A, q, R, cm, c2m), 2E-6, 1. / 2E-6);
     const double dtsdr = div_c(ts05_theta_s(A, q, rdp, TH, sth, s2, s3) - ts05_theta_s(A, q, rdm, TH, sth, s2, s3),
                                2E-6, 1. / 2E-6);
-    const double dtsdt = div_c(ts05_theta_s(A, q, R, tdp, sp, s2p, sin(3. * tdp)) -
-                                   ts05_theta_s(A, q, R, tdm, sm, s2m, sin(3. * tdm)),
+    const double dtsdt = div_c(ts05_theta_s(A, q, R, tdp, sp, s2p, ol_sin(3. * tdp)) -
+                                   ts05_theta_s(A, q, R, tdm, sm, s2m, ol_sin(3. * tdm)),
                                2E-6, 1. / 2E-6);
     const double br = -div_r(rsr, R, rr) * stsst * btast * drsdt;
     const double bth = rsr * stsst * btast * drsdr;
@@ -269,7 +269,7 @@ __device__ __forceinline__ Vec3 ts05_one_cone(const double* __restrict__ A, cons
 }
 
 // birk_1n2, birk_tot.c:125-234 (MODE 1), numb 1 -> R11, 2 -> R21
-__device__ __forceinline__ Vec3 ts05_birk_1n2(const int numb, const double x, const double y, const double z,
+static __device__ __noinline__ Vec3 ts05_birk_1n2(const int numb, const double x, const double y, const double z,
                                              const double xkappa) {
     const double dphi = numb == 1 ? 0.055 : 0.030;
     const double dth = numb == 1 ? 0.06 : 0.09;
@@ -278,16 +278,16 @@ __device__ __forceinline__ Vec3 ts05_birk_1n2(const int numb, const double x, co
     const double rho = sqrt(xs2 + zs2);
     const double rho2 = rho * rho;
     double phi = 0.;
-    if (xs_ != 0. || zs_ != 0.) phi = atan2(-zs_, xs_);
+    if (xs_ != 0. || zs_ != 0.) phi = ol_atan2(-zs_, xs_);
     double sphic, cphic;
-    sincos(phi, &sphic, &cphic);
+    ol_sincos(phi, &sphic, &cphic);
     const double r02 = 49. + rho2;
     const double brack = dphi + 0.5 * 49. / 50. * (rho2 - 1.) / r02;
     const double phis = phi - brack * sphic;
     const double dpsp = 1. - brack * cphic;
     const double dpsr = -2. * 0.5 * 49. * rho / (r02 * r02) * sphic;
     double sphics, cphics;
-    sincos(phis, &sphics, &cphics);
+    ol_sincos(phis, &sphics, &cphics);
     const double xs = rho * cphics, zs = -rho * sphics;
     const double* A = numb == 1 ? c_ts05_a11 : c_ts05_a21;
     const double* q = c_ts05.rs_sq[numb - 1];
@@ -304,23 +304,23 @@ __device__ __forceinline__ Vec3 ts05_birk_1n2(const int numb, const double x, co
 
 // birk_shl (birk_tot.c:374-403, fac = 1) and rc_shield (full_rc.c:690-721):
 // 3x3 Cartesian shields with condition-dependent amplitudes.
-__device__ __forceinline__ Vec3 ts05_shield3(const double* __restrict__ P, const double* __restrict__ Rr,
+static __device__ __noinline__ Vec3 ts05_shield3(const double* __restrict__ P, const double* __restrict__ Rr,
                                             const double* __restrict__ SQ, const double* __restrict__ amp,
                                             const double fac, const bool has_fac, const double x, const double y,
                                             const double z) {
     double szk[3], czk[3];
 #pragma unroll
-    for (int k = 0; k < 3; k++) sincos(z / Rr[k], &szk[k], &czk[k]);
+    for (int k = 0; k < 3; k++) ol_sincos(z / Rr[k], &szk[k], &czk[k]);
     double gx = 0., gy = 0., gz = 0.;
 #pragma unroll
     for (int j = 0; j < 3; j++) {
         const double p = P[j];
         double sy, cy;
-        sincos(y / p, &sy, &cy);
+        ol_sincos(y / p, &sy, &cy);
 #pragma unroll
         for (int k = 0; k < 3; k++) {
             const double sq = SQ[3 * j + k];
-            const double e = exp(x * sq);
+            const double e = ol_exp(x * sq);
             const double a = amp[3 * j + k];
             if (has_fac) {
                 gx += (-sq * e * cy * szk[k] * fac) * a;
@@ -338,21 +338,21 @@ __device__ __forceinline__ Vec3 ts05_shield3(const double* __restrict__ P, const
 
 // ---- full_rc.c ------------------------------------------------------------------
 __device__ __forceinline__ void ts05_ellip(const double xk2s, double& elk, double& ele) {
-    const double dl = log(1. / xk2s);
+    const double dl = ol_log(1. / xk2s);
     elk = 1.38629436112 + xk2s * (0.09666344259 + xk2s * (0.03590092383 + xk2s * (0.03742563713 + xk2s * 0.01451196212))) +
           dl * (0.5 + xk2s * (0.12498593597 + xk2s * (0.06880248576 + xk2s * (0.03328355346 + xk2s * 0.00441787012))));
     ele = 1. + xk2s * (0.44325141463 + xk2s * (0.0626060122 + xk2s * (0.04757383546 + xk2s * 0.01736506451))) +
           dl * xk2s * (0.2499836831 + xk2s * (0.09200180037 + xk2s * (0.04069697526 + xk2s * 0.00526449639)));
 }
 
-__device__ __forceinline__ double ts05_two_loops(const double alpha_s, const double gamma_s, const double rrc1,
+static __device__ __noinline__ double ts05_two_loops(const double alpha_s, const double gamma_s, const double rrc1,
                                                  const double dd1, const double rrc2, const double dd2,
                                                  const double a1, const double a2) {
     const double gs2 = gamma_s * gamma_s;
     const double alsqh = (alpha_s * alpha_s) * 0.5;
     const double F = 64. / 27. * gs2 + (alsqh * alsqh);
-    const double Q = pow((sqrt(F) + alsqh), (1. / 3.));
-    const double g13 = pow(gs2, (1. / 3.));
+    const double Q = ol_pow((sqrt(F) + alsqh), (1. / 3.));
+    const double g13 = ol_pow(gs2, (1. / 3.));
     double C = Q - 4. * g13 / (3. * Q);
     if (C < 0.) C = 0.;
     const double G = sqrt(C * C + 4. * g13);
@@ -379,7 +379,7 @@ __device__ __forceinline__ double ts05_two_loops(const double alpha_s, const dou
     return a1 * aphi1 + a2 * aphi2;
 }
 
-__device__ __forceinline__ double ts05_ap(const double R, const double sint, const double cost) {
+static __device__ __noinline__ double ts05_ap(const double R, const double sint, const double cost) {
     bool prox = false;
     double s1 = sint, c1 = cost;
     if (s1 < 1.E-2) {
@@ -394,9 +394,9 @@ __device__ __forceinline__ double ts05_ap(const double R, const double sint, con
     const double arg1 = -(q1 * q1) - (l1 * l1);
     const double arg2 = -(q2 * q2) - (l2 * l2);
     const double arg3 = -(q3 * q3);
-    const double e1 = arg1 >= -500. ? exp(arg1) : 0.;
-    const double e2 = arg2 >= -500. ? exp(arg2) : 0.;
-    const double e3 = arg3 >= -500. ? exp(arg3) : 0.;
+    const double e1 = arg1 >= -500. ? ol_exp(arg1) : 0.;
+    const double e2 = arg2 >= -500. ? ol_exp(arg2) : 0.;
+    const double e3 = arg3 >= -500. ? ol_exp(arg3) : 0.;
     const double alpha = (s1 * s1) / R;
     const double alpha_s = alpha * (1. + -0.2291904607 * e1 + 0.1556236119 * e2 + 0.1855957207 * e3);
     const double gamma = c1 / (R * R);
@@ -406,7 +406,7 @@ __device__ __forceinline__ double ts05_ap(const double R, const double sint, con
     return ap;
 }
 
-__device__ __forceinline__ double ts05_apprc(const double R, const double sint, const double cost) {
+static __device__ __noinline__ double ts05_apprc(const double R, const double sint, const double cost) {
     constexpr double P1 = .3058309043, ALPHA1 = .1817139853, DAL1 = .1257532909, BETA1 = 3.422509402, DG1 = .04742939676;
     constexpr double P2 = -4.800458958, ALPHA2 = -.02845643596, DAL2 = .2188114228, BETA2 = 2.545944574, DG2 = .00813272793;
     constexpr double BETA3 = .35868244, P3 = 103.1601001, ALPHA3 = -.00764731187, DAL3 = .1046487459;
@@ -427,19 +427,19 @@ __device__ __forceinline__ double ts05_apprc(const double R, const double sint, 
     const double a4 = div_c(alpha - ALPHA4, DAL4, 1. / DAL4);
     const double arg1 = -(g1 * g1);
     const double arg2 = -(a4 * a4) - (g4 * g4);
-    const double e1 = arg1 >= -500. ? exp(arg1) : 0.;
-    const double e2 = arg2 >= -500. ? exp(arg2) : 0.;
+    const double e1 = arg1 >= -500. ? ol_exp(arg1) : 0.;
+    const double e2 = arg2 >= -500. ? ol_exp(arg2) : 0.;
     const double u1 = div_c(alpha - ALPHA1, DAL1, 1. / DAL1);
     const double u2 = div_c(alpha - ALPHA2, DAL2, 1. / DAL2);
     const double u3 = div_c(alpha - ALPHA3, DAL3, 1. / DAL3);
     const double u5 = div_c(alpha - ALPHA5, DAL5, 1. / DAL5);
     const double v2 = div_c(gamma, DG2, 1. / DG2), v3 = div_c(gamma, DG3, 1. / DG3), v5 = div_c(gamma, DG5, 1. / DG5);
     const double am3 = alpha - ALPHA3;
-    const double alpha_s = alpha * (1. + P1 / pow((1. + u1 * u1), BETA1) * e1 +
-                                    P2 * (alpha - ALPHA2) / pow((1. + u2 * u2), BETA2) / pow((1. + v2 * v2), BETA3) +
-                                    P3 * (am3 * am3) / pow((1. + u3 * u3), BETA4) / pow((1. + v3 * v3), BETA5));
+    const double alpha_s = alpha * (1. + P1 / ol_pow((1. + u1 * u1), BETA1) * e1 +
+                                    P2 * (alpha - ALPHA2) / ol_pow((1. + u2 * u2), BETA2) / ol_pow((1. + v2 * v2), BETA3) +
+                                    P3 * (am3 * am3) / ol_pow((1. + u3 * u3), BETA4) / ol_pow((1. + v3 * v3), BETA5));
     const double gamma_s = gamma * (1. + Q0 + Q1 * (alpha - ALPHA4) * e2 +
-                                    Q2 * (alpha - ALPHA5) / pow((1. + u5 * u5), BETA6) / pow((1. + v5 * v5), BETA7));
+                                    Q2 * (alpha - ALPHA5) / ol_pow((1. + u5 * u5), BETA6) / ol_pow((1. + v5 * v5), BETA7));
     double ap = ts05_two_loops(alpha_s, gamma_s, 6.560486035, 1.930711037, 3.827208119, .7789990504, -80.11202281,
                                12.58246758);
     if (prox) ap = ap * sint / s1;
@@ -448,7 +448,7 @@ __device__ __forceinline__ double ts05_apprc(const double R, const double sint, 
 
 // rc_symm (full_rc.c:116-152) and prc_symm (:264-300)
 template <bool PRC>
-__device__ __forceinline__ Vec3 ts05_symm(const double x, const double y, const double z) {
+static __device__ __noinline__ Vec3 ts05_symm(const double x, const double y, const double z) {
     constexpr double DS = 1.E-2, DC = 0.99994999875, D = 1.E-4, DRD = 5E3;
     const double rho2 = x * x + y * y;
     const double r2 = rho2 + z * z;
@@ -466,10 +466,10 @@ __device__ __forceinline__ Vec3 ts05_symm(const double x, const double y, const 
         fxy = z * (2. * A - dardr) / (R * r2);
         bz = div_r(2. * A * (cost * cost) + dardr * (sint * sint), R, rr);
     } else {
-        const double th = atan2(sint, cost);
+        const double th = ol_atan2(sint, cost);
         double stp, ctp, stm, ctm;
-        sincos(th + D, &stp, &ctp);
-        sincos(th - D, &stm, &ctm);
+        ol_sincos(th + D, &stp, &ctp);
+        ol_sincos(th - D, &stm, &ctm);
         const double br = (stp * (PRC ? ts05_apprc(R, stp, ctp) : ts05_ap(R, stp, ctp)) -
                            stm * (PRC ? ts05_apprc(R, stm, ctm) : ts05_ap(R, stm, ctm))) /
                           (R * sint) * DRD;
@@ -493,20 +493,20 @@ __device__ __forceinline__ void ts05_ffs(const double A, const double A0, const 
     FS = 0.5 * (sq1 + sq2) / (sq1 * sq2) * (1. - F * F);
 }
 
-__device__ __forceinline__ double ts05_br_prc_q(const double R, const double sint, const double cost) {
+static __device__ __noinline__ double ts05_br_prc_q(const double R, const double sint, const double cost) {
     const double sint2 = sint * sint, cost2 = cost * cost, sc = sint * cost;
     const double alpha = sint2 / R;
     const double gamma = cost / (R * R);
     double F, FA, FS;
     ts05_ffs(alpha, .1417519429, .6388013110E-02, F, FA, FS);
-    const double d1 = sc * pow(F, 2.318824273) / (pow(div_c(R, 5.303934488, 1. / 5.303934488), 4.213397467) + 1.);
+    const double d1 = sc * ol_pow(F, 2.318824273) / (ol_pow(div_c(R, 5.303934488, 1. / 5.303934488), 4.213397467) + 1.);
     const double d2 = d1 * cost2;
     ts05_ffs(alpha, .1401142771, .2306094179E-01, F, FA, FS);
-    const double d3 = sc * pow(FS, .7955534018) / (pow(div_c(R, 3.462235072, 1. / 3.462235072), 2.568743010) + 1.);
+    const double d3 = sc * ol_pow(FS, .7955534018) / (ol_pow(div_c(R, 3.462235072, 1. / 3.462235072), 2.568743010) + 1.);
     const double d4 = d3 * cost2;
     ts05_ffs(alpha, .1485233485, .2319676273E-01, F, FA, FS);
-    const double d5 = sc * (pow(alpha, 3.477425908)) * (pow(FS, 1.922155110)) /
-                      (pow(div_c(R, 7.830223587, 1. / 7.830223587), 8.492933868) + 1.);
+    const double d5 = sc * (ol_pow(alpha, 3.477425908)) * (ol_pow(FS, 1.922155110)) /
+                      (ol_pow(div_c(R, 7.830223587, 1. / 7.830223587), 8.492933868) + 1.);
     const double d6 = d5 * cost2;
     const double a4 = div_c(alpha - .1295221828, .01753008801, 1. / .01753008801);
     const double g1 = div_c(gamma, .01125504083, 1. / .01125504083);
@@ -535,20 +535,20 @@ __device__ __forceinline__ double ts05_br_prc_q(const double R, const double sin
            -50646.71204 * d16 + 7746.058231 * d17 + 1.531069371 * d18;
 }
 
-__device__ __forceinline__ double ts05_bt_prc_q(const double R, const double sint, const double cost) {
+static __device__ __noinline__ double ts05_bt_prc_q(const double R, const double sint, const double cost) {
     const double sint2 = sint * sint, cost2 = cost * cost;
     const double alpha = sint2 / R;
     const double gamma = cost / (R * R);
     double F, FA, FS;
     ts05_ffs(alpha, .2071721360, .05030555417, F, FA, FS);
-    const double d1 = pow(F, 1.243288286) / (pow(div_c(R, 7.471332374, 1. / 7.471332374), 3.180533613) + 1.);
+    const double d1 = ol_pow(F, 1.243288286) / (ol_pow(div_c(R, 7.471332374, 1. / 7.471332374), 3.180533613) + 1.);
     const double d2 = d1 * cost2;
     ts05_ffs(alpha, .1568504222, .02092910682, F, FA, FS);
-    const double d3 = pow(FA, 1.376743507) / pow(R, 1.985148197);
+    const double d3 = ol_pow(FA, 1.376743507) / ol_pow(R, 1.985148197);
     const double d4 = d3 * cost2;
     ts05_ffs(alpha, .1701395257, .1019870070, F, FA, FS);
-    const double d5 = pow(FS, .3157139940) * pow(alpha, 1.056309517) /
-                      (pow(div_c(R, 6.293740981, 1. / 6.293740981), 5.671824276) + 1.);
+    const double d5 = ol_pow(FS, .3157139940) * ol_pow(alpha, 1.056309517) /
+                      (ol_pow(div_c(R, 6.293740981, 1. / 6.293740981), 5.671824276) + 1.);
     const double d6 = d5 * cost2;
     ts05_ffs(gamma, 0., .01040696080, F, FA, FS);
     const double a4 = div_c(alpha - .1280772299, .02189060799, 1. / .02189060799);
@@ -573,7 +573,7 @@ __device__ __forceinline__ double ts05_bt_prc_q(const double R, const double sin
 }
 
 // prc_quad, full_rc.c:425-481
-__device__ __forceinline__ Vec3 ts05_prc_quad(const double x, const double y, const double z) {
+static __device__ __noinline__ Vec3 ts05_prc_quad(const double x, const double y, const double z) {
     constexpr double D = 1.E-4, DD = 2.E-4, DS = 1.E-2, DC = 0.99994999875;
     const double rho2 = x * x + y * y;
     const double R = sqrt(rho2 + z * z);
@@ -587,20 +587,20 @@ __device__ __forceinline__ Vec3 ts05_prc_quad(const double x, const double y, co
         const double br = ts05_br_prc_q(R, sint, cost);
         const double bt = ts05_bt_prc_q(R, sint, cost);
         const double dbrr = div_c(ts05_br_prc_q(rp, sint, cost) - ts05_br_prc_q(rm, sint, cost), DD, 1. / DD);
-        const double th = atan2(sint, cost);
+        const double th = ol_atan2(sint, cost);
         double stp, ctp, stm, ctm;
-        sincos(th + D, &stp, &ctp);
-        sincos(th - D, &stm, &ctm);
+        ol_sincos(th + D, &stp, &ctp);
+        ol_sincos(th - D, &stm, &ctm);
         const double dbtt = div_c(ts05_bt_prc_q(R, stp, ctp) - ts05_bt_prc_q(R, stm, ctm), DD, 1. / DD);
         return {sint * (br + (br + R * dbrr + dbtt) * (sphi * sphi)) + cost * bt,
                 -sint * sphi * cphi * (br + R * dbrr + dbtt), (br * cost - bt * sint) * cphi};
     }
     const double st = DS;
     const double ct = z < 0. ? -DC : DC;
-    const double th = atan2(st, ct);
+    const double th = ol_atan2(st, ct);
     double stp, ctp, stm, ctm;
-    sincos(th + D, &stp, &ctp);
-    sincos(th - D, &stm, &ctm);
+    ol_sincos(th + D, &stp, &ctp);
+    ol_sincos(th - D, &stm, &ctm);
     const double br = ts05_br_prc_q(R, st, ct);
     const double bt = ts05_bt_prc_q(R, st, ct);
     const double dbrr = div_c(ts05_br_prc_q(rp, st, ct) - ts05_br_prc_q(rm, st, ct), DD, 1. / DD);
@@ -616,7 +616,7 @@ __device__ __forceinline__ Vec3 ts05_prc_quad(const double x, const double y, co
 
 // ---- ts05.c ---------------------------------------------------------------------
 // shlcar3x3, ts05.c:136-235
-__device__ __forceinline__ Vec3 ts05_shlcar3x3(const double x, const double y, const double z) {
+static __device__ __noinline__ Vec3 ts05_shlcar3x3(const double x, const double y, const double z) {
     constexpr double PS[3] = {9.620648151, 6.082014949, 27.75216226};
     constexpr double R1 = 12.44199571, R2 = 5.122226936, R3 = 6.982039615;
     constexpr double r32 = R3 * R3;
@@ -625,9 +625,9 @@ __device__ __forceinline__ Vec3 ts05_shlcar3x3(const double x, const double y, c
                               125.8739681 - 372.3384278,  -235.4720434 + 286.7594095, 21.86305585 - 27.42344605};
     const double z1 = div_c(z, R1, 1. / R1), z2 = div_c(z, R2, 1. / R2), z3 = div_c(z, R3, 1. / R3);
     double s1, c1, s2, c2, s3, c3;
-    sincos(z1, &s1, &c1);
-    sincos(z2, &s2, &c2);
-    sincos(z3, &s3, &c3);
+    ol_sincos(z1, &s1, &c1);
+    ol_sincos(z2, &s2, &c2);
+    ol_sincos(z3, &s3, &c3);
     const double s3r = div_c(s3, R3, 1. / R3);
     const double xr3 = div_c(x, R3, 1. / R3);
     const double xr32 = div_c(x, r32, 1. / r32);
@@ -636,23 +636,23 @@ __device__ __forceinline__ Vec3 ts05_shlcar3x3(const double x, const double y, c
     for (int i = 0; i < 3; i++) {
         const double P = PS[i];
         double syp, cyp;
-        sincos(div_c(y, P, 1. / P), &syp, &cyp);
+        ol_sincos(div_c(y, P, 1. / P), &syp, &cyp);
         double h[9];
         double sq = c_ts05.s3_sq[3 * i];
-        double e = exp(sq * x);
+        double e = ol_exp(sq * x);
         const double ep = div_c(e, P, 1. / P);
         h[0] = -sq * e * cyp * s1;
         h[1] = ep * syp * s1;
         h[2] = div_c(-e * cyp, R1, 1. / R1) * c1;
         sq = c_ts05.s3_sq[3 * i + 1];
-        e = exp(sq * x);
+        e = ol_exp(sq * x);
         const double ep2 = div_c(e, P, 1. / P);
         h[3] = -sq * e * cyp * s2;
         h[4] = ep2 * syp * s2;
         h[5] = div_c(-e * cyp, R2, 1. / R2) * c2;
         sq = c_ts05.s3_sq[3 * i + 2];
         const double rsq = c_ts05.s3_rsq[i];
-        e = exp(sq * x);
+        e = ol_exp(sq * x);
         const double ep3 = div_c(e, P, 1. / P);
         h[6] = -e * cyp * (sq * z * c3 + s3r * (x + rsq));
         h[7] = ep3 * syp * (z * c3 + div_r(xr3 * s3, sq, rsq));
@@ -685,7 +685,7 @@ __device__ __forceinline__ Vec3 ts05_dipole(const double x, const double y, cons
 }
 
 // ts05_gsm, ts05.c:7-134.  X = GSM position [R_E].
-__device__ __forceinline__ Vec3 ts05_field(const TS05Cond& c, const Vec3 X) {
+static __device__ __noinline__ Vec3 ts05_field(const TS05Cond& c, const Vec3 X) {
     const double x = X.x, y = X.y, z = X.z;
     const double oimfy = c.oimfy_k, oimfz = c.oimfz_k;
     double xmxm = c.am + x - c.x0;

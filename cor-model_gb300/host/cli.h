@@ -34,6 +34,7 @@ typedef struct {
     double zn;
     int nk1, iopt, ist;
     double rig, del, rk;
+    double lat_step, lon_step;   /* field mode (src/io.c:52-67) */
 } InfileHeader;
 
 typedef cor_model_params ModelsParams;
@@ -67,6 +68,8 @@ int read_cutoff_infile_header(FILE *input_file, InfileHeader *h);
 int write_cutoff_outfile_header(FILE *output_file, const InfileHeader *h, const Model **models, uint64_t steps_count);
 int read_ts05_params(FILE *input_file, ModelsParams *params);
 int read_t96_params(FILE *input_file, ModelsParams *params);
+int read_field_infile_header(FILE *input_file, InfileHeader *h);
+int write_field_outfile_header(FILE *output_file, const InfileHeader *h, const Model **models);
 
 /* cli_models.c -- src/models.c */
 extern const Model *internal_models[];
@@ -83,5 +86,11 @@ void trajectory_simulation_cutoff(InfileHeader *header, const Model **models, Mo
                                   uint32_t parallel);
 int cli_write_scan(FILE *outfile, const InfileHeader *h, const cor_site_result *site, const uint8_t *status,
                    const cor_traj_record *records);
+
+int trajectory_simulation(InfileHeader *header, const Model **models, ModelsParams *models_params, FILE *tragsm,
+                          FILE *trasph, uint64_t step_limit, double tu_angle, double particle_mass);
+
+/* cli_field.c -- src/field.c */
+int field_simulation(const InfileHeader *header, const ModelsParams *params, const Model **models, FILE *outfile);
 
 #endif

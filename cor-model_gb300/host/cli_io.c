@@ -45,3 +45,27 @@ int read_t96_params(FILE *f, ModelsParams *p) {
     const int items = fscanf(f, "%lf %lf %lf %lf\n", &p->parmod[1], &p->parmod[0], &p->parmod[2], &p->parmod[3]);
     return items != 4 ? -1 : 0;
 }
+
+int read_field_infile_header(FILE *f, InfileHeader *h) {
+    /* src/io.c:52-67: r0 lat0 lon0 / lat_step lon_step lat1 lon1 / date */
+    const int items = fscanf(f, "%lf %lf %lf\n%lf %lf %lf %lf\n%d %d %d %d %d %d %d\n", &h->r0, &h->the0, &h->fi0,
+                             &h->lat_step, &h->lon_step, &h->the1, &h->fi1, &h->iy, &h->mes, &h->ide, &h->id, &h->ih,
+                             &h->min, &h->is);
+    return items < 0 ? -1 : 0;
+}
+
+int write_field_outfile_header(FILE *out, const InfileHeader *h, const Model **models) {
+    /* src/io.c:69-96 */
+    if (fprintf(out, "\n\n\n                GEOMAGNETIC FIELD\n Geomagnetic Model(s): ") < 0) return -1;
+    const char *pad = "";
+    for (int i = 0; models[i]; i++) {
+        if (fprintf(out, "%s%s", pad, models[i]->name) < 0) return -1;
+        pad = ", ";
+    }
+    const int res = fprintf(out,
+                            "\n lat step: %.3f, lon step: %.3f\n"
+                            " Date: %4d %2d %2d  time: %2d h %2d min %2d sec\n\n"
+                            " lat : lon : B [nT] : BXGEO [nT] : BYGEO [nT] : BZGEO [nT]\n",
+                            h->lat_step, h->lon_step, h->iy, h->mes, h->ide, h->ih, h->min, h->is);
+    return res < 0 ? -1 : 0;
+}

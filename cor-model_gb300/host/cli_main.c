@@ -23,7 +23,7 @@ static struct argp_option options[] = {
     { "output", 'o', "FILE", 0, "Output to FILE instead of standard output." },
     { "steps-count", 's', "COUNT", 0, "Maximal single trajectory steps count (default: 25000)" },
     { "tu-angle", 'u', "RAD", 0, "TU angle, specifies the precision of the trajectory calculation (default: 0.01 rad)" },
-    { "mode", 'm', "MODE", 0, "Calculation mode: cutoff (default: cutoff)" },
+    { "mode", 'm', "MODE", 0, "Calculation mode: cutoff, field, trajectory (default: cutoff)" },
     { "particle-type", 't', "TYPE", 0, "Particle type: electron or proton (default: proton)" },
     { "batch", 'b', "MANIFEST", 0, "Trace every 'INFILE OUTFILE' pair listed in MANIFEST in one GPU call" },
     { 0, 0, 0, 0, "Geomagnetic field models:" },
@@ -154,6 +154,118 @@ static int cutoff(const CLIArguments *args, const Model **models) {
     return 0;
 }
 
+/* `-m field` (src/main.c:96-155): the field on a latitude/longitude grid. */
+static int field(const CLIArguments *args, const Model **models) {
+    FILE *f = fopen(args->input_file_name, "r");
+    if (!f) {
+        perror("Error: Cannot open input file for reading");
+        return 1;
+    }
+    InfileHeader h;
+    ModelsParams p;
+    memset(&h, 0, sizeof h);
+    memset(&p, 0, sizeof p);
+    if (read_field_infile_header(f, &h) != 0 || models_setup(models, f, &h, &p) != 0) {
+        fprintf(stderr, "Error: Invalid input file\n");
+        fclose(f);
+        return 1;
+    }
+    if (fclose(f) != 0) {
+        perror("Error: Cannot close input file");
+        return 1;
+    }
+    FILE *out = stdout;
+    if (args->output_file_name) {
+        out = fopen(args->output_file_name, "w");
+        if (!out) {
+            perror("Error: Cannot open output file for writing");
+            return 1;
+        }
+    }
+    if (write_field_outfile_header(out, &h, models) != 0) {
+        fprintf(stderr, "Error: Cannot write output file header\n");
+        if (out != stdout) fclose(out);
+        return 1;
+    }
+    const int rc = field_simulation(&h, &p, models, out);
+    if (out != stdout && fclose(out) != 0) {
+        perror("Error: Cannot close output file");
+        return 1;
+    }
+    return rc;
+}
+
+/* `-m trajectory` (src/main.c:157-252): one INFILE with rig == rk, every
+ * accepted step to tragsm_<OUTPUT> (GSM) and trasph_<OUTPUT> (spherical). */
+static int trajectory(const CLIArguments *args, const Model **models) {
+    if (!args->output_file_name) {
+        fprintf(stderr, "Error: Output file name is required for trajectory calculation mode\n");
+        return 1;
+    }
+    RunOptions o;
+    if (run_options(args, &o)) return 1;
+    FILE *f = fopen(args->input_file_name, "r");
+    if (!f) {
+        perror("Error: Cannot open input file for reading");
+        return 1;
+    }
+    InfileHeader h;
+    ModelsParams p;
+    memset(&h, 0, sizeof h);
+    memset(&p, 0, sizeof p);
+    if (read_cutoff_infile_header(f, &h) != 0) {
+        fprintf(stderr, "Error: Invalid input file\n");
+        fclose(f);
+        return 1;
+    }
+    if (h.rig != h.rk) {
+        fprintf(stderr, "Error: Invalid input file - starting and ending rigidity must be the same for trajectory "
+                        "calculation mode\n");
+        fclose(f);
+        return 1;
+    }
+    if (models_setup(models, f, &h, &p) != 0) {
+        fprintf(stderr, "Error: Invalid input file\n");
+        fclose(f);
+        return 1;
+    }
+    if (fclose(f) != 0) {
+        perror("Error: Cannot close input file");
+        return 1;
+    }
+    /* one rigidity: the step only sizes the single-point grid.  A zero step
+     * makes the reference's grid count round(0/0), which yields no rigidity;
+     * a negative one still gives the single point. */
+    const int none = !(h.del != 0.) || h.del != h.del;
+    if (h.del < 0.) h.del = -h.del;
+    const size_t len = strlen(args->output_file_name);
+    char *gsm_name = malloc(len + 8), *sph_name = malloc(len + 8);
+    if (!gsm_name || !sph_name) return 1;
+    strcpy(gsm_name, "tragsm_");
+    strcat(gsm_name, args->output_file_name);
+    strcpy(sph_name, "trasph_");
+    strcat(sph_name, args->output_file_name);
+    FILE *g = fopen(gsm_name, "w");
+    if (!g) {
+        perror("Error: Cannot open tragsm output file for writing");
+        return 1;
+    }
+    FILE *s = fopen(sph_name, "w");
+    if (!s) {
+        fclose(g);
+        perror("Error: Cannot open trasfer output file for writing");
+        return 1;
+    }
+    const int rc = none ? 0 : trajectory_simulation(&h, models, &p, g, s, o.steps, o.tu_angle, o.mass);
+    free(gsm_name);
+    free(sph_name);
+    if (fclose(g) != 0 || fclose(s) != 0) {
+        perror("Error: Cannot close output file");
+        return 1;
+    }
+    return rc;
+}
+
 /* -b MANIFEST: all scans in one cor_trace_batch call, one parameter block per
  * INFILE (each INFILE has its own date and external-field parameters). */
 static int batch(const CLIArguments *args, const Model **models) {
@@ -257,8 +369,10 @@ int main(int argc, char **argv) {
         }
         models[index++] = m;
     }
+    if (strcmp(args.mode, "field") == 0) return field(&args, models);
+    if (strcmp(args.mode, "trajectory") == 0) return trajectory(&args, models);
     if (strcmp(args.mode, "cutoff") != 0) {
-        fprintf(stderr, "Error: Invalid calculation mode (this build provides the cutoff scan only)\n");
+        fprintf(stderr, "Error: Invalid calculation mode\n");
         return 1;
     }
     return args.batch_file_name ? batch(&args, models) : cutoff(&args, models);

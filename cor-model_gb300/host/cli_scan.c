@@ -38,6 +38,8 @@ static void job_from_header(const InfileHeader *h, cor_scan_job *j) {
     j->zn = h->zn;
     j->nk1 = h->nk1;
     j->param_index = 0;
+    j->i_first = 0;  /* the whole grid */
+    j->i_count = 0;
 }
 
 /* car_to_sph, src/utils.c:43-73 */
@@ -132,4 +134,68 @@ void trajectory_simulation_cutoff(InfileHeader *header, const Model **models, Mo
     cli_write_scan(outfile, header, &site, status, records);
     free(status);
     free(records);
+}
+
+/* `cor -m trajectory` (src/trajectory.c:163-273): every accepted step of each
+ * rigidity, traced on the GPU with the scan's integrator and recorded there
+ * (cor_trace_steps), printed here in the reference's two formats. */
+#define TRAJ_MAX_RECORDED 4000000u
+
+int trajectory_simulation(InfileHeader *header, const Model **models, ModelsParams *models_params, FILE *tragsm,
+                          FILE *trasph, uint64_t step_limit, double tu_angle, double particle_mass) {
+    cor_ctx *ctx;
+    if (cli_context(&ctx) != COR_OK) return 1;
+    cor_scan_job job;
+    job_from_header(header, &job);
+    uint64_t n = 0;
+    if (cor_batch_count(&job, 1, &n, NULL) != COR_OK) {
+        fprintf(stderr, "Error: invalid rigidity grid\n");
+        return 1;
+    }
+    const uint32_t cap = step_limit < TRAJ_MAX_RECORDED ? (uint32_t)(step_limit ? step_limit : 1) : TRAJ_MAX_RECORDED;
+    cor_step_record *steps = (cor_step_record *)malloc(sizeof(cor_step_record) * (size_t)cap * (size_t)n);
+    cor_traj_record *records = (cor_traj_record *)malloc(sizeof(cor_traj_record) * (size_t)n);
+    uint8_t *status = (uint8_t *)malloc((size_t)n);
+    if (!steps || !records || !status) {
+        fprintf(stderr, "Error: out of memory\n");
+        return 1;
+    }
+    cor_site_result site;
+    cor_batch_req req;
+    memset(&req, 0, sizeof req);
+    req.jobs = &job;
+    req.n_jobs = 1;
+    req.params = models_params;
+    req.n_params = 1;
+    req.models = models_device_set(models);
+    req.step_limit = step_limit;
+    req.tu_angle = tu_angle;
+    req.particle_mass = particle_mass;
+    cor_batch_result res;
+    memset(&res, 0, sizeof res);
+    res.sites = &site;
+    res.status = status;
+    res.records = records;
+    if (cor_trace_steps(ctx, &req, &res, steps, cap) != COR_OK) {
+        fprintf(stderr, "Error: %s\n", cor_last_error_string(ctx));
+        return 1;
+    }
+    for (uint64_t t = 0; t < n; t++) {
+        const cor_step_record *s = steps + t * cap;
+        for (uint32_t k = 0; k < cap && s[k].step == k + 1; k++) {
+            double sph[3];
+            car_to_sph(s[k].pos, sph);
+            const double r = sph[0] / DEF_RE;
+            const double td = 90. - (sph[1] / DEF_TO_RAD);
+            const double fei = sph[2] / DEF_TO_RAD;
+            fprintf(tragsm, "%6d%17.5f%17.5f%17.5f%14.2f%15.10f%18.2f\n", (int)s[k].step, s[k].gsm[0], s[k].gsm[1],
+                    s[k].gsm[2], s[k].v, s[k].time, s[k].length);
+            fprintf(trasph, "%6d%17.5f%17.5f%17.5f%14.2f%15.10f%18.2f\n", (int)s[k].step, r, td, fei, s[k].v,
+                    s[k].time, s[k].length);
+        }
+    }
+    free(steps);
+    free(records);
+    free(status);
+    return 0;
 }

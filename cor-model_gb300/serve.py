@@ -1,0 +1,276 @@
+"""Serving loop for cutoff-map requests (no counterpart in the reference).
+
+A request is one site or a latitude/longitude grid box, one geomagnetic
+condition, vertical incidence or 9 directions (vertical plus 30 deg zenith at
+8 azimuths), scanned on the 0.01 GV grid.  Requests arrive as a seeded
+Poisson stream.  The server keeps several slots in flight, each a context
+with its own CUDA stream (continuous batching): whenever a slot is free it
+takes every admitted request that is waiting, up to a per-batch trajectory
+cap, and traces them in one call while the other slots' batches run on the
+GPU.  A request is admitted when its device memory (jobs, start vectors,
+offsets, classes, results, parameter block) fits in what the HBM budget has
+left after the requests in flight.  With a window model, each site-direction
+is first scanned over its predicted window and falls back to the full scan
+on an edge hit.  Each request's latency runs from its arrival to the end of
+the batch that completed it; results are per site-direction P(S), P(C), P(M),
+identical whether a request ran alone or in a mix (trajectories are
+independent and deterministic).
+
+    python cor-model_gb300/serve.py --rate 2 --requests 40 [--window FILE]
+"""
+from __future__ import annotations
+
+import argparse
+import dataclasses
+import json
+import os
+import queue
+import sys
+import threading
+import time
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, HERE)
+
+import autotune  # noqa: E402
+import cortrace as ct  # noqa: E402
+import window  # noqa: E402
+
+DIRECTIONS_9 = [(0.0, 0.0)] + [(30.0, 45.0 * k) for k in range(8)]
+R0 = 1.0031391260673028
+
+
+@dataclasses.dataclass
+class Request:
+    rid: int
+    arrival: float                 # seconds after the stream's start
+    sites: list                    # [(lat, lon)]
+    directions: list               # [(zenith, azimuth)]
+    time7: list
+    parmod: list
+    external: int = ct.EXTERNAL_TS05
+    rig: tuple = (0.01, 20.0, 0.01)
+    # filled by the server
+    done_at: float = -1.0
+    result: np.ndarray | None = None   # SITE_DTYPE per site-direction
+    fallback: int = 0
+
+    @property
+    def n_scans(self) -> int:
+        return len(self.sites) * len(self.directions)
+
+    @property
+    def n_rig(self) -> int:
+        r, rk, d = self.rig
+        return int(round((rk - r) / d)) + 1
+
+    def device_bytes(self) -> int:
+        n = self.n_scans
+        traj = n * self.n_rig
+        return n * (ct.JOB_DTYPE.itemsize + ct.TRIG_DTYPE.itemsize + ct.SITE_DTYPE.itemsize + 8) + traj + \
+            ct.PARAMS_DTYPE.itemsize + 4096
+
+
+def poisson_stream(seed: int, rate: float, n: int, external=ct.EXTERNAL_TS05, max_box_sites: int = 64) -> list:
+    """n requests with exponential inter-arrival times of mean 1/rate: half
+    single sites, half grid boxes of 2-10 deg spacing (at most max_box_sites
+    sites); vertical incidence or the 9 directions; storm-range conditions."""
+    rng = np.random.default_rng(seed)
+    t = 0.0
+    out = []
+    for k in range(n):
+        t += rng.exponential(1.0 / rate)
+        if rng.uniform() < 0.5:
+            sites = [(float(np.degrees(np.arcsin(rng.uniform(-1, 1)))), float(rng.uniform(0, 360)))]
+        else:
+            sp = float(rng.integers(2, 11))
+            side = int(max(1, np.floor(np.sqrt(max_box_sites))))
+            nlat, nlon = int(rng.integers(1, side + 1)), int(rng.integers(1, side + 1))
+            lat0 = float(rng.uniform(-88, 88 - sp * (nlat - 1))) if sp * (nlat - 1) < 176 else -88.0
+            lon0 = float(rng.uniform(0, 360))
+            sites = [(min(88.0, lat0 + sp * i), (lon0 + sp * j) % 360.0) for i in range(nlat) for j in range(nlon)]
+        dirs = [(0.0, 0.0)] if rng.uniform() < 0.5 else DIRECTIONS_9
+        cond = window.sample_conditions(rng, 1, "ts05" if external == ct.EXTERNAL_TS05 else "t96")[0]
+        out.append(Request(k, t, sites, dirs, cond["time7"], cond["parmod"], external))
+    return out
+
+
+def request_jobs(req: Request, param_index: int) -> np.ndarray:
+    r, rk, d = req.rig
+    jobs = []
+    for lat, lon in req.sites:
+        for zen, az in req.directions:
+            the1, fi1 = window.arrival_direction(lat, lon, zen, az)
+            jobs.append(ct.make_job(lat, lon, rig=r, rk=rk, dele=d, r0=R0, the1=the1, fi1=fi1,
+                                    param_index=param_index))
+    return np.concatenate(jobs)
+
+
+def request_features(req: Request, params: np.ndarray) -> np.ndarray:
+    tilt = window.dipole_tilt(params)
+    ep = window.decimal_epoch(req.time7)
+    return np.array([window.features(lat, lon, zen, az, ep, req.parmod, tilt)
+                     for lat, lon in req.sites for zen, az in req.directions])
+
+
+class Server:
+    """Continuous batching over `slots` contexts under an HBM budget."""
+
+    def __init__(self, device: int = 0, slots: int = 3, hbm_budget: float = 40e9, max_batch_traj: int = 2_000_000,
+                 window_model: window.WindowModel | None = None, executor=None):
+        self.budget = int(hbm_budget)
+        self.in_flight = 0
+        self.max_batch_traj = max_batch_traj
+        self.window_model = window_model
+        self.lock = threading.Condition()
+        self.waiting: list[Request] = []
+        self.closed = False
+        self.t0 = None
+        self.batches = 0
+        self.rejected: list[Request] = []
+        if executor is None:
+            self.ctxs = [ct.Context(device) for _ in range(slots)]
+            tune = autotune.load_tuning()
+            if tune:
+                for c in self.ctxs:
+                    c.set_regroup(tune["park_below"], tune["max_generations"], tune["min_park"])
+            self.executor = self._gpu_execute
+        else:
+            self.ctxs = [None] * slots
+            self.executor = executor
+        self.threads = [threading.Thread(target=self._slot_loop, args=(c,), daemon=True) for c in self.ctxs]
+
+    # -- the GPU path: one call per batch, windows first when a model is loaded
+    def _gpu_execute(self, ctx, jobs, params, models, feats):
+        if self.window_model is None or feats is None:
+            res = ctx.trace_batch(jobs, params, models=models, want_status=False)
+            return res.sites, np.zeros(len(jobs), bool)
+        i_lo, i_hi = self.window_model.windows(feats)
+        sites, fb, _, _ = window.trace_windows(ctx, jobs, params, models, i_lo, i_hi)
+        return sites, fb
+
+    def start(self):
+        self.t0 = time.perf_counter()
+        for t in self.threads:
+            t.start()
+
+    def now(self) -> float:
+        return time.perf_counter() - self.t0
+
+    def submit(self, req: Request):
+        with self.lock:
+            if req.device_bytes() > self.budget:
+                req.done_at = self.now()
+                self.rejected.append(req)
+                return
+            self.waiting.append(req)
+            self.lock.notify_all()
+
+    def close(self):
+        with self.lock:
+            self.closed = True
+            self.lock.notify_all()
+        for t in self.threads:
+            t.join()
+        for c in self.ctxs:
+            if c is not None:
+                c.close()
+
+    def _take(self) -> list[Request] | None:
+        with self.lock:
+            while True:
+                batch, traj, mem = [], 0, 0
+                for r in list(self.waiting):
+                    b = r.device_bytes()
+                    n = r.n_scans * r.n_rig
+                    if self.in_flight + mem + b > self.budget:
+                        break                      # admission: wait for memory to free up
+                    if batch and traj + n > self.max_batch_traj:
+                        break
+                    batch.append(r)
+                    traj += n
+                    mem += b
+                if batch:
+                    for r in batch:
+                        self.waiting.remove(r)
+                    self.in_flight += mem
+                    return batch
+                if self.closed and not self.waiting:
+                    return None
+                self.lock.wait(0.05)
+
+    def _slot_loop(self, ctx):
+        while True:
+            batch = self._take()
+            if batch is None:
+                return
+            by_ext = {}
+            for r in batch:
+                by_ext.setdefault(r.external, []).append(r)
+            for ext, reqs in by_ext.items():
+                params = np.concatenate([ct.internal_setup("igrf14", r.time7, parmod=r.parmod) for r in reqs])
+                jobs = np.concatenate([request_jobs(r, k) for k, r in enumerate(reqs)])
+                feats = None
+                if self.window_model is not None:
+                    feats = np.concatenate([request_features(r, params[k:k + 1]) for k, r in enumerate(reqs)])
+                sites, fb = self.executor(ctx, jobs, params, ct.model_set(ct.INTERNAL_SH, ext), feats)
+                o = 0
+                t = self.now()
+                for r in reqs:
+                    r.result = sites[o:o + r.n_scans].copy()
+                    r.fallback = int(fb[o:o + r.n_scans].sum())
+                    r.done_at = t
+                    o += r.n_scans
+            with self.lock:
+                self.in_flight -= sum(r.device_bytes() for r in batch)
+                self.batches += 1
+                self.lock.notify_all()
+
+
+def run_stream(server: Server, reqs: list[Request]) -> dict:
+    """Feeds the requests at their arrival times and waits for all of them."""
+    server.start()
+    for r in reqs:
+        delay = r.arrival - server.now()
+        if delay > 0:
+            time.sleep(delay)
+        server.submit(r)
+    server.close()
+    wall = max([r.done_at for r in reqs] + [server.now()])
+    lat = np.array([r.done_at - r.arrival for r in reqs if r.result is not None])
+    scans = sum(r.n_scans for r in reqs if r.result is not None)
+    return {"requests": len(reqs), "completed": int(len(lat)), "rejected": len(server.rejected),
+            "batches": server.batches, "site_cutoffs": scans, "wall_s": wall,
+            "site_cutoffs_per_s": scans / wall if wall > 0 else 0.0,
+            "latency_p50_s": float(np.percentile(lat, 50)) if len(lat) else None,
+            "latency_p99_s": float(np.percentile(lat, 99)) if len(lat) else None,
+            "fallbacks": int(sum(r.fallback for r in reqs))}
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--rate", type=float, default=1.0, help="requests per second")
+    ap.add_argument("--requests", type=int, default=20)
+    ap.add_argument("--seed", type=int, default=7)
+    ap.add_argument("--slots", type=int, default=3)
+    ap.add_argument("--budget-gb", type=float, default=40.0)
+    ap.add_argument("--external", default="ts05", choices=["t96", "ts05"])
+    ap.add_argument("--window", default=None, help="trained window model (train_window.py output)")
+    ap.add_argument("--max-box-sites", type=int, default=16)
+    args = ap.parse_args()
+    ext = ct.EXTERNAL_TS05 if args.external == "ts05" else ct.EXTERNAL_T96
+    reqs = poisson_stream(args.seed, args.rate, args.requests, ext, args.max_box_sites)
+    wm = window.WindowModel(args.window) if args.window else None
+    srv = Server(0, args.slots, args.budget_gb * 1e9, window_model=wm)
+    out = run_stream(srv, reqs)
+    out.update({"rate": args.rate, "seed": args.seed, "slots": args.slots, "external": args.external,
+                "window": bool(args.window)})
+    print(json.dumps(out), flush=True)
+    if wm:
+        wm.close()
+
+
+if __name__ == "__main__":
+    main()

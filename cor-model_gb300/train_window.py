@@ -1,0 +1,173 @@
+"""Train the learned rigidity window on cutoffs traced by the plain GPU scan.
+
+    python cor-model_gb300/train_window.py [--samples N] [--val M] [--seed S] [--out FILE]
+
+1. Seeded site-directions (uniform over the sphere; half vertical, half at
+   30 deg zenith and one of 8 azimuths) and conditions (window.sample_conditions:
+   Pdyn, Dst, By, Bz over storm ranges, the tilt through the date), IGRF-14 + T96.
+2. Labels from the plain tracer: a coarse scan (20 -> 0.1 GV by 0.1) of every
+   sample, then the 0.01 GV grid traced over the coarse penumbra plus a margin;
+   R_U and R_L of that window are the labels (log GV).
+3. The network (include/cor_window.h) is trained on the GPU with its own
+   tensor-core kernels (AdamW, minibatches), on standardised features and
+   targets.
+4. The residual spread on the held-out samples gives sigma_U, sigma_L, the
+   half-widths (in log R) the windows are built from.
+The result (parameters, standardisation, sigmas, provenance) goes to --out.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import os
+import sys
+import time
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, HERE)
+
+import cortrace as ct  # noqa: E402
+import window  # noqa: E402
+
+R0 = 1.0031391260673028          # 20 km, as the reference's INFILEs give it
+COARSE = (0.1, 20.0, 0.1)
+MARGIN = 20                      # fine-grid indices traced beyond the coarse penumbra
+
+
+def sample_sites(rng, n):
+    lat = np.degrees(np.arcsin(rng.uniform(-1, 1, n)))
+    lon = rng.uniform(0, 360, n)
+    vertical = rng.uniform(0, 1, n) < 0.5
+    az = rng.integers(0, 8, n) * 45.0
+    zen = np.where(vertical, 0.0, 30.0)
+    return lat, lon, zen, np.where(vertical, 0.0, az)
+
+
+def build_samples(rng, n, external="t96"):
+    lat, lon, zen, az = sample_sites(rng, n)
+    conds = window.sample_conditions(rng, n, external)
+    params = np.concatenate([ct.internal_setup("igrf14", c["time7"], parmod=c["parmod"]) for c in conds])
+    feats, dirs = [], []
+    for k in range(n):
+        the1, fi1 = window.arrival_direction(lat[k], lon[k], zen[k], az[k])
+        dirs.append((the1, fi1))
+        feats.append(window.features(lat[k], lon[k], zen[k], az[k], window.decimal_epoch(conds[k]["time7"]),
+                                     conds[k]["parmod"], window.dipole_tilt(params[k:k + 1])))
+    return {"lat": lat, "lon": lon, "dirs": dirs, "params": params, "features": np.array(feats)}
+
+
+def label(ctx, s, models, chunk=4000):
+    """(log R_U, log R_L, trajectories traced) of every sample."""
+    n = len(s["lat"])
+    traced = 0
+    ru = np.zeros(n)
+    rl = np.zeros(n)
+    for a in range(0, n, chunk):
+        b = min(n, a + chunk)
+        jobs = np.concatenate([ct.make_job(s["lat"][k], s["lon"][k], rig=COARSE[0], rk=COARSE[1], dele=COARSE[2],
+                                           r0=R0, the1=s["dirs"][k][0], fi1=s["dirs"][k][1], param_index=k - a)
+                               for k in range(a, b)])
+        res = ctx.trace_batch(jobs, s["params"][a:b], models=models, want_status=False)
+        traced += int(res.counters["trajectories"])
+        lo = np.array([res.sites[k]["r_lower"] for k in range(b - a)])
+        hi = np.array([res.sites[k]["r_upper"] for k in range(b - a)])
+        i_lo = np.clip(np.floor((lo - COARSE[2] - window.GRID_RIG) / window.GRID_DEL) - MARGIN, 0,
+                       window.GRID_N - 1).astype(int)
+        i_hi = np.clip(np.ceil((hi - window.GRID_RIG) / window.GRID_DEL) + MARGIN, 0, window.GRID_N - 1).astype(int)
+        fine = np.concatenate([ct.make_job(s["lat"][k], s["lon"][k], rig=window.GRID_RIG, rk=20.0,
+                                           dele=window.GRID_DEL, r0=R0, the1=s["dirs"][k][0], fi1=s["dirs"][k][1],
+                                           param_index=k - a, i_first=int(i_lo[k - a]), i_last=int(i_hi[k - a]))
+                               for k in range(a, b)])
+        fr = ctx.trace_batch(fine, s["params"][a:b], models=models, want_status=False)
+        traced += int(fr.counters["trajectories"])
+        ru[a:b] = np.log(np.maximum(fr.sites["r_upper"], window.GRID_RIG))
+        rl[a:b] = np.log(np.maximum(fr.sites["r_lower"], window.GRID_RIG))
+        print(f"  labelled {b}/{n} ({traced} trajectories)", flush=True)
+    return ru, rl, traced
+
+
+def train(x, y, xv, yv, seed, epochs, batch=512, lr=2e-3):
+    import torch
+    net = window.Network(0, max_batch=max(batch, len(xv)))
+    net.set_params(window.init_params(seed))
+    xd = torch.from_numpy(x.astype(np.float32)).cuda()
+    yd = torch.from_numpy(y.astype(np.float32)).cuda()
+    rng = np.random.default_rng(seed)
+    n = len(x)
+    steps = 0
+    for ep in range(epochs):
+        perm = torch.from_numpy(rng.permutation(n)).cuda()
+        lr_ep = lr * 0.5 * (1 + math.cos(math.pi * ep / epochs))
+        tot = 0.0
+        for a in range(0, n - batch + 1, batch):
+            idx = perm[a:a + batch]
+            tot += net.train_step(xd[idx], yd[idx], lr=lr_ep, weight_decay=1e-4)
+            steps += 1
+        if ep % 10 == 0 or ep == epochs - 1:
+            pv = net.forward(torch.from_numpy(xv.astype(np.float32)).cuda()).cpu().numpy()
+            print(f"  epoch {ep}: train loss {tot / max(1, n // batch):.4f}, val mse {np.mean((pv - yv) ** 2):.4f}",
+                  flush=True)
+    params = net.get_params()
+    pv = net.forward(torch.from_numpy(xv.astype(np.float32)).cuda()).cpu().numpy()
+    net.close()
+    return params, pv, steps
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--samples", type=int, default=8000)
+    ap.add_argument("--val", type=int, default=1000)
+    ap.add_argument("--seed", type=int, default=2024)
+    ap.add_argument("--epochs", type=int, default=200)
+    ap.add_argument("--batch", type=int, default=512)
+    ap.add_argument("--out", default=os.path.join(HERE, "window_t96.npz"))
+    ap.add_argument("--labels", default=None, help="labelled set: loaded when the file exists, else traced "
+                    "and saved there")
+    args = ap.parse_args()
+    rng = np.random.default_rng(args.seed)
+    models = ct.model_set(ct.INTERNAL_SH, ct.EXTERNAL_T96)
+    t0 = time.time()
+    tr = build_samples(rng, args.samples)
+    va = build_samples(rng, args.val)
+    if args.labels and os.path.exists(args.labels):
+        d = np.load(args.labels)
+        assert d["features"].shape == tr["features"].shape, "labels were made for other samples"
+        ru, rl, vru, vrl = d["ru"], d["rl"], d["vru"], d["vrl"]
+        n1, n2 = int(d["n1"]), int(d["n2"])
+    else:
+        ctx = ct.Context(0)
+        ru, rl, n1 = label(ctx, tr, models)
+        vru, vrl, n2 = label(ctx, va, models)
+        ctx.close()
+        if args.labels:
+            np.savez(args.labels, features=tr["features"], ru=ru, rl=rl, val_features=va["features"], vru=vru,
+                     vrl=vrl, n1=n1, n2=n2)
+    t_label = time.time() - t0
+    print(f"labels: {n1 + n2} trajectories in {t_label:.0f} s", flush=True)
+    fm, fs = tr["features"].mean(0), tr["features"].std(0)
+    fs[fs == 0] = 1.0
+    y = np.stack([ru, rl], 1)
+    ym, ys = y.mean(0), y.std(0)
+    x = (tr["features"] - fm) / fs
+    xv = (va["features"] - fm) / fs
+    yn = (y - ym) / ys
+    yvn = (np.stack([vru, vrl], 1) - ym) / ys
+    params, pv, steps = train(x, yn, xv, yvn, args.seed, args.epochs, batch=args.batch)
+    resid = (pv * ys + ym) - np.stack([vru, vrl], 1)
+    sigma = resid.std(0)
+    print(f"held-out residual sigma (log R): U {sigma[0]:.4f}, L {sigma[1]:.4f}; "
+          f"|resid| > 3 sigma: {np.mean(np.abs(resid) > 3 * sigma, 0)}", flush=True)
+    info = {"samples": args.samples, "val": args.val, "seed": args.seed, "epochs": args.epochs, "steps": steps,
+            "batch": args.batch, "sigma_log_ru": float(sigma[0]), "sigma_log_rl": float(sigma[1]),
+            "model": "igrf14+t96", "label_trajectories": n1 + n2, "label_seconds": t_label,
+            "total_seconds": time.time() - t0}
+    np.savez(args.out, params=params, feat_mean=fm, feat_std=fs, y_mean=ym, y_std=ys, sigma=sigma,
+             val_features=va["features"], val_targets=np.stack([vru, vrl], 1), info=json.dumps(info))
+    print(json.dumps(info), flush=True)
+
+
+if __name__ == "__main__":
+    main()

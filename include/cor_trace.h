@@ -27,7 +27,7 @@
 extern "C" {
 #endif
 
-#define COR_TRACE_ABI_VERSION 1
+#define COR_TRACE_ABI_VERSION 2
 
 /* Number of Gauss coefficients of the degree-13 internal models
  * (INTERNAL_COEFS_SIZE, lib/internal/coefs/coefs.h:6). */
@@ -78,8 +78,14 @@ typedef struct {
 
 /* One rigidity scan = one INFILE of `cor -m cutoff` (InfileHeader,
  * src/common.h:26-54; read by read_cutoff_infile_header, src/io.c:4-20).
- * Rigidities are rig + i*del for i = 0 .. round((rk-rig)/del)
- * (src/trajectory.c:7,14). */
+ * The scan's grid is rig + i*del for i = 0 .. N-1, N = round((rk-rig)/del) + 1
+ * (src/trajectory.c:7,14).  i_first / i_count select a window of that grid
+ * (no counterpart in the reference; zero = the reference's whole scan): the
+ * indices i_first .. i_first + i_count - 1 are traced with the same
+ * rigidities rig + i*del as the whole scan, and the reduction counts the
+ * untraced indices below the window as forbidden and those above it as
+ * allowed, so a window that holds the whole penumbra gives the whole scan's
+ * P(S), P(C), P(M) bit for bit. */
 typedef struct {
     double r0;     /* start radius [R_E]                              */
     double the0;   /* start geographic latitude [deg]                 */
@@ -92,6 +98,8 @@ typedef struct {
     double zn;     /* charge number                                   */
     int32_t nk1;   /* steps per gyro period (initial)                 */
     int32_t param_index; /* which cor_model_params block this scan uses */
+    int32_t i_first; /* first grid index traced (0: from the grid's start) */
+    int32_t i_count; /* indices traced (0: to the grid's end)             */
 } cor_scan_job;
 
 /* Termination class of one trajectory (src/trajectory.c:48-145). */
@@ -125,8 +133,8 @@ typedef struct {
     double r_lower;     /* rmi  */
     double r_upper;     /* rmx  = max(rmx1, rmx2) + del */
     double r_cutoff;    /* rms  = rmi + zan*del */
-    int32_t n_forbidden;  /* nza */
-    int32_t n_traj;
+    int32_t n_forbidden;  /* nza (a window's untraced lower indices count as forbidden) */
+    int32_t n_traj;       /* trajectories traced                                   */
 } cor_site_result;
 
 typedef struct {
@@ -196,6 +204,16 @@ int cor_trace_batch(cor_ctx *ctx, const cor_batch_req *req, cor_batch_result *ou
  * host. */
 int cor_upload_params(cor_ctx *ctx, const cor_model_params *params, int32_t n_params);
 
+/* Regrouping of the scan kernel on this context (no counterpart in the
+ * reference; an autotuner's knobs).  After the work queue drains, a block
+ * parks its live trajectories for the next kernel generation when fewer than
+ * park_below lanes per warp are live (0..32; default 16), or once half of the
+ * generation's warps have parked; at most max_generations generations run
+ * (1..1024; default 48; 1 = never regroup), and a generation with at most
+ * min_park live trajectories (default 256) runs them to the end.  Results
+ * do not depend on these settings, only the time does. */
+int cor_ctx_set_regroup(cor_ctx *ctx, int32_t park_below, int32_t max_generations, int64_t min_park);
+
 /* Replaces the crustal model's coefficient table on this context: G and H as
  * packed lower triangles (index n*(n+1)/2 + m, degrees n = 0 .. nmax-1), the
  * layout of lib/chaos/coefs/chaos_7_16.h read by chaos_geo
@@ -254,6 +272,30 @@ int cor_trace_batch_device_noalloc(cor_ctx *ctx,
                                    double tu_angle, double particle_mass,
                                    cor_site_result *sites_dev, cor_traj_record *records_dev,
                                    cor_counters *counters_dev, uint32_t flags, void *stream);
+
+/* ---- trajectory dump (`cor -m trajectory`) ----------------------------- */
+/* One accepted step of a traced trajectory: what trajectory_simulation
+ * (src/trajectory.c:163-273) prints per step to its tragsm_ and trasph_ files
+ * (the host derives r, latitude and longitude from pos with the C library). */
+typedef struct {
+    double gsm[3];    /* GSM position [m]                 */
+    double pos[3];    /* GEO position [m]                 */
+    double v;         /* speed [m/s]                      */
+    double time;      /* accumulated time [s]             */
+    double length;    /* accumulated path length [m]      */
+    uint32_t step;    /* accepted step number (1-based)   */
+    uint32_t reserved;
+} cor_step_record;
+
+/* Traces every rigidity of the jobs like cor_trace_batch and also records
+ * each accepted step: trajectory t (in batch order) writes its steps 1..k to
+ * steps[t * step_capacity .. t * step_capacity + k - 1] for k up to
+ * step_capacity (steps beyond the capacity are traced but not recorded).
+ * out->records, when given, holds each trajectory's final state, whose
+ * `steps` is the number of accepted steps.  The reference's trajectory mode
+ * traces one rigidity per INFILE (rig == rk). */
+int cor_trace_steps(cor_ctx *ctx, const cor_batch_req *req, cor_batch_result *out, cor_step_record *steps,
+                    uint32_t step_capacity);
 
 /* ---- field ------------------------------------------------------------ */
 /* calculate_field (src/models.c:194-207) at n points: gsm_pos is n x 3 GSM

@@ -273,6 +273,15 @@ static int64_t o_n_rig(const cor_scan_job *job) {
     return (int64_t)(int)round((job->rk - job->rig) / job->del) + 1;  /* :7,12 */
 }
 
+/* Indices traced: the whole grid, or the window i_first .. i_first+i_count-1
+ * of it (cor_trace.h); -1 for an invalid window. */
+static int64_t o_n_traced(const cor_scan_job *job) {
+    const int64_t n = o_n_rig(job);
+    if (job->i_first < 0 || job->i_count < 0 || job->i_first >= n) return -1;
+    const int64_t m = job->i_count ? job->i_count : n - job->i_first;
+    return job->i_first + m > n ? -1 : m;
+}
+
 /* One trajectory, src/trajectory.c:13-153.  Returns the COR_TRAJ_* class. */
 static int o_trace_one(const cor_scan_job *job, const cor_model_params *p, cor_model_set models,
                        uint64_t step_limit, double tu_angle, double mass, double rig,
@@ -369,11 +378,13 @@ int orc_scan_job(const cor_scan_job *job, const cor_model_params *params, cor_mo
                  cor_site_result *site, uint8_t *status, cor_traj_record *records,
                  cor_counters *counters) {
     if (!(job->del > 0.)) return COR_ERR_INVALID;
-    const int64_t n = o_n_rig(job);
-    int nza = 0;
+    const int64_t n = o_n_traced(job);
+    if (n < 0) return COR_ERR_INVALID;
+    int nza = job->i_first;  /* a window's untraced lower indices count as forbidden */
     double rmx1 = 0., rmx2 = 0., rmi = job->rk;                        /* :8-9 */
     uint64_t steps = 0, trials = 0, wd = 0;
-    for (int64_t i = 0; i < n; i++) {
+    for (int64_t k = 0; k < n; k++) {
+        const int64_t i = job->i_first + k;
         const double rig = job->rig + i * job->del;                    /* :14 */
         cor_traj_record r;
         const int st = o_trace_one(job, params, models, step_limit, tu_angle, particle_mass, rig, &r);
@@ -389,8 +400,8 @@ int orc_scan_job(const cor_scan_job *job, const cor_model_params *params, cor_mo
         }
         steps += r.steps;
         trials += r.trials;
-        if (status) status[i] = (uint8_t)st;
-        if (records) records[i] = r;
+        if (status) status[k] = (uint8_t)st;
+        if (records) records[k] = r;
     }
     double rmx = fmax(rmx1, rmx2);                                     /* :156-159 */
     const double zan = nza - (rmi - job->rig) / job->del;

@@ -9,7 +9,7 @@ and driven two ways:
     giving the printed rows and the CUTOFF line of whole rigidity scans.
 
 Run here (where the reference tree exists):  python tests/golden/make_golden.py [section ...]
-Sections: setup field scan0 scan_t96 scan_ts05 scan_chaos nudge nudge_extra.  The fixtures are small JSON
+Sections: setup field scan0 scan_t96 scan_ts05 scan_chaos field_cli trajectory_cli nudge nudge_extra.  The fixtures are small JSON
 files; nothing on the GPU side reads the reference.
 """
 from __future__ import annotations
@@ -269,6 +269,53 @@ def make_scan_chaos(n_sites: int = 12) -> dict:
             "step_limit": 2000, "sites": recs}
 
 
+def make_field_cli() -> dict:
+    """`cor -m field` of the reference on three grids (src/field.c:6-53): its
+    text output, header included, for the drop-in CLI to reproduce."""
+    cases = [
+        ("igrf14", ["-i", "igrf14"], "1.0 -90 0\n10 10 90 360\n2020 1 1 1 0 0 0\n"),
+        ("igrf14+t96", ["-i", "igrf14", "-e", "t96"], "3.0 -75 0\n15 20 75 360\n2020 6 21 173 12 0 0\n-20 2 0 -1\n"),
+        ("igrf14+ts05", ["-i", "igrf14", "-e", "ts05"],
+         "5.0 -60 10\n20 30 60 350\n2020 6 21 173 12 0 0\n-20 2 0 -1\n1 1 1 1 1 1\n"),
+    ]
+    out = {}
+    for name, args, text in cases:
+        out[name] = {"args": args, "infile": text,
+                     "output": pyoracle.run_ref_cor(text, ["-m", "field", *args], parallel=False)}
+    return out
+
+
+def make_trajectory_cli() -> dict:
+    """`cor -m trajectory -o NAME` of the reference (src/trajectory.c:163-273):
+    line count, SHA-256 and the first and last lines of its tragsm_ and
+    trasph_ files for three single-rigidity INFILEs."""
+    import hashlib
+    import subprocess
+    import tempfile
+    cases = [
+        ("igrf14_allowed", ["-i", "igrf14"], infile(50.0, 15.0, 50.0, 15.0, 10.0, 10.0, 0.05, [2020, 1, 1, 1, 0, 0, 0])),
+        ("igrf14_forbidden", ["-i", "igrf14"], infile(0.0, 100.0, 0.0, 100.0, 3.0, 3.0, 0.05, [2020, 1, 1, 1, 0, 0, 0])),
+        ("igrf14+t96", ["-i", "igrf14", "-e", "t96"],
+         infile(45.0, 30.0, 45.0, 30.0, 4.0, 4.0, 0.01, [2020, 6, 21, 173, 12, 0, 0], ext_lines=["-20 2 0 -1"])),
+    ]
+    out = {}
+    for name, args, text in cases:
+        with tempfile.TemporaryDirectory() as td:
+            f = os.path.join(td, "t.in")
+            with open(f, "w") as fh:
+                fh.write(text)
+            subprocess.run([os.path.join(pyoracle.REF_DIR, "cor"), "-m", "trajectory", "-o", "out.txt", *args, f],
+                           cwd=td, check=True, capture_output=True)
+            rec = {"args": args, "infile": text}
+            for pre in ("tragsm_", "trasph_"):
+                body = open(os.path.join(td, pre + "out.txt")).read()
+                lines = body.splitlines()
+                rec[pre] = {"lines": len(lines), "sha256": hashlib.sha256(body.encode()).hexdigest(),
+                            "head": lines[:40], "tail": lines[-10:]}
+            out[name] = rec
+    return out
+
+
 # ---- the reference's own sensitivity to a one-ulp libm change ------------------
 def _scan_agreement(g, res):
     """Flag agreement and sites within one step of a scan result vs a golden set."""
@@ -391,6 +438,8 @@ def main(sections):
         "scan_t96": ("scan_t96.json", lambda: make_scan_ext("t96")),
         "scan_ts05": ("scan_ts05.json", lambda: make_scan_ext("ts05")),
         "scan_chaos": ("scan_chaos.json", make_scan_chaos),
+        "field_cli": ("field_cli.json", make_field_cli),
+        "trajectory_cli": ("trajectory_cli.json", make_trajectory_cli),
         "nudge": ("nudge_sensitivity.json", make_nudge),
         "nudge_extra": ("nudge_sensitivity.json", make_nudge_extra),
     }

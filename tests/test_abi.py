@@ -33,7 +33,7 @@ def test_library_exports_every_declared_function():
 
 
 def test_abi_version():
-    assert ct.load().cor_abi_version() == 1
+    assert ct.load().cor_abi_version() == 2
 
 
 def test_batch_count_matches_reference_grid():
@@ -66,3 +66,21 @@ def test_context_without_gpu_reports_nodev():
     lib = ct.load()
     h = C.c_void_p()
     assert lib.cor_ctx_create(0, C.byref(h)) == -5
+
+
+def test_batch_count_windows():
+    # a window of the 0.01 GV grid: indices 100..199 (rigidities 1.01..2.00 GV)
+    full = ct.make_job(0, 0, rig=0.01, rk=20.0, dele=0.01)
+    win = ct.make_job(0, 0, rig=0.01, rk=20.0, dele=0.01, i_first=100, i_last=199)
+    tail = ct.make_job(0, 0, rig=0.01, rk=20.0, dele=0.01, i_first=1990)
+    n, off = ct.batch_offsets(np.concatenate([full, win, tail]))
+    assert off.tolist() == [0, 2000, 2100, 2110] and n == 2110
+    for bad in (dict(i_first=2000), dict(i_first=1990, i_last=2000), dict(i_first=-1)):
+        with pytest.raises(ct.CorError):
+            ct.batch_offsets(ct.make_job(0, 0, rig=0.01, rk=20.0, dele=0.01, **bad))
+
+
+def test_regroup_and_steps_reject_null_context():
+    lib = ct.load()
+    assert lib.cor_ctx_set_regroup(None, 16, 48, 256) == -1
+    assert lib.cor_trace_steps(None, None, None, None, 0) == -1

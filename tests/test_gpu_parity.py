@@ -368,3 +368,48 @@ def test_scan_chaos_matches_reference(ctx):
     jobs = config0_jobs(g["sites"], g["rig"], g["rk"], g["del"])
     res = ctx.trace_batch(jobs, p, models=models, step_limit=g["step_limit"])
     _scan_vs_reference("scan_chaos.json", res, "CHAOS scan")
+
+
+def test_scan_window_equals_whole_scan(ctx):
+    """Windows of the grid (i_first/i_count) that hold the penumbra give the
+    whole scan's P(S), P(C), P(M) bit for bit and the same classes; the
+    learned window relies on this (IGRF-14 + T96, 40 sites)."""
+    models = ct.model_set(ct.INTERNAL_SH, ct.EXTERNAL_T96)
+    g, p, jobs = _scan_golden("scan_t96.json", models)
+    jobs = jobs[:40]
+    full = ctx.trace_batch(jobs, p, models=models)
+    win = jobs.copy()
+    for j in range(len(jobs)):
+        st = full.status[full.offsets[j]:full.offsets[j + 1]]
+        allowed = np.nonzero(st == ct.TRAJ_ALLOWED)[0]
+        forbidden = np.nonzero(st != ct.TRAJ_ALLOWED)[0]
+        lo = max(0, int(allowed.min()) - 2) if len(allowed) else 0
+        hi = min(len(st) - 1, int(forbidden.max()) + 2) if len(forbidden) else len(st) - 1
+        win[j]["i_first"], win[j]["i_count"] = lo, hi - lo + 1
+    part = ctx.trace_batch(win, p, models=models)
+    assert part.counters["trajectories"] < full.counters["trajectories"]
+    for j in range(len(jobs)):
+        for k in ("r_lower", "r_upper", "r_cutoff", "n_forbidden"):
+            assert part.sites[j][k] == full.sites[j][k], (j, k)
+        a = int(full.offsets[j]) + int(win[j]["i_first"])
+        assert np.array_equal(part.status[part.offsets[j]:part.offsets[j + 1]],
+                              full.status[a:a + int(win[j]["i_count"])])
+
+
+def test_results_do_not_depend_on_regrouping(ctx):
+    """The autotuner's knobs move time, not results: never regrouping, and
+    parking at every thinning, give the same sites and records."""
+    models = ct.model_set(ct.INTERNAL_SH, ct.EXTERNAL_T96)
+    g, p, jobs = _scan_golden("scan_t96.json", models)
+    jobs = jobs[:24]
+    out = []
+    for park_below, gens in ((16, 48), (0, 1), (32, 8)):
+        c = ct.Context(0)
+        try:
+            c.set_regroup(park_below, gens, 0)
+            out.append(c.trace_batch(jobs, p, models=models, want_records=True))
+        finally:
+            c.close()
+    for r in out[1:]:
+        assert np.array_equal(r.sites.view(np.uint8), out[0].sites.view(np.uint8))
+        assert np.array_equal(r.records.view(np.uint8), out[0].records.view(np.uint8))

@@ -133,3 +133,33 @@ def test_oracle_calculate_field_crustal_bit_exact():
         want = unhex(case["b"]).reshape(-1, 3)
         got = pyoracle.calculate_field(pts, p, models=ct.model_set(ct.INTERNAL_SH, ext, ct.CRUSTAL_CHAOS))
         assert np.array_equal(got.view(np.uint64), want.view(np.uint64)), key
+
+
+def test_oracle_window_equals_whole_scan():
+    """A window of the grid that holds the penumbra gives the whole scan's
+    P(S), P(C), P(M) bit for bit and the same classes on its indices; a
+    window that cuts into the penumbra does not (cor_trace.h, i_first/i_count)."""
+    g = golden("scan_config0.json")
+    sites = [s for s in g["sites"] if float(s["cutoff"][0]) < float(s["cutoff"][1]) - 0.2][:3]
+    p = ct.internal_setup(g["model"], g["time"])
+    jobs = config0_jobs(sites, g["rig"], g["rk"], g["del"])
+    full = pyoracle.scan_batch(jobs, p, threads=8)
+    win = jobs.copy()
+    for j in range(len(sites)):
+        st = full.status[full.offsets[j]:full.offsets[j + 1]]
+        allowed = np.nonzero(st == ct.TRAJ_ALLOWED)[0]
+        forbidden = np.nonzero(st != ct.TRAJ_ALLOWED)[0]
+        lo, hi = int(allowed.min()) - 3, int(forbidden.max()) + 3
+        win[j]["i_first"], win[j]["i_count"] = lo, hi - lo + 1
+    part = pyoracle.scan_batch(win, p, threads=8)
+    for j in range(len(sites)):
+        for k in ("r_lower", "r_upper", "r_cutoff", "n_forbidden"):
+            assert part.sites[j][k] == full.sites[j][k], (j, k)
+        a = int(full.offsets[j]) + int(win[j]["i_first"])
+        assert np.array_equal(part.status[part.offsets[j]:part.offsets[j + 1]],
+                              full.status[a:a + int(win[j]["i_count"])])
+    # cutting the penumbra from above changes P(C)
+    cut = win.copy()
+    cut["i_count"] = cut["i_count"] - 6
+    bad = pyoracle.scan_batch(cut, p, threads=8)
+    assert any(bad.sites[j]["r_upper"] != full.sites[j]["r_upper"] for j in range(len(sites)))

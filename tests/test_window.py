@@ -1,0 +1,110 @@
+"""The learned window's network: the numpy restatement (CPU) and the device
+kernels against it (GPU): forward pass, gradient, and that training on the
+tensor cores fits a smooth function."""
+from __future__ import annotations
+
+import numpy as np
+import pytest
+
+import mlp_oracle
+import window
+
+
+def test_oracle_backprop_matches_finite_differences():
+    assert mlp_oracle.check_backprop(seed=3) < 1e-6
+
+
+def test_bf16_rounding_is_nearest_even():
+    x = np.array([1.0, 1.0 + 2 ** -8, 1.0 + 3 * 2 ** -8, -2.5, 3.0e-5], np.float32)
+    got = mlp_oracle.bf16(x)
+    assert got[0] == 1.0 and got[1] == 1.0 and got[2] == 1.0 + 2 ** -6
+    assert got[3] == -2.5
+    assert abs(got[4] - 3.0e-5) / 3.0e-5 < 2 ** -8
+
+
+def _problem(seed, n):
+    rng = np.random.default_rng(seed)
+    x = rng.normal(0, 1, (n, window.N_IN)).astype(np.float32)
+    t = np.stack([np.sin(x[:, 0]) + 0.5 * x[:, 1] * x[:, 2], np.cos(x[:, 3] - x[:, 4])], 1).astype(np.float32)
+    return x, t
+
+
+def _rel(a, b):
+    return float(np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-30))
+
+
+@pytest.fixture
+def net():
+    torch = pytest.importorskip("torch")
+    if not torch.cuda.is_available():
+        pytest.skip("no GPU")
+    nw = window.Network(0, max_batch=1024)
+    yield nw
+    nw.close()
+
+
+@pytest.mark.gpu
+def test_forward_matches_oracle(net):
+    import torch
+    p = window.init_params(11)
+    net.set_params(p)
+    x, _ = _problem(1, 300)                  # 300 rows: the last 128-row tile is partly padding
+    y = net.forward(torch.from_numpy(x).cuda()).cpu().numpy()
+    want, _ = mlp_oracle.forward(p, x.astype(np.float64))
+    err = _rel(y, want)
+    print(f"forward: relative error {err:.2e}")
+    assert err < 1e-2
+
+
+@pytest.mark.gpu
+def test_gradient_matches_oracle(net):
+    import torch
+    p = window.init_params(12)
+    net.set_params(p)
+    x, t = _problem(2, 300)
+    loss, g = net.gradient(torch.from_numpy(x).cuda(), torch.from_numpy(t).cuda())
+    want_loss, want = mlp_oracle.gradient(p, x.astype(np.float64), t.astype(np.float64))
+    assert abs(loss - want_loss) / want_loss < 1e-3
+    o = 0
+    for k, shp in enumerate(mlp_oracle.SHAPES):
+        n = int(np.prod(shp))
+        err = _rel(g[o:o + n], want[o:o + n])
+        print(f"gradient tensor {k} {shp}: relative error {err:.2e}")
+        assert err < 2e-2, k
+        o += n
+    assert o == window.N_PARAMS
+
+
+@pytest.mark.gpu
+def test_training_fits_a_smooth_function(net):
+    import torch
+    net.set_params(window.init_params(13))
+    x, t = _problem(3, 1024)
+    xd, td = torch.from_numpy(x).cuda(), torch.from_numpy(t).cuda()
+    first = net.train_step(xd, td, lr=1e-3)
+    for _ in range(300):
+        last = net.train_step(xd, td, lr=1e-3)
+    print(f"training: loss {first:.4f} -> {last:.4f}")
+    assert last < 0.1 * first
+
+
+def test_features_are_the_networks_inputs():
+    f = window.features(50.0, 15.0, 30.0, 45.0, 2020.47, [2.0, -20.0, 0.0, -1.0], 25.8)
+    assert f.shape == (window.N_IN,) == (19,)
+    assert abs(f[0] - np.sin(np.radians(50.0))) < 1e-15 and f[4] == 30.0 and f[7] == 2020.47
+    # vertical incidence points the backtraced velocity along the local vertical
+    assert window.arrival_direction(50.0, 15.0, 0.0, 0.0) == (50.0, 15.0)
+    la, lo = window.arrival_direction(50.0, 15.0, 30.0, 0.0)
+    assert abs(la - 80.0) < 1e-9 and abs(lo - 15.0) < 1e-9
+
+
+def test_window_indices_and_edge_rule():
+    i_lo, i_hi = window.window_indices(np.log([5.0]), np.log([4.0]), 0.1, 0.1, k=3.0)
+    lo, hi = 4.0 * np.exp(-0.3), 5.0 * np.exp(0.3)
+    assert i_lo[0] == int(np.floor((lo - 0.01) / 0.01)) and i_hi[0] == int(np.ceil((hi - 0.01) / 0.01))
+    import cortrace as ct
+    F, A = 2, ct.TRAJ_ALLOWED
+    assert not window.edge_hit(np.array([F, F, A, F, A, A]), 100, 105)    # boundaries inside
+    assert window.edge_hit(np.array([A, F, A, A]), 100, 103)              # allowed at the bottom edge
+    assert window.edge_hit(np.array([F, A, A, F]), 100, 103)              # forbidden at the top edge
+    assert not window.edge_hit(np.array([A, A]), 0, 1)                    # the grid's own first index
