@@ -40,6 +40,10 @@ PARMOD = [2.0, -20.0, 0.0, -1.0]
 N_RIG = 2000
 METRIC = "site cutoffs/s"
 WINDOW_FILE = os.path.join(ROOT, "cor-model_gb300", "window_t96.npz")
+# DRAM bytes (read + write) per trajectory of the scan kernel, from the ncu
+# capture of the profiling case (profiles/trace_kernel_igrf_t96_profile_case.md:
+# 1.61 MB + 0.19 MB over the 64,000 trajectories of its generation-0 launch)
+DRAM_BYTES_PER_TRAJ = (1.613312e6 + 0.185856e6) / 64000
 TUNING_FILE = os.path.join(ROOT, "cor-model_gb300", "tuning.json")
 
 
@@ -48,8 +52,10 @@ def tuning() -> dict:
     if os.path.exists(TUNING_FILE):
         with open(TUNING_FILE) as f:
             t = json.load(f)
-        return {k: t[k] for k in ("inflight", "park_below", "max_generations", "min_park")} | {"source": "autotune"}
-    return {"inflight": 3, "park_below": 16, "max_generations": 48, "min_park": 256, "source": "defaults"}
+        out = {k: t[k] for k in ("inflight", "park_below", "max_generations", "min_park")}
+        return out | {"rigidity_major": t.get("rigidity_major", 1), "source": "autotune"}
+    return {"inflight": 3, "park_below": 16, "max_generations": 48, "min_park": 256, "rigidity_major": 1,
+            "source": "defaults"}
 
 
 def grid_sites() -> list[tuple[float, float]]:
@@ -180,8 +186,11 @@ class Lane:
         import torch
         self.torch = torch
         self.ctx = ct.Context(dev)
+        self.flags = ct.FLAG_UNIFORM_GRID
         if tune:
             self.ctx.set_regroup(tune["park_below"], tune["max_generations"], tune["min_park"])
+            self.ctx.set_queue_order(bool(tune["rigidity_major"]))
+            self.flags = ct.FLAG_UNIFORM_GRID if tune["rigidity_major"] else 0
         self.stream = torch.cuda.Stream(device=dev)
         rc = self.ctx.lib.cor_upload_params(self.ctx.h, p.ctypes.data, len(p))
         if rc != 0:
@@ -197,7 +206,7 @@ class Lane:
         rc = lib.cor_trace_batch_device(
             self.ctx.h, bf["jobs"].data_ptr(), bf["trig"].data_ptr(), bf["n_jobs"], bf["off"].data_ptr(), bf["n"],
             models(), step_limit, 0.01, ct.DEF_HM0_P, bf["sites"].data_ptr(), bf["status"].data_ptr(), None,
-            self.cnt.data_ptr(), ct.FLAG_UNIFORM_GRID, C.c_void_p(self.stream.cuda_stream))
+            self.cnt.data_ptr(), self.flags, C.c_void_p(self.stream.cuda_stream))
         if rc != 0:
             raise ct.CorError(rc, self.ctx.error())
         e1.record(self.stream)
@@ -408,7 +417,10 @@ def run_ours(args, rank: int, world: int, dist) -> dict | None:
         "batch_kernel_ms": launch_ms,
         "roofline": {"bound": "fp64", "achieved": achieved, "peak": peak.value / 1e12, "unit": "TFLOP/s",
                      "frac": achieved / (peak.value / 1e12) if peak.value else None,
-                     "traffic": None, "work_model": wm.get("source"),
+                     "traffic": DRAM_BYTES_PER_TRAJ * traj_done / max(1, args.steps * world),
+                     "traffic_unit": "bytes per step (one batch), scaled by trajectories from the ncu capture of "
+                                     "the profiling case",
+                     "work_model": wm.get("source"),
                      "flops_per_step": wm["flops_per_step"],
                      "peak_source": "DFMA microbenchmark in libcortrace (cor_probe_fp64_peak), FMA = 2 flops"},
         "e2e": {"value": sites_done / e2e_s, "unit": METRIC,

@@ -10,7 +10,9 @@ fastest to FILE (JSON), which bench.py and serve.py read:
     generation, and max_generations (1 = never regroup);
   * inflight: how many batches run at once, each on its own context and
     stream, so that one batch's tail of long trajectories overlaps the next
-    batch's bulk.
+    batch's bulk;
+  * the work-queue order (cor_ctx_set_queue_order): lowest rigidities of all
+    scans first, or consecutive rigidities of one scan to neighbouring lanes.
 Results do not depend on any setting (checked: every candidate's P(S), P(C),
 P(M) must equal the first's); only the time does.
 """
@@ -41,7 +43,8 @@ def load_tuning(path: str = DEFAULT_OUT) -> dict | None:
         return None
     with open(path) as f:
         t = json.load(f)
-    return {k: t[k] for k in ("inflight", "park_below", "max_generations", "min_park")}
+    return {k: t.get(k, 1) if k == "rigidity_major" else t[k]
+            for k in ("inflight", "park_below", "max_generations", "min_park", "rigidity_major")}
 
 
 def sample_jobs(n_sites: int, parts: int):
@@ -81,13 +84,17 @@ def main():
             if inflight > 1 and (park_below, gens) not in ((16, 48), (8, 48), (24, 48)):
                 continue
             candidates.append({"inflight": inflight, "park_below": park_below, "max_generations": gens,
-                               "min_park": 256})
+                               "min_park": 256, "rigidity_major": 1})
+    for inflight in (1, 3):
+        candidates.append({"inflight": inflight, "park_below": 16, "max_generations": 48, "min_park": 256,
+                           "rigidity_major": 0})
     ctxs = [ct.Context(0) for _ in range(4)]
     ref = None
     results = []
     for c in candidates:
         for x in ctxs:
             x.set_regroup(c["park_below"], c["max_generations"], c["min_park"])
+            x.set_queue_order(bool(c["rigidity_major"]))
         parts = sample_jobs(args.sites, c["inflight"])
         run(ctxs[:c["inflight"]], [pp[:2] for pp in parts], p, models)      # warm the kernels
         dt, out = run(ctxs[:c["inflight"]], parts, p, models)
@@ -105,11 +112,12 @@ def main():
     best = min(ok, key=lambda r: r["seconds"])
     out = {"inflight": best["inflight"], "park_below": best["park_below"],
            "max_generations": best["max_generations"], "min_park": best["min_park"],
+           "rigidity_major": best["rigidity_major"],
            "sample": f"{args.sites} sites of the 5-deg grid x 2000 rigidities, IGRF-14 + T96",
            "measurements": results}
     with open(args.out, "w") as f:
         json.dump(out, f, indent=1)
-    print(json.dumps({k: out[k] for k in ("inflight", "park_below", "max_generations", "min_park")}))
+    print(json.dumps({k: out[k] for k in ("inflight", "park_below", "max_generations", "min_park", "rigidity_major")}))
 
 
 if __name__ == "__main__":

@@ -83,7 +83,7 @@ EXPORTS = [
     "cor_ctx_create", "cor_ctx_destroy", "cor_last_error_string", "cor_abi_version", "cor_batch_count",
     "cor_prepare_trig", "cor_trace_batch", "cor_trace_batch_device", "cor_upload_params", "cor_field_batch",
     "cor_internal_setup", "cor_gsm_setup", "cor_probe_fp64_peak", "cor_upload_crustal",
-    "cor_trace_batch_device_noalloc", "cor_ctx_set_regroup", "cor_trace_steps",
+    "cor_trace_batch_device_noalloc", "cor_ctx_set_regroup", "cor_trace_steps", "cor_ctx_set_queue_order",
 ]
 NOALLOC_MAX_TRAJ = 1048576  # COR_NOALLOC_MAX_TRAJ
 
@@ -112,6 +112,7 @@ def load(path: str = LIB_PATH) -> C.CDLL:
     lib.cor_upload_params.argtypes = [vp, vp, i32]
     lib.cor_upload_crustal.argtypes = [vp, vp, vp, i32]
     lib.cor_ctx_set_regroup.argtypes = [vp, i32, i32, i64]
+    lib.cor_ctx_set_queue_order.argtypes = [vp, i32]
     lib.cor_trace_steps.argtypes = [vp, C.POINTER(BatchReq), C.POINTER(BatchResult), vp, C.c_uint32]
     lib.cor_trace_batch_device_noalloc.argtypes = [vp, vp, vp, i32, vp, u64, ModelSet, u64, dbl, dbl,
                                                    vp, vp, vp, C.c_uint32, vp]
@@ -233,6 +234,10 @@ class Context:
     def set_regroup(self, park_below: int = 16, max_generations: int = 48, min_park: int = 256) -> None:
         """cor_ctx_set_regroup: the scan kernel's regrouping knobs."""
         self._check(self.lib.cor_ctx_set_regroup(self.h, park_below, max_generations, min_park), "cor_ctx_set_regroup")
+
+    def set_queue_order(self, rigidity_major: bool = True) -> None:
+        """cor_ctx_set_queue_order: lowest rigidities first (True) or scan by scan."""
+        self._check(self.lib.cor_ctx_set_queue_order(self.h, 1 if rigidity_major else 0), "cor_ctx_set_queue_order")
 
     def upload_crustal(self, g: np.ndarray, h: np.ndarray, nmax: int) -> None:
         """cor_upload_crustal: packed lower-triangle G, H (index n(n+1)/2 + m)."""

@@ -1,10 +1,14 @@
 // cor_device.cuh -- FP64 device building blocks of the rigidity scan.
 //
-// Every function here keeps the reference's expression order, and the
-// translation units that include it are compiled with --fmad=false (the
+// Every function here keeps the reference's expression order.  The units of
+// the IGRF-only model set and the C ABI are compiled with --fmad=false (the
 // reference is built with -ffp-contract=off, CMakeLists.txt:17), so each
-// result is the correctly rounded IEEE value of the same expression tree:
-// bit-identical to the reference wherever only + - * / sqrt are involved.
+// result there is the correctly rounded IEEE value of the same expression
+// tree: bit-identical to the reference wherever only + - * / sqrt are
+// involved.  The units with an external or crustal model (whose C-library
+// functions differ from CUDA's anyway) are compiled with FMA contraction;
+// div_c/div_r spell out their roundings (__dmul_rn, __fma_rn), so they stay
+// exact there too.
 #pragma once
 
 #include <stdint.h>

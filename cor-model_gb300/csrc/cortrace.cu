@@ -48,6 +48,7 @@ struct cor_ctx {
     double* crust = nullptr;              // crustal tables: g, h, k1, k2 (packed), kd
     int crust_nmax = 0;
     int crust_n_first = 0;
+    int rig_major = 1;                    // queue order for uniform grids (cor_ctx_set_queue_order)
     int park_below = 16;                  // regroup settings (cor_ctx_set_regroup)
     int max_generations = 48;
     uint64_t min_park = 256;
@@ -627,6 +628,13 @@ extern "C" int cor_upload_crustal(cor_ctx* ctx, const double* g, const double* h
     return upload_crustal(ctx, g, h, nmax);
 }
 
+extern "C" int cor_ctx_set_queue_order(cor_ctx* ctx, int32_t rigidity_major) {
+    if (!ctx) return COR_ERR_INVALID;
+    if (rigidity_major != 0 && rigidity_major != 1) return fail(ctx, COR_ERR_INVALID, "queue order must be 0 or 1");
+    ctx->rig_major = rigidity_major;
+    return COR_OK;
+}
+
 extern "C" int cor_ctx_set_regroup(cor_ctx* ctx, int32_t park_below, int32_t max_generations, int64_t min_park) {
     if (!ctx) return COR_ERR_INVALID;
     if (park_below < 0 || park_below > 32 || max_generations < 1 || max_generations > 1024 || min_park < 0)
@@ -766,7 +774,7 @@ extern "C" int cor_trace_batch(cor_ctx* ctx, const cor_batch_req* req, cor_batch
                                     req->tu_angle, req->particle_mass,
                                     (cor_site_result*)ctx->sites.p, (uint8_t*)ctx->status.p,
                                     out->records ? (cor_traj_record*)ctx->records.p : nullptr, ctx->counters,
-                                    uniform ? COR_FLAG_UNIFORM_GRID : 0u, s);
+                                    (uniform && ctx->rig_major) ? COR_FLAG_UNIFORM_GRID : 0u, s);
         if (rc != COR_OK) break;
         TRY(cudaMemcpyAsync(out->sites, ctx->sites.p, sizeof(cor_site_result) * (size_t)nj, cudaMemcpyDeviceToHost, s));
         if (out->status) TRY(cudaMemcpyAsync(out->status, ctx->status.p, (size_t)n_traj, cudaMemcpyDeviceToHost, s));

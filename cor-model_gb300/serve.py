@@ -136,6 +136,7 @@ class Server:
             if tune:
                 for c in self.ctxs:
                     c.set_regroup(tune["park_below"], tune["max_generations"], tune["min_park"])
+                    c.set_queue_order(bool(tune["rigidity_major"]))
             self.executor = self._gpu_execute
         else:
             self.ctxs = [None] * slots

@@ -11,8 +11,11 @@
 3. The network (include/cor_window.h) is trained on the GPU with its own
    tensor-core kernels (AdamW, minibatches), on standardised features and
    targets.
-4. The residual spread on the held-out samples gives sigma_U, sigma_L, the
-   half-widths (in log R) the windows are built from.
+4. The residual spread on the held-out samples, per band of predicted R_L
+   (8 equal-count bands: the spread in log R is wide for low cutoffs, where a
+   wide relative window is only a few grid points, and narrow above 4 GV),
+   gives the sigma_U, sigma_L the windows are built from (prediction +- 3
+   sigma).
 The result (parameters, standardisation, sigmas, provenance) goes to --out.
 """
 from __future__ import annotations
@@ -124,8 +127,8 @@ def main():
     ap.add_argument("--epochs", type=int, default=200)
     ap.add_argument("--batch", type=int, default=512)
     ap.add_argument("--out", default=os.path.join(HERE, "window_t96.npz"))
-    ap.add_argument("--labels", default=None, help="labelled set: loaded when the file exists, else traced "
-                    "and saved there")
+    ap.add_argument("--labels", default=os.path.join(HERE, "window_t96_labels.npz"),
+                    help="labelled set: loaded when the file exists, else traced and saved there")
     args = ap.parse_args()
     rng = np.random.default_rng(args.seed)
     models = ct.model_set(ct.INTERNAL_SH, ct.EXTERNAL_T96)
@@ -156,15 +159,25 @@ def main():
     yn = (y - ym) / ys
     yvn = (np.stack([vru, vrl], 1) - ym) / ys
     params, pv, steps = train(x, yn, xv, yvn, args.seed, args.epochs, batch=args.batch)
-    resid = (pv * ys + ym) - np.stack([vru, vrl], 1)
+    pred = pv * ys + ym
+    truth = np.stack([vru, vrl], 1)
+    resid = pred - truth
     sigma = resid.std(0)
-    print(f"held-out residual sigma (log R): U {sigma[0]:.4f}, L {sigma[1]:.4f}; "
-          f"|resid| > 3 sigma: {np.mean(np.abs(resid) > 3 * sigma, 0)}", flush=True)
+    edges, band_sigma = window.band_sigmas(pred, resid)
+    b = window.band_of(pred[:, 1], edges)
+    lo = np.exp(pred[:, 1] - 3 * band_sigma[b, 1])
+    hi = np.exp(pred[:, 0] + 3 * band_sigma[b, 0])
+    miss = np.mean((lo > np.exp(truth[:, 1])) | (hi < np.exp(truth[:, 0])))
+    print(f"held-out residual sigma (log R): U {sigma[0]:.4f}, L {sigma[1]:.4f}; per band of predicted R_L "
+          f"(edges {np.exp(edges).round(2).tolist()} GV): U {band_sigma[:, 0].round(3).tolist()}, "
+          f"L {band_sigma[:, 1].round(3).tolist()}; held-out windows missing the penumbra: {miss:.4f}", flush=True)
     info = {"samples": args.samples, "val": args.val, "seed": args.seed, "epochs": args.epochs, "steps": steps,
             "batch": args.batch, "sigma_log_ru": float(sigma[0]), "sigma_log_rl": float(sigma[1]),
+            "band_sigma": band_sigma.round(4).tolist(), "heldout_window_miss": float(miss),
             "model": "igrf14+t96", "label_trajectories": n1 + n2, "label_seconds": t_label,
             "total_seconds": time.time() - t0}
     np.savez(args.out, params=params, feat_mean=fm, feat_std=fs, y_mean=ym, y_std=ys, sigma=sigma,
+             band_edges=edges, band_sigma=band_sigma,
              val_features=va["features"], val_targets=np.stack([vru, vrl], 1), info=json.dumps(info))
     print(json.dumps(info), flush=True)
 

@@ -40,16 +40,16 @@ def _bind(lib: C.CDLL) -> C.CDLL:
 
 
 def init_params(seed: int) -> np.ndarray:
-    """Seeded initial parameters: uniform +-sqrt(6/fan_in) weights (SiLU
-    layers), +-sqrt(3/fan_in) for the linear output layer, zero biases."""
+    """Seeded initial parameters: weights and biases uniform in
+    +-1/sqrt(fan_in) of their layer."""
     rng = np.random.default_rng(seed)
     out = []
-    for k, shp in enumerate(SHAPES):
-        if len(shp) == 1:
-            out.append(np.zeros(shp, np.float32))
-        else:
-            lim = math.sqrt((3.0 if k == len(SHAPES) - 2 else 6.0) / shp[1])
-            out.append(rng.uniform(-lim, lim, shp).astype(np.float32))
+    fan_in = None
+    for shp in SHAPES:
+        if len(shp) == 2:
+            fan_in = shp[1]
+        lim = 1.0 / math.sqrt(fan_in)
+        out.append(rng.uniform(-lim, lim, shp).astype(np.float32))
     return np.concatenate([a.ravel() for a in out])
 
 
@@ -219,6 +219,21 @@ def edge_hit(status_row: np.ndarray, i_lo: int, i_hi: int, n: int = GRID_N) -> b
     return False
 
 
+def band_of(log_rl: np.ndarray, edges: np.ndarray) -> np.ndarray:
+    """Band index of predicted log R_L values for the inner band edges."""
+    return np.searchsorted(np.asarray(edges), np.asarray(log_rl), side="right")
+
+
+def band_sigmas(pred: np.ndarray, resid: np.ndarray, n_bands: int = 8):
+    """(inner edges, sigma per band): equal-count bands of predicted log R_L
+    and the standard deviation of the held-out residuals (log R_U, log R_L)
+    in each."""
+    edges = np.quantile(pred[:, 1], np.linspace(0, 1, n_bands + 1))[1:-1]
+    b = band_of(pred[:, 1], edges)
+    sig = np.array([resid[b == k].std(0) if np.sum(b == k) > 1 else resid.std(0) for k in range(n_bands)])
+    return edges, sig
+
+
 def window_jobs(jobs: np.ndarray, i_lo: np.ndarray, i_hi: np.ndarray) -> np.ndarray:
     """The jobs restricted to grid windows [i_lo, i_hi] (inclusive)."""
     w = np.array(jobs, copy=True)
@@ -262,6 +277,10 @@ class WindowModel:
         self.feat_mean, self.feat_std = d["feat_mean"], d["feat_std"]
         self.y_mean, self.y_std = d["y_mean"], d["y_std"]
         self.sigma = d["sigma"]
+        # held-out spread per band of predicted log R_L (inner edges; one
+        # sigma pair per band); the global pair when absent
+        self.band_edges = d["band_edges"] if "band_edges" in d else np.zeros(0)
+        self.band_sigma = d["band_sigma"] if "band_sigma" in d else self.sigma[None, :]
         self.info = str(d["info"])
         self.net = Network(device, max_batch=max_batch)
         self.net.set_params(self.params)
@@ -284,8 +303,11 @@ class WindowModel:
         return y * self.y_std + self.y_mean
 
     def windows(self, feats: np.ndarray, k: float = 3.0):
+        """Grid windows: the prediction +- k sigma, sigma of the prediction's
+        band of log R_L."""
         y = self.predict(feats)
-        return window_indices(y[:, 0], y[:, 1], self.sigma[0], self.sigma[1], k=k)
+        b = band_of(y[:, 1], self.band_edges)
+        return window_indices(y[:, 0], y[:, 1], self.band_sigma[b, 0], self.band_sigma[b, 1], k=k)
 
     def close(self):
         self.net.close()

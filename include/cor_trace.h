@@ -214,6 +214,15 @@ int cor_upload_params(cor_ctx *ctx, const cor_model_params *params, int32_t n_pa
  * do not depend on these settings, only the time does. */
 int cor_ctx_set_regroup(cor_ctx *ctx, int32_t park_below, int32_t max_generations, int64_t min_park);
 
+/* Work-queue order of cor_trace_batch on this context when every job has the
+ * same number of rigidities (no counterpart in the reference; an autotuner's
+ * knob): 1 (default) hands out the lowest rigidity of every scan first
+ * (longest trajectories first); 0 hands consecutive rigidities of one scan
+ * to neighbouring lanes, whose paths start out alike.  The device path takes
+ * the order from its flags (COR_FLAG_UNIFORM_GRID).  Results do not depend
+ * on it. */
+int cor_ctx_set_queue_order(cor_ctx *ctx, int32_t rigidity_major);
+
 /* Replaces the crustal model's coefficient table on this context: G and H as
  * packed lower triangles (index n*(n+1)/2 + m, degrees n = 0 .. nmax-1), the
  * layout of lib/chaos/coefs/chaos_7_16.h read by chaos_geo

@@ -71,9 +71,11 @@ def test_cli_field_mode(tmp_path, case):
         try:
             va, vb = [float(x) for x in fa], [float(x) for x in fb]
         except ValueError:
-            assert a == b
+            va = vb = None
+        if va is None or len(fb) != 6:
+            assert a == b               # header and blank lines
             continue
-        assert len(va) == len(vb) == 6 and va[:2] == vb[:2]
+        assert len(va) == 6 and va[:2] == vb[:2]
         assert max(abs(x - y) for x, y in zip(va, vb)) <= 0.0100001, (a, b)
 
 
