@@ -213,6 +213,7 @@ class Lane:
         self.stream.synchronize()
         bf["counters"] = self.cnt.cpu().numpy().copy()
         bf["kernel_ms"] = e0.elapsed_time(e1)
+        bf["generations"] = self.ctx.generation_log()
 
 
 def run_batches(slots, bufs, order) -> None:
@@ -415,6 +416,7 @@ def run_ours(args, rank: int, world: int, dist) -> dict | None:
                          "outputs are MB-sized", "parallelism": f"sites split over {world} GPU(s)"},
         "trajectories_per_s": traj_done / dev_s, "steps_per_s": steps_acc / dev_s,
         "batch_kernel_ms": launch_ms,
+        "batch_generations": [[(n, round(ms, 1)) for n, ms in b.get("generations", [])] for b in timed[:1]],
         "roofline": {"bound": "fp64", "achieved": achieved, "peak": peak.value / 1e12, "unit": "TFLOP/s",
                      "frac": achieved / (peak.value / 1e12) if peak.value else None,
                      "traffic": DRAM_BYTES_PER_TRAJ * traj_done / max(1, args.steps * world),

@@ -3,7 +3,9 @@
     python cor-model_gb300/autotune.py [--sites N] [--out FILE]
 
 Times a sample of the IGRF-14 + T96 5-degree-grid workload (every k-th site,
-the full 2,000-rigidity scans) under candidate settings and writes the
+the full 2,000-rigidity scans, cut into interleaved batches that stream
+through the slots as the bench's do, so that both the steady state and the
+tails of long trajectories count) under candidate settings and writes the
 fastest to FILE (JSON), which bench.py and serve.py read:
   * regrouping (cor_ctx_set_regroup): park_below, the live lanes per warp
     under which a block parks its trajectories for the next kernel
@@ -14,7 +16,7 @@ fastest to FILE (JSON), which bench.py and serve.py read:
   * the work-queue order (cor_ctx_set_queue_order): lowest rigidities of all
     scans first, or consecutive rigidities of one scan to neighbouring lanes.
 Results do not depend on any setting (checked: every candidate's P(S), P(C),
-P(M) must equal the first's); only the time does.
+P(M) must equal the first's, bit for bit); only the time does.
 """
 from __future__ import annotations
 
@@ -47,23 +49,34 @@ def load_tuning(path: str = DEFAULT_OUT) -> dict | None:
             for k in ("inflight", "park_below", "max_generations", "min_park", "rigidity_major")}
 
 
-def sample_jobs(n_sites: int, parts: int):
-    grid = [(float(la), float(lo)) for la in range(-90, 91, 5) for lo in range(0, 360, 5)]
-    step = max(1, len(grid) // n_sites)
-    sites = grid[::step][:n_sites]
-    jobs = [np.concatenate([ct.make_job(la, lo, rig=0.01, rk=20.0, dele=0.01) for la, lo in sites[k::parts]])
-            for k in range(parts)]
-    return jobs
+def sample_batches(n_batches: int, stride: int):
+    """Interleaved slices of every stride-th site of the 5-degree grid, as
+    the bench cuts the whole grid into its batches."""
+    grid = [(float(la), float(lo)) for la in range(-90, 91, 5) for lo in range(0, 360, 5)][::stride]
+    return [np.concatenate([ct.make_job(la, lo, rig=0.01, rk=20.0, dele=0.01) for la, lo in grid[b::n_batches]])
+            for b in range(n_batches)]
 
 
-def run(ctxs, parts, p, models):
-    out = [None] * len(parts)
+def run(ctxs, batches, p, models):
+    """Streams the batches through the contexts (each takes the next batch
+    as soon as it is free, as bench.py's slots do); returns (seconds, results
+    in batch order)."""
+    import queue
+    q = queue.Queue()
+    for k in range(len(batches)):
+        q.put(k)
+    out = [None] * len(batches)
 
-    def work(k):
-        out[k] = ctxs[k % len(ctxs)].trace_batch(parts[k], p, models=models, want_status=False)
+    def work(ctx):
+        while True:
+            try:
+                k = q.get_nowait()
+            except queue.Empty:
+                return
+            out[k] = ctx.trace_batch(batches[k], p, models=models, want_status=False)
 
     t0 = time.perf_counter()
-    ths = [threading.Thread(target=work, args=(k,)) for k in range(len(parts))]
+    ths = [threading.Thread(target=work, args=(c,)) for c in ctxs]
     for t in ths:
         t.start()
     for t in ths:
@@ -73,48 +86,40 @@ def run(ctxs, parts, p, models):
 
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("--sites", type=int, default=48)
+    ap.add_argument("--stride", type=int, default=24, help="every stride-th site of the grid (default: 111 sites)")
+    ap.add_argument("--batches", type=int, default=8)
     ap.add_argument("--out", default=DEFAULT_OUT)
     args = ap.parse_args()
     p = ct.internal_setup("igrf14", TIME7, parmod=PARMOD)
     models = ct.model_set(ct.INTERNAL_SH, ct.EXTERNAL_T96)
-    candidates = []
-    for inflight in (1, 2, 3, 4):
-        for park_below, gens in ((16, 48), (8, 48), (24, 48), (16, 1)):
-            if inflight > 1 and (park_below, gens) not in ((16, 48), (8, 48), (24, 48)):
-                continue
-            candidates.append({"inflight": inflight, "park_below": park_below, "max_generations": gens,
-                               "min_park": 256, "rigidity_major": 1})
-    for inflight in (1, 3):
-        candidates.append({"inflight": inflight, "park_below": 16, "max_generations": 48, "min_park": 256,
-                           "rigidity_major": 0})
+    batches = sample_batches(args.batches, args.stride)
+    n_sites = sum(len(b) for b in batches)
+    candidates = [{"inflight": f, "park_below": pb, "max_generations": g, "min_park": 256, "rigidity_major": 1}
+                  for f in (2, 4) for pb in (8, 16) for g in (1, 48)]
+    candidates.append({"inflight": 4, "park_below": 8, "max_generations": 48, "min_park": 256, "rigidity_major": 0})
     ctxs = [ct.Context(0) for _ in range(4)]
+    run(ctxs[:1], [b[:2] for b in batches[:1]], p, models)          # load the kernels
     ref = None
     results = []
     for c in candidates:
         for x in ctxs:
             x.set_regroup(c["park_below"], c["max_generations"], c["min_park"])
             x.set_queue_order(bool(c["rigidity_major"]))
-        parts = sample_jobs(args.sites, c["inflight"])
-        run(ctxs[:c["inflight"]], [pp[:2] for pp in parts], p, models)      # warm the kernels
-        dt, out = run(ctxs[:c["inflight"]], parts, p, models)
-        # results must not depend on the setting
-        sites = np.sort(np.concatenate([o.sites for o in out]),
-                        order=["r_lower", "r_upper", "r_cutoff", "n_forbidden", "n_traj"])
+        dt, out = run(ctxs[:c["inflight"]], batches, p, models)
+        sites = np.concatenate([o.sites for o in out])
         if ref is None:
             ref = sites
-        same = bool(np.array_equal(sites, ref))
-        results.append({**c, "seconds": dt, "site_cutoffs_per_s": args.sites / dt, "same_results": same})
+        same = bool(np.array_equal(sites.view(np.uint8), ref.view(np.uint8)))
+        results.append({**c, "seconds": dt, "site_cutoffs_per_s": n_sites / dt, "same_results": same})
         print(json.dumps(results[-1]), flush=True)
     for x in ctxs:
         x.close()
     ok = [r for r in results if r["same_results"]]
     best = min(ok, key=lambda r: r["seconds"])
-    out = {"inflight": best["inflight"], "park_below": best["park_below"],
-           "max_generations": best["max_generations"], "min_park": best["min_park"],
-           "rigidity_major": best["rigidity_major"],
-           "sample": f"{args.sites} sites of the 5-deg grid x 2000 rigidities, IGRF-14 + T96",
-           "measurements": results}
+    out = {k: best[k] for k in ("inflight", "park_below", "max_generations", "min_park", "rigidity_major")}
+    out.update({"sample": f"{n_sites} sites of the 5-deg grid (every {args.stride}th) x 2000 rigidities in "
+                          f"{args.batches} interleaved batches streamed through the slots, IGRF-14 + T96",
+                "measurements": results})
     with open(args.out, "w") as f:
         json.dump(out, f, indent=1)
     print(json.dumps({k: out[k] for k in ("inflight", "park_below", "max_generations", "min_park", "rigidity_major")}))

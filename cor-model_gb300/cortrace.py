@@ -84,6 +84,7 @@ EXPORTS = [
     "cor_prepare_trig", "cor_trace_batch", "cor_trace_batch_device", "cor_upload_params", "cor_field_batch",
     "cor_internal_setup", "cor_gsm_setup", "cor_probe_fp64_peak", "cor_upload_crustal",
     "cor_trace_batch_device_noalloc", "cor_ctx_set_regroup", "cor_trace_steps", "cor_ctx_set_queue_order",
+    "cor_ctx_generation_log",
 ]
 NOALLOC_MAX_TRAJ = 1048576  # COR_NOALLOC_MAX_TRAJ
 
@@ -113,6 +114,8 @@ def load(path: str = LIB_PATH) -> C.CDLL:
     lib.cor_upload_crustal.argtypes = [vp, vp, vp, i32]
     lib.cor_ctx_set_regroup.argtypes = [vp, i32, i32, i64]
     lib.cor_ctx_set_queue_order.argtypes = [vp, i32]
+    lib.cor_ctx_generation_log.argtypes = [vp, i32, vp, vp]
+    lib.cor_ctx_generation_log.restype = i32
     lib.cor_trace_steps.argtypes = [vp, C.POINTER(BatchReq), C.POINTER(BatchResult), vp, C.c_uint32]
     lib.cor_trace_batch_device_noalloc.argtypes = [vp, vp, vp, i32, vp, u64, ModelSet, u64, dbl, dbl,
                                                    vp, vp, vp, C.c_uint32, vp]
@@ -234,6 +237,13 @@ class Context:
     def set_regroup(self, park_below: int = 16, max_generations: int = 48, min_park: int = 256) -> None:
         """cor_ctx_set_regroup: the scan kernel's regrouping knobs."""
         self._check(self.lib.cor_ctx_set_regroup(self.h, park_below, max_generations, min_park), "cor_ctx_set_regroup")
+
+    def generation_log(self) -> list[tuple[int, float]]:
+        """(live trajectories, wall ms) per kernel generation of the last scan."""
+        live = np.zeros(1024, np.uint64)
+        ms = np.zeros(1024)
+        n = self.lib.cor_ctx_generation_log(self.h, 1024, live.ctypes.data, ms.ctypes.data)
+        return [(int(live[k]), float(ms[k])) for k in range(max(0, n))]
 
     def set_queue_order(self, rigidity_major: bool = True) -> None:
         """cor_ctx_set_queue_order: lowest rigidities first (True) or scan by scan."""

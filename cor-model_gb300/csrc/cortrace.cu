@@ -3,6 +3,7 @@
 #include <cuda_runtime.h>
 
 #include <math.h>
+#include <chrono>
 #include <mutex>
 #include <stdarg.h>
 #include <stdio.h>
@@ -44,6 +45,9 @@ struct cor_ctx {
     unsigned int* park_count_host = nullptr;  // pinned readback of the parked count
     unsigned long long* launches_host = nullptr;  // pinned: kernels launched by the last scan
     int generations = 0;                  // generations of the last scan (diagnostics)
+    uint64_t gen_live[1024];              // live trajectories at each generation's start
+    double gen_ms[1024];                  // host wall time of each generation
+    std::chrono::steady_clock::time_point gen_t0;
     cor_counters* counters = nullptr;
     double* crust = nullptr;              // crustal tables: g, h, k1, k2 (packed), kd
     int crust_nmax = 0;
@@ -495,8 +499,14 @@ static int launch_trace(cor_ctx* ctx, const ModelOps* ops, TraceArgs a, cudaStre
     int cur = 0;
     ctx->generations = 0;
     for (int g = 0; g < ctx->max_generations && live > 0; g++) {
-        uint64_t blocks = (live + kTraceThreads - 1) / kTraceThreads;
-        if (blocks > cap_blocks) blocks = cap_blocks;
+        // as many blocks as there are warps of work, up to the resident
+        // capacity, and that work spread evenly over them
+        const uint64_t warps = (live + 31) / 32;
+        uint64_t blocks = warps < cap_blocks ? warps : cap_blocks;
+        if (blocks < 1) blocks = 1;
+        uint64_t per_block = 32 * ((warps + blocks - 1) / blocks);
+        if (per_block > (uint64_t)kTraceThreads) per_block = kTraceThreads;
+        a.active_threads = (uint32_t)per_block;
         a.restore = g == 0 ? nullptr : (const ParkedLane*)ctx->park[cur ^ 1].p;
         a.n_restore = n_restore;
         a.park = (ParkedLane*)ctx->park[cur].p;
@@ -505,12 +515,16 @@ static int launch_trace(cor_ctx* ctx, const ModelOps* ops, TraceArgs a, cudaStre
         a.park_below = ctx->park_below;
         a.launched_warps = (uint32_t)(blocks * kTraceWarps);
         CUDA_TRY(ctx, cudaMemsetAsync(ctx->gen, 0, sizeof(GenCounters), s));
+        ctx->gen_t0 = std::chrono::steady_clock::now();
+        ctx->gen_live[g] = live;
+        ctx->gen_ms[g] = -1.;
         CUDA_TRY(ctx, ops->launch_generation(a, (unsigned)blocks, s));
         ctx->generations = g + 1;
         if (!a.allow_park) break;
         CUDA_TRY(ctx, cudaMemcpyAsync(ctx->park_count_host, &ctx->gen->park_count, sizeof(unsigned int),
                                       cudaMemcpyDeviceToHost, s));
         CUDA_TRY(ctx, cudaStreamSynchronize(s));
+        ctx->gen_ms[g] = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - ctx->gen_t0).count();
         n_restore = *ctx->park_count_host;
         live = n_restore;
         cur ^= 1;
@@ -538,6 +552,9 @@ static int launch_scan(cor_ctx* ctx, const TraceArgs& a, cor_model_set models, c
     // the pinned staging value is read by the copy before the next call can
     // change it: every call on a context synchronises its stream first
     CUDA_TRY(ctx, cudaStreamSynchronize(s));
+    if (ctx->generations > 0 && ctx->gen_ms[ctx->generations - 1] < 0.)
+        ctx->gen_ms[ctx->generations - 1] =
+            std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - ctx->gen_t0).count();
     *ctx->launches_host = launches;
     CUDA_TRY(ctx, cudaMemcpyAsync(&a.counters->kernel_launches, ctx->launches_host, sizeof(unsigned long long),
                                   cudaMemcpyHostToDevice, s));
@@ -626,6 +643,16 @@ extern "C" int cor_upload_crustal(cor_ctx* ctx, const double* g, const double* h
     if (!ctx) return COR_ERR_INVALID;
     if (!g || !h) return fail(ctx, COR_ERR_INVALID, "null crustal table");
     return upload_crustal(ctx, g, h, nmax);
+}
+
+extern "C" int32_t cor_ctx_generation_log(const cor_ctx* ctx, int32_t cap, uint64_t* live, double* ms) {
+    if (!ctx) return COR_ERR_INVALID;
+    const int n = ctx->generations;
+    for (int g = 0; g < n && g < cap; g++) {
+        if (live) live[g] = ctx->gen_live[g];
+        if (ms) ms[g] = ctx->gen_ms[g];
+    }
+    return n;
 }
 
 extern "C" int cor_ctx_set_queue_order(cor_ctx* ctx, int32_t rigidity_major) {
@@ -1010,9 +1037,12 @@ extern "C" int cor_trace_batch_device_noalloc(cor_ctx* ctx, const cor_scan_job* 
         int per_sm = 0;
         CUDA_TRY(ctx, ops->occupancy(&per_sm));
         if (per_sm < 1) per_sm = 1;
-        uint64_t blocks = (n_traj + kTraceThreads - 1) / kTraceThreads;
         const uint64_t cap = (uint64_t)ctx->sms * (uint64_t)per_sm;
-        if (blocks > cap) blocks = cap;
+        const uint64_t warps = (n_traj + 31) / 32;
+        uint64_t blocks = warps < cap ? warps : cap;
+        uint64_t per_block = 32 * ((warps + blocks - 1) / blocks);
+        if (per_block > (uint64_t)kTraceThreads) per_block = kTraceThreads;
+        a.active_threads = (uint32_t)per_block;
         a.launched_warps = (uint32_t)(blocks * kTraceWarps);
         CUDA_TRY(ctx, ops->launch_generation(a, (unsigned)blocks, s));
         launches++;

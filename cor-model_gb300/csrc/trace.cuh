@@ -73,6 +73,11 @@ struct TraceArgs {
     // step_records[t * step_cap + step - 1] (null: not recorded)
     cor_step_record* step_records;
     uint32_t step_cap;
+    // threads of each block that take trajectories (a multiple of 32, at
+    // most kTraceThreads): a generation with few trajectories spreads them
+    // over more SMs, a warp or two each, instead of packing them into a few
+    // blocks whose warps would share one SM's FP64 pipe
+    uint32_t active_threads;
 };
 
 __device__ __forceinline__ int find_job(const uint64_t* __restrict__ off, int n_jobs, uint64_t t) {
@@ -298,14 +303,14 @@ constexpr int kTraceWarps = kTraceThreads / 32;
 // instructions together and share the instruction-cache fills.
 // A lane with no trajectory takes the next parked one, else the next queue
 // index.  Once the queue is drained, a block whose live lanes fall below
-// park_below per warp -- or any block, once half of the generation's warps
-// have parked -- writes its live trajectories to the park list and leaves;
+// park_below per working warp -- or any block, once half of the generation's
+// warps have parked -- writes its live trajectories to the park list and leaves;
 // the host then launches the next generation sized to the parked count,
 // which restores them densely (the regroup step).
 template <class MS>
 __global__ void __launch_bounds__(kTraceThreads, 1) trace_kernel(const TraceArgs a) {
     Lane L;
-    bool has = false, done = false;
+    bool has = false, done = threadIdx.x >= a.active_threads;
     unsigned long long n_steps = 0, n_trials = 0, n_traj = 0, n_wd = 0;
     const int lane = threadIdx.x & 31;
     for (;;) {
@@ -354,15 +359,16 @@ __global__ void __launch_bounds__(kTraceThreads, 1) trace_kernel(const TraceArgs
                 done = true;
             }
         }
-        // block-wide decisions: every thread of the block takes the same branch
+        // block-wide decisions: every thread of the block takes the same
+        // branch (threads beyond active_threads are done from the start)
         const int n_done = __syncthreads_count(done);
         if (n_done == kTraceThreads) break;
-        if (a.allow_park && n_done > 0) {
+        if (a.allow_park && n_done > kTraceThreads - (int)a.active_threads) {
             const int n_live = __syncthreads_count(has);
             unsigned pw = 0;
             if (threadIdx.x == 0) pw = *((volatile unsigned int*)&a.gen->parked_warps);
             const int half = __syncthreads_or(threadIdx.x == 0 && 2u * pw >= a.launched_warps);
-            if (n_live < a.park_below * kTraceWarps || half) {
+            if (n_live < a.park_below * (int)(a.active_threads / 32) || half) {
                 // need_field lanes were just initialised or advanced: the
                 // generation that restores them evaluates their field (the
                 // loop keeps a single calculate_field call site, so the field

@@ -214,6 +214,13 @@ int cor_upload_params(cor_ctx *ctx, const cor_model_params *params, int32_t n_pa
  * do not depend on these settings, only the time does. */
 int cor_ctx_set_regroup(cor_ctx *ctx, int32_t park_below, int32_t max_generations, int64_t min_park);
 
+/* Diagnostics of the last scan on this context (no counterpart in the
+ * reference): for each kernel generation, the live trajectories it started
+ * with and its host wall time [ms] (generation 0 drains the work queue; the
+ * later ones run regrouped tails).  Fills up to cap entries and returns the
+ * number of generations (negative COR_ERR_* for a null context). */
+int32_t cor_ctx_generation_log(const cor_ctx *ctx, int32_t cap, uint64_t *live, double *ms);
+
 /* Work-queue order of cor_trace_batch on this context when every job has the
  * same number of rigidities (no counterpart in the reference; an autotuner's
  * knob): 1 (default) hands out the lowest rigidity of every scan first
