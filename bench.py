@@ -38,7 +38,8 @@ WORKLOAD = "igrf14+t96 5x5deg global grid, vertical, 20 km, 20->0.01 GV by 0.01 
 TIME7 = [2020, 6, 21, 173, 12, 0, 0]
 PARMOD = [2.0, -20.0, 0.0, -1.0]
 N_RIG = 2000
-METRIC = "site cutoffs/s"
+METRIC = "site cutoffs/s on 1 GB300: plain scan vs learned window at |\u0394Rc|\u22640.01 GV"
+UNIT = "site cutoffs/s"
 WINDOW_FILE = os.path.join(ROOT, "cor-model_gb300", "window_t96.npz")
 # DRAM bytes (read + write) per trajectory of the scan kernel, from the ncu
 # capture of the profiling case (profiles/trace_kernel_igrf_t96_profile_case.md:
@@ -170,7 +171,7 @@ def cpu_baseline(n_batches: int, seconds_hint: float = 20.0) -> dict:
     t = time.perf_counter()
     res = pyoracle.scan_batch(jobs, params(), models=models(), threads=threads)
     dt = time.perf_counter() - t
-    return {"value": len(sample) / dt, "unit": METRIC, "cores": threads, "kind": "port",
+    return {"value": len(sample) / dt, "unit": UNIT, "cores": threads, "kind": "port",
             "sample": f"{len(sample)} sites x {N_RIG} rigidities of the same grid and conditions "
                       f"({res.counters['trajectories']} trajectories, {dt:.1f} s wall)",
             "steps_per_s": res.counters["accepted_steps"] / dt}
@@ -299,7 +300,7 @@ def measure_window(args, slots, bufs, p, plain_e2e: float) -> dict:
         full_traj += bufs[i]["n"]
     wm.close()
     v = n_sites / wall
-    return {"value": v, "unit": METRIC, "speedup_vs_plain_e2e": v / plain_e2e if plain_e2e else None,
+    return {"value": v, "unit": UNIT, "speedup_vs_plain_e2e": v / plain_e2e if plain_e2e else None,
             "sites": n_sites, "agree_frac_dRc_le_0.01GV": agree / n_sites, "max_abs_dRc_GV": worst,
             "fallback_frac": fallback / n_sites, "trajectories_frac_of_full_scan": traced / full_traj,
             "model": json.loads(wm.info) if wm.info.startswith("{") else wm.info,
@@ -405,7 +406,7 @@ def run_ours(args, rank: int, world: int, dist) -> dict | None:
     flops = steps_acc * wm["flops_per_step"] + rejected * wm["flops_per_rejected_trial"]
     achieved = flops / dev_s / 1e12
     out = {
-        "metric": METRIC, "value": sites_done / dev_s, "unit": METRIC, "n_gpus": world,
+        "metric": METRIC, "value": sites_done / dev_s, "unit": UNIT, "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": dev_s * 1e3 / args.steps,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
         "data": "synthetic grid of sites (the configuration's own sites; no dataset)",
@@ -425,7 +426,7 @@ def run_ours(args, rank: int, world: int, dist) -> dict | None:
                      "work_model": wm.get("source"),
                      "flops_per_step": wm["flops_per_step"],
                      "peak_source": "DFMA microbenchmark in libcortrace (cor_probe_fp64_peak), FMA = 2 flops"},
-        "e2e": {"value": sites_done / e2e_s, "unit": METRIC,
+        "e2e": {"value": sites_done / e2e_s, "unit": UNIT,
                 "h2d_bytes_per_step": h2d // args.steps, "d2h_bytes_per_step": d2h // args.steps},
         "gpu_launches": sum(int(b["counters"][4]) for b in timed),
         "clocks": clocks.summary(),
@@ -494,13 +495,13 @@ def run_reference(args, rank: int) -> dict | None:
             dt_tot += dt
             steps += 1
     v = done / dt_tot
-    return {"metric": METRIC, "value": v, "unit": METRIC, "n_gpus": 0, "steps": args.steps, "warmup": args.warmup,
+    return {"metric": METRIC, "value": v, "unit": UNIT, "n_gpus": 0, "steps": args.steps, "warmup": args.warmup,
             "ms_per_step": dt_tot * 1e3 / max(1, steps), "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f64", "data": "synthetic grid of sites", "impl": "reference",
             "config": {"workload": WORKLOAD, "sites_per_step": threads},
-            "cpu_baseline": {"value": v, "unit": METRIC, "cores": threads, "kind": "port",
+            "cpu_baseline": {"value": v, "unit": UNIT, "cores": threads, "kind": "port",
                              "sample": f"{threads} sites x {N_RIG} rigidities per step, one site per thread"},
-            "e2e": {"value": v, "unit": METRIC, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+            "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
 
 
 def main():
