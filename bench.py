@@ -308,6 +308,20 @@ def measure_window(args, slots, bufs, p, plain_e2e: float) -> dict:
                    "cor_trace_batch, network inference on the tensor cores inside the timed region"}
 
 
+def reduce_over_ranks(dist, seconds: float, counts: list, device: str) -> list:
+    """Whole-job figures of a multi-rank run: the slowest rank's time (MAX)
+    and the sums of the per-rank counts.  Returns [seconds, *counts]."""
+    import torch
+    t = torch.tensor([seconds], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    out = [float(t.item())]
+    if counts:
+        c = torch.tensor([float(v) for v in counts], dtype=torch.float64, device=device)
+        dist.all_reduce(c)
+        out += [int(v) for v in c.tolist()]
+    return out
+
+
 def run_ours(args, rank: int, world: int, dist) -> dict | None:
     import torch
     dev = int(os.environ.get("LOCAL_RANK", "0"))
@@ -352,13 +366,8 @@ def run_ours(args, rank: int, world: int, dist) -> dict | None:
     sites_done = sum(b["n_jobs"] for b in timed)
     launch_ms = [b["kernel_ms"] for b in timed]
     if dist:
-        import torch.distributed as tdist
-        t = torch.tensor([dev_s], dtype=torch.float64, device=f"cuda:{dev}")
-        tdist.all_reduce(t, op=tdist.ReduceOp.MAX)
-        dev_s = float(t.item())
-        tot = torch.tensor([sites_done, traj_done, steps_acc, trials_acc], dtype=torch.float64, device=f"cuda:{dev}")
-        tdist.all_reduce(tot)
-        sites_done, traj_done, steps_acc, trials_acc = (int(v) for v in tot.tolist())
+        dev_s, sites_done, traj_done, steps_acc, trials_acc = reduce_over_ranks(
+            dist, dev_s, [sites_done, traj_done, steps_acc, trials_acc], f"cuda:{dev}")
 
     # e2e through the public C ABI with host buffers (same overlap, one host
     # thread per slot, cor_trace_batch copies in and out inside the call)
@@ -390,10 +399,7 @@ def run_ours(args, rank: int, world: int, dist) -> dict | None:
     h2d = sum(a for a, _ in sizes)
     d2h = sum(b for _, b in sizes)
     if dist:
-        import torch.distributed as tdist
-        t = torch.tensor([e2e_s], dtype=torch.float64, device=f"cuda:{dev}")
-        tdist.all_reduce(t, op=tdist.ReduceOp.MAX)
-        e2e_s = float(t.item())
+        e2e_s = reduce_over_ranks(dist, e2e_s, [], f"cuda:{dev}")[0]
     learned = None
     if args.window and os.path.exists(args.window) and world == 1:
         learned = measure_window(args, slots, bufs, p, sites_done / e2e_s)
