@@ -302,10 +302,11 @@ def measure_window(args, slots, bufs, p, plain_e2e: float) -> dict:
     v = n_sites / wall
     return {"value": v, "unit": UNIT, "speedup_vs_plain_e2e": v / plain_e2e if plain_e2e else None,
             "sites": n_sites, "agree_frac_dRc_le_0.01GV": agree / n_sites, "max_abs_dRc_GV": worst,
-            "fallback_frac": fallback / n_sites, "trajectories_frac_of_full_scan": traced / full_traj,
+            "widened_frac": fallback / n_sites, "trajectories_frac_of_full_scan": traced / full_traj,
             "model": json.loads(wm.info) if wm.info.startswith("{") else wm.info,
-            "how": "predicted window +-3 sigma on the 0.01 GV grid, full scan on an edge hit; host buffers through "
-                   "cor_trace_batch, network inference on the tensor cores inside the timed region"}
+            "how": "predicted window +-3 sigma on the 0.01 GV grid, widened on the hit side on an edge hit (full scan "
+                   "after 3 widenings); host buffers through cor_trace_batch, network inference on the tensor cores "
+                   "inside the timed region"}
 
 
 def reduce_over_ranks(dist, seconds: float, counts: list, device: str) -> list:

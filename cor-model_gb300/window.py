@@ -242,29 +242,48 @@ def window_jobs(jobs: np.ndarray, i_lo: np.ndarray, i_hi: np.ndarray) -> np.ndar
     return w
 
 
-def trace_windows(ctx, jobs, params, models, i_lo, i_hi, **kw):
-    """Scan every job over its window, then scan in full every job whose
-    window had a boundary on an edge.  Returns (sites, fallback mask,
-    trajectories traced, accepted steps)."""
-    wj = window_jobs(jobs, i_lo, i_hi)
-    res = ctx.trace_batch(wj, params, models=models, **kw)
+def trace_windows(ctx, jobs, params, models, i_lo, i_hi, widen: int = 3, **kw):
+    """Scan every job over its window.  A job whose window had a boundary on
+    an edge is scanned again over a window widened on that side (its width
+    doubled there, clipped to the grid), up to `widen` times, and then over
+    its whole grid: every reported cutoff comes from a window whose first
+    rigidity is forbidden and whose last is allowed (or from the whole scan).
+    Returns (sites, mask of jobs that needed more than one pass, trajectories
+    traced, accepted steps)."""
     n_grid = (np.round((jobs["rk"] - jobs["rig"]) / jobs["del"]).astype(np.int64) + 1)
-    fallback = np.zeros(len(jobs), bool)
-    for j in range(len(jobs)):
-        st = res.status[res.offsets[j]:res.offsets[j + 1]]
-        fallback[j] = edge_hit(st, int(i_lo[j]), int(i_hi[j]), int(n_grid[j]))
-    sites = res.sites.copy()
-    traced = int(res.counters["trajectories"])
-    steps = int(res.counters["accepted_steps"])
-    if fallback.any():
-        fj = np.array(jobs[fallback], copy=True)
-        fj["i_first"] = 0
-        fj["i_count"] = 0
-        fr = ctx.trace_batch(fj, params, models=models, want_status=False, **kw)
-        sites[fallback] = fr.sites
-        traced += int(fr.counters["trajectories"])
-        steps += int(fr.counters["accepted_steps"])
-    return sites, fallback, traced, steps
+    lo = np.asarray(i_lo, np.int64).copy()
+    hi = np.asarray(i_hi, np.int64).copy()
+    sites = np.zeros(len(jobs), ct.SITE_DTYPE)
+    redone = np.zeros(len(jobs), bool)
+    todo = np.arange(len(jobs))
+    traced = steps = 0
+    for attempt in range(widen + 2):
+        if len(todo) == 0:
+            break
+        if attempt == widen + 1:                 # last resort: the whole grid
+            lo[todo] = 0
+            hi[todo] = n_grid[todo] - 1
+        res = ctx.trace_batch(window_jobs(jobs[todo], lo[todo], hi[todo]), params, models=models, **kw)
+        traced += int(res.counters["trajectories"])
+        steps += int(res.counters["accepted_steps"])
+        again = []
+        for k, j in enumerate(todo):
+            st = res.status[res.offsets[k]:res.offsets[k + 1]]
+            allowed = st == ct.TRAJ_ALLOWED
+            low = lo[j] > 0 and allowed[0]
+            high = hi[j] < n_grid[j] - 1 and not allowed[-1]
+            if not (low or high):
+                sites[j] = res.sites[k]
+                continue
+            width = hi[j] - lo[j] + 1
+            if low:
+                lo[j] = max(0, lo[j] - width)
+            if high:
+                hi[j] = min(n_grid[j] - 1, hi[j] + width)
+            again.append(j)
+        redone[again] = True
+        todo = np.array(again, np.int64)
+    return sites, redone, traced, steps
 
 
 class WindowModel:

@@ -108,3 +108,33 @@ def test_window_indices_and_edge_rule():
     assert window.edge_hit(np.array([A, F, A, A]), 100, 103)              # allowed at the bottom edge
     assert window.edge_hit(np.array([F, A, A, F]), 100, 103)              # forbidden at the top edge
     assert not window.edge_hit(np.array([A, A]), 0, 1)                    # the grid's own first index
+
+
+class _OracleCtx:
+    """cor_trace_batch of the oracle, standing in for a GPU context."""
+
+    def trace_batch(self, jobs, params, models=None, **kw):
+        import pyoracle
+        return pyoracle.scan_batch(jobs, params, models=models, threads=4)
+
+
+def test_window_scan_widens_to_the_whole_scans_cutoffs():
+    """Windows that miss the penumbra on either side are widened until they
+    hold it; the cutoffs then equal the whole scans' bit for bit (oracle,
+    IGRF-14, coarse grid).  (A window that ends on an allowed rigidity
+    inside the penumbra looks conclusive and is not widened: the method's
+    own limit, which the bench's comparison with the full scan measures.)"""
+    import cortrace as ct
+    p = ct.internal_setup("igrf14", [2020, 1, 1, 1, 0, 0, 0])
+    jobs = np.concatenate([ct.make_job(la, lo, rig=0.2, rk=20.0, dele=0.2) for la, lo in ((10.0, 30.0), (-40.0, 200.0),
+                                                                                           (55.0, 90.0))])
+    ctx = _OracleCtx()
+    whole = ctx.trace_batch(jobs, p, models=ct.model_set())
+    n = len(whole.status) // len(jobs)
+    # deliberately poor windows: above the penumbra (two of them) and below it
+    i_lo = np.array([n - 20, 40, 2])
+    i_hi = np.array([n - 10, 50, 4])
+    sites, redone, traced, _ = window.trace_windows(ctx, jobs, p, ct.model_set(), i_lo, i_hi)
+    for k in ("r_lower", "r_upper", "r_cutoff", "n_forbidden"):
+        assert np.array_equal(sites[k], whole.sites[k]), k
+    assert redone.all()
