@@ -67,7 +67,7 @@ struct TraceArgs {
     ParkedLane* park;              // where this generation parks (capacity = launched threads)
     GenCounters* gen;
     int allow_park;                // 0 in the last generation
-    int park_below;                // a warp parks when fewer lanes than this are live
+    int park_below;                // a block parks when fewer lanes than this per working warp are live
     uint32_t launched_warps;
     // trajectory dump: every accepted step of trajectory t goes to
     // step_records[t * step_cap + step - 1] (null: not recorded)
