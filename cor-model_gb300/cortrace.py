@@ -51,7 +51,9 @@ SITE_DTYPE = np.dtype([
     ("n_forbidden", "i4"), ("n_traj", "i4")], align=True)
 TRIG_DTYPE = np.dtype([(k, "f8") for k in ("st0", "ct0", "sp0", "cp0", "st1", "ct1", "sp1", "cp1")], align=True)
 
-assert JOB_DTYPE.itemsize == 88 and PARAMS_DTYPE.itemsize == 2672
+STEP_DTYPE = np.dtype([("gsm", "f8", 3), ("pos", "f8", 3), ("v", "f8"), ("time", "f8"), ("length", "f8"),
+                       ("step", "u4"), ("reserved", "u4")], align=True)
+assert JOB_DTYPE.itemsize == 88 and PARAMS_DTYPE.itemsize == 2672 and STEP_DTYPE.itemsize == 80
 assert RECORD_DTYPE.itemsize == 88 and SITE_DTYPE.itemsize == 32
 
 
@@ -233,6 +235,30 @@ class Context:
         res = BatchResult(_ptr(sites), _ptr(status), _ptr(records), Counters())
         self._check(self.lib.cor_trace_batch(self.h, C.byref(req), C.byref(res)), "trace_batch")
         return ScanResult(sites, status, records, off, res.counters.as_dict())
+
+    def trace_steps(self, jobs: np.ndarray, params: np.ndarray, models: ModelSet | None = None,
+                    step_limit: int = 25000, tu_angle: float = 0.01, particle_mass: float = DEF_HM0_P,
+                    capacity: int = 25000) -> tuple[ScanResult, list[np.ndarray]]:
+        """cor_trace_steps: the scan's result and, per trajectory, its
+        accepted steps (STEP_DTYPE records, at most `capacity`)."""
+        jobs = np.ascontiguousarray(jobs, JOB_DTYPE)
+        params = np.ascontiguousarray(params, PARAMS_DTYPE)
+        n, off = batch_offsets(jobs)
+        sites = np.zeros(len(jobs), SITE_DTYPE)
+        status = np.zeros(n, np.uint8)
+        records = np.zeros(n, RECORD_DTYPE)
+        steps = np.zeros(n * capacity, STEP_DTYPE)
+        req = BatchReq(_ptr(jobs), len(jobs), len(params), _ptr(params), models or model_set(),
+                       step_limit, tu_angle, particle_mass)
+        res = BatchResult(_ptr(sites), _ptr(status), _ptr(records), Counters())
+        self._check(self.lib.cor_trace_steps(self.h, C.byref(req), C.byref(res), _ptr(steps), capacity), "trace_steps")
+        per = []
+        for t in range(n):
+            s = steps[t * capacity:(t + 1) * capacity]
+            k = int(np.argmax(s["step"] != np.arange(1, capacity + 1))) if np.any(
+                s["step"] != np.arange(1, capacity + 1)) else capacity
+            per.append(s[:k].copy())
+        return ScanResult(sites, status, records, off, res.counters.as_dict()), per
 
     def set_regroup(self, park_below: int = 16, max_generations: int = 48, min_park: int = 256) -> None:
         """cor_ctx_set_regroup: the scan kernel's regrouping knobs."""

@@ -24,7 +24,6 @@ import argparse
 import dataclasses
 import json
 import os
-import queue
 import sys
 import threading
 import time

@@ -11,7 +11,6 @@ from __future__ import annotations
 
 import ctypes as C
 import math
-import os
 
 import numpy as np
 

@@ -285,7 +285,7 @@ static int64_t o_n_traced(const cor_scan_job *job) {
 /* One trajectory, src/trajectory.c:13-153.  Returns the COR_TRAJ_* class. */
 static int o_trace_one(const cor_scan_job *job, const cor_model_params *p, cor_model_set models,
                        uint64_t step_limit, double tu_angle, double mass, double rig,
-                       cor_traj_record *rec) {
+                       cor_traj_record *rec, cor_step_record *steps, uint32_t step_cap) {
     int nk0 = job->nk1;
     double alength = 0., time = 0.;
     const double a = rig * 1.0e+09 * job->zn * O_Q / (mass * O_C * O_C);
@@ -357,6 +357,16 @@ static int o_trace_one(const cor_scan_job *job, const cor_model_params *p, cor_m
         alength += sqrt((pos[0] - prev_pos[0]) * (pos[0] - prev_pos[0]) +
                         (pos[1] - prev_pos[1]) * (pos[1] - prev_pos[1]) +
                         (pos[2] - prev_pos[2]) * (pos[2] - prev_pos[2]));
+        if (steps && step <= step_cap) {                               /* trajectory mode, :254-258 */
+            cor_step_record *o = &steps[step - 1];
+            memcpy(o->gsm, gsm, sizeof gsm);
+            memcpy(o->pos, pos, sizeof pos);
+            o->v = v;
+            o->time = time;
+            o->length = alength;
+            o->step = step;
+            o->reserved = 0;
+        }
         nk0 = job->nk1;
     }
     if (rec) {
@@ -387,7 +397,7 @@ int orc_scan_job(const cor_scan_job *job, const cor_model_params *params, cor_mo
         const int64_t i = job->i_first + k;
         const double rig = job->rig + i * job->del;                    /* :14 */
         cor_traj_record r;
-        const int st = o_trace_one(job, params, models, step_limit, tu_angle, particle_mass, rig, &r);
+        const int st = o_trace_one(job, params, models, step_limit, tu_angle, particle_mass, rig, &r, NULL, 0);
         if (st == COR_TRAJ_ALLOWED) {
             rmi = fmin(rmi, rig);                                      /* :115 */
         } else if (st == COR_TRAJ_REENTRY || st == COR_TRAJ_SUPERLUM) {
@@ -481,4 +491,21 @@ int orc_scan_batch(const cor_batch_req *req, const uint64_t *offsets, int thread
     pthread_mutex_destroy(&pl.lock);
     if (counters) *counters = pl.total;
     return pl.err;
+}
+
+/* trajectory_simulation (src/trajectory.c:163-273) for the first traced
+ * rigidity of a job: every accepted step into steps[0 .. step_cap-1]; returns
+ * the number recorded (or a negative COR_ERR_*). */
+int orc_trace_steps(const cor_scan_job *job, const cor_model_params *params, cor_model_set models,
+                    uint64_t step_limit, double tu_angle, double particle_mass,
+                    cor_step_record *steps, uint32_t step_cap, cor_traj_record *rec) {
+    if (!(job->del > 0.) || o_n_traced(job) < 1) return COR_ERR_INVALID;
+    const double rig = job->rig + (int64_t)job->i_first * job->del;
+    cor_traj_record r;
+    memset(steps, 0, sizeof(cor_step_record) * step_cap);
+    o_trace_one(job, params, models, step_limit, tu_angle, particle_mass, rig, &r, steps, step_cap);
+    if (rec) *rec = r;
+    uint32_t n = 0;
+    while (n < step_cap && steps[n].step == n + 1) n++;
+    return (int)n;
 }

@@ -47,6 +47,11 @@ void orc_set_crustal_table(const double *g, const double *h, int nmax);
 /* trajectory_simulation_cutoff, src/trajectory.c:6-161, serial semantics,
  * for one scan.  records/status have round((rk-rig)/del)+1 entries (either may
  * be NULL).  Counters are added to *counters when not NULL. */
+/* Per-step records of the first traced rigidity of a job (trajectory mode). */
+int orc_trace_steps(const cor_scan_job *job, const cor_model_params *params, cor_model_set models,
+                    uint64_t step_limit, double tu_angle, double particle_mass,
+                    cor_step_record *steps, uint32_t step_cap, cor_traj_record *rec);
+
 int orc_scan_job(const cor_scan_job *job, const cor_model_params *params, cor_model_set models,
                  uint64_t step_limit, double tu_angle, double particle_mass,
                  cor_site_result *site, uint8_t *status, cor_traj_record *records,

@@ -40,6 +40,7 @@ def load() -> C.CDLL:
         lib.orc_set_crustal_table.argtypes = [vp, vp, C.c_int]
         lib.orc_scan_job.argtypes = [vp, vp, ct.ModelSet, C.c_uint64, dbl, dbl, vp, vp, vp, vp]
         lib.orc_scan_batch.argtypes = [C.POINTER(ct.BatchReq), vp, C.c_int, vp, vp, vp, vp]
+        lib.orc_trace_steps.argtypes = [vp, vp, ct.ModelSet, C.c_uint64, dbl, dbl, vp, C.c_uint32, vp]
         lib.orc_internal_geo_flops.argtypes = [dbl]
         lib.orc_internal_geo_flops.restype = C.c_int64
         _lib = lib
@@ -153,6 +154,24 @@ def scan_batch(jobs: np.ndarray, params: np.ndarray, models=None, step_limit=250
     if rc != 0:
         raise RuntimeError(f"oracle scan failed: {rc}")
     return ct.ScanResult(sites, status, records, off, cnt.as_dict())
+
+
+STEP_DTYPE = ct.STEP_DTYPE
+
+
+def trace_steps(job: np.ndarray, params: np.ndarray, models=None, step_limit=25000, tu_angle=0.01,
+                particle_mass=ct.DEF_HM0_P, cap=25000) -> np.ndarray:
+    """Every accepted step of the job's first traced rigidity (cor_step_record)."""
+    lib = load()
+    job = np.ascontiguousarray(job, ct.JOB_DTYPE)
+    params = np.ascontiguousarray(params, ct.PARAMS_DTYPE)
+    out = np.zeros(cap, STEP_DTYPE)
+    m = models or ct.model_set()
+    _crustal(lib, m)
+    n = lib.orc_trace_steps(_p(job), _p(params), m, step_limit, tu_angle, particle_mass, _p(out), cap, None)
+    if n < 0:
+        raise RuntimeError(f"oracle trajectory failed: {n}")
+    return out[:n]
 
 
 def internal_geo_flops(R: float) -> int:

@@ -414,3 +414,21 @@ def test_results_do_not_depend_on_regrouping(ctx):
     for r in out[1:]:
         assert np.array_equal(r.sites.view(np.uint8), out[0].sites.view(np.uint8))
         assert np.array_equal(r.records.view(np.uint8), out[0].records.view(np.uint8))
+
+
+def test_trace_steps_equal_oracle(ctx):
+    """cor_trace_steps (the trajectory dump) records the oracle's steps bit
+    for bit with IGRF-14: positions, GSM positions, speed, time and length of
+    every accepted step, for an allowed and a forbidden rigidity."""
+    p = ct.internal_setup("igrf14", [2020, 1, 1, 1, 0, 0, 0])
+    for lat, lon, rig in ((50.0, 15.0, 10.0), (0.0, 100.0, 3.0)):
+        job = ct.make_job(lat, lon, rig=rig, rk=rig, dele=0.05)
+        res, per = ctx.trace_steps(job, p)
+        want = pyoracle.trace_steps(job, p)
+        got = per[0]
+        # an allowed trajectory's record counts its recorded steps; any other
+        # also counts the step that ended it (src/trajectory.c:133-145)
+        ended = int(res.records[0]["status"] != ct.TRAJ_ALLOWED)
+        assert len(got) == len(want) == int(res.records[0]["steps"]) - ended
+        for k in ("gsm", "pos", "v", "time", "length", "step"):
+            assert np.array_equal(got[k], want[k]), k

@@ -163,3 +163,45 @@ def test_oracle_window_equals_whole_scan():
     cut["i_count"] = cut["i_count"] - 6
     bad = pyoracle.scan_batch(cut, p, threads=8)
     assert any(bad.sites[j]["r_upper"] != full.sites[j]["r_upper"] for j in range(len(sites)))
+
+
+def _parse_cutoff_infile(text):
+    """INFILE of `cor -m cutoff|trajectory` (src/io.c:4-20) -> (job, time7)."""
+    v = text.split()
+    rig, zn, rk, r0, lat, lon, the1, fi1 = (float(x) for x in v[:8])
+    t7 = [int(x) for x in v[8:15]]
+    nk1, dele = int(v[15]), float(v[18])
+    return ct.make_job(lat, lon, rig=rig, rk=rk, dele=dele if dele > 0 else 1.0, r0=r0, the1=the1, fi1=fi1, zn=zn,
+                       nk1=nk1), t7
+
+
+def test_oracle_trajectory_mode_matches_reference():
+    """The oracle's per-step records, printed in trajectory_simulation's
+    formats (src/trajectory.c:254-258), reproduce the reference's tragsm_ and
+    trasph_ files byte for byte (IGRF-14, one allowed and one forbidden
+    rigidity)."""
+    import hashlib
+    import math
+    g = golden("trajectory_cli.json")
+    for case in ("igrf14_allowed", "igrf14_forbidden"):
+        job, t7 = _parse_cutoff_infile(g[case]["infile"])
+        p = ct.internal_setup("igrf14", t7)
+        steps = pyoracle.trace_steps(job, p)
+        gsm_lines, sph_lines = [], []
+        for s in steps:
+            x, y, z = s["pos"]
+            sq = x * x + y * y
+            r = math.sqrt(sq + z * z)
+            theta = math.atan2(math.sqrt(sq), z)
+            phi = math.atan2(y, x)
+            if phi < 0.:
+                phi += 6.28318531
+            to_rad = 3.141592654 / 180.
+            row = (s["v"], s["time"], s["length"])
+            gsm_lines.append("%6d%17.5f%17.5f%17.5f%14.2f%15.10f%18.2f\n" % (s["step"], *s["gsm"], *row))
+            sph_lines.append("%6d%17.5f%17.5f%17.5f%14.2f%15.10f%18.2f\n"
+                             % (s["step"], r / 6.3712e+06, 90. - theta / to_rad, phi / to_rad, *row))
+        for pre, lines in (("tragsm_", gsm_lines), ("trasph_", sph_lines)):
+            body = "".join(lines)
+            assert len(lines) == g[case][pre]["lines"], (case, pre)
+            assert hashlib.sha256(body.encode()).hexdigest() == g[case][pre]["sha256"], (case, pre)
