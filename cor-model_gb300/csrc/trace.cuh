@@ -1,13 +1,16 @@
 // trace.cuh -- the persistent rigidity-scan kernel (trajectory_simulation_cutoff,
-// src/trajectory.c:6-161) and the per-scan reduction (:156-160).
+// src/trajectory.c:6-153); the per-scan reduction (:156-160) is reduce.cuh.
 //
 // One trajectory per thread.  Threads pull trajectory indices from a device
 // work queue (one 64-bit counter, warp-aggregated atomics) and refill
 // themselves as soon as their trajectory terminates, so a warp keeps all 32
 // lanes busy while trajectory lengths range from tens to 25k steps.  Each
 // pass of the main loop advances every lane by exactly one accepted step (or
-// one termination + refill), and then evaluates the field for all lanes at
-// once, so the expensive field evaluation runs converged.
+// one termination + refill) and then evaluates the field for all lanes at
+// once, so the expensive field evaluation runs converged; the pass's exit and
+// park decisions are block-wide, which also keeps the block's warps in step
+// through the field models' code.  The same loop records every accepted step
+// when a trajectory dump is requested (cor_trace_steps).
 #pragma once
 
 #include "field.cuh"
