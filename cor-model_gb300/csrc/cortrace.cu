@@ -1,6 +1,7 @@
 // cortrace.cu -- the C ABI of libcortrace.so (include/cor_trace.h) over the
 // device kernels in trace.cuh.  Compiled with --fmad=false: see cor_device.cuh.
 #include <cuda_runtime.h>
+#include <nvtx3/nvToolsExt.h>
 
 #include <math.h>
 #include <chrono>
@@ -65,6 +66,15 @@ extern "C" {
 const char* cor_last_error_string(const cor_ctx* ctx) { return ctx ? ctx->err : "null context"; }
 int cor_abi_version(void) { return COR_TRACE_ABI_VERSION; }
 }
+
+// NVTX range over a phase of a call (scan, generation, reduction, field
+// batch); a no-op unless a profiler is attached.
+struct NvtxRange {
+    explicit NvtxRange(const char* name) { nvtxRangePushA(name); }
+    ~NvtxRange() { nvtxRangePop(); }
+    NvtxRange(const NvtxRange&) = delete;
+    NvtxRange& operator=(const NvtxRange&) = delete;
+};
 
 static int fail(cor_ctx* ctx, int code, const char* fmt, ...) {
     if (ctx) {
@@ -518,7 +528,10 @@ static int launch_trace(cor_ctx* ctx, const ModelOps* ops, TraceArgs a, cudaStre
         ctx->gen_t0 = std::chrono::steady_clock::now();
         ctx->gen_live[g] = live;
         ctx->gen_ms[g] = -1.;
-        CUDA_TRY(ctx, ops->launch_generation(a, (unsigned)blocks, s));
+        {
+            NvtxRange r(g == 0 ? "cor: scan generation 0" : "cor: scan generation (regrouped)");
+            CUDA_TRY(ctx, ops->launch_generation(a, (unsigned)blocks, s));
+        }
         ctx->generations = g + 1;
         if (!a.allow_park) break;
         CUDA_TRY(ctx, cudaMemcpyAsync(ctx->park_count_host, &ctx->gen->park_count, sizeof(unsigned int),
@@ -709,6 +722,7 @@ extern "C" int cor_trace_batch_device(cor_ctx* ctx, const cor_scan_job* jobs_dev
                                       uint64_t step_limit, double tu_angle, double particle_mass,
                                       cor_site_result* sites_dev, uint8_t* status_dev, cor_traj_record* records_dev,
                                       cor_counters* counters_dev, uint32_t flags, void* stream) {
+    NvtxRange nvtx_range("cor_trace_batch_device");
     if (!ctx) return COR_ERR_INVALID;
     int rc = check_req(ctx, models, ctx->n_params, step_limit, tu_angle, particle_mass);
     if (rc != COR_OK) return rc;
@@ -750,6 +764,7 @@ extern "C" int cor_trace_batch_device(cor_ctx* ctx, const cor_scan_job* jobs_dev
 }
 
 extern "C" int cor_trace_batch(cor_ctx* ctx, const cor_batch_req* req, cor_batch_result* out) {
+    NvtxRange nvtx_range("cor_trace_batch");
     if (!ctx || !req || !out) return COR_ERR_INVALID;
     int rc = check_req(ctx, req->models, req->n_params, req->step_limit, req->tu_angle, req->particle_mass);
     if (rc != COR_OK) return rc;
@@ -819,6 +834,7 @@ extern "C" int cor_trace_batch(cor_ctx* ctx, const cor_batch_req* req, cor_batch
 
 extern "C" int cor_trace_steps(cor_ctx* ctx, const cor_batch_req* req, cor_batch_result* out, cor_step_record* steps,
                                uint32_t step_capacity) {
+    NvtxRange nvtx_range("cor_trace_steps");
     if (!ctx || !req || !out) return COR_ERR_INVALID;
     if (!steps || step_capacity == 0) return fail(ctx, COR_ERR_INVALID, "no step record buffer");
     uint64_t n_traj = 0;
@@ -841,6 +857,7 @@ extern "C" int cor_trace_steps(cor_ctx* ctx, const cor_batch_req* req, cor_batch
 
 extern "C" int cor_field_batch(cor_ctx* ctx, cor_model_set models, const cor_model_params* params, int32_t n_params,
                                const int32_t* param_index, const double* gsm_pos, int64_t n, double* geo_field) {
+    NvtxRange nvtx_range("cor_field_batch");
     if (!ctx) return COR_ERR_INVALID;
     if (!model_set_ok(models))
         return fail(ctx, COR_ERR_UNSUPPORTED, "model set {%d,%d,%d} not available", models.internal_model,
