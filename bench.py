@@ -502,10 +502,12 @@ def run_reference(args, rank: int) -> dict | None:
             dt_tot += dt
             steps += 1
     v = done / dt_tot
-    return {"metric": METRIC, "value": v, "unit": UNIT, "n_gpus": 0, "steps": args.steps, "warmup": args.warmup,
-            "ms_per_step": dt_tot * 1e3 / max(1, steps), "higher_is_better": True, "scaling": "weak",
-            "vs_baseline": None, "dtype": "f64", "data": "synthetic grid of sites", "impl": "reference",
-            "config": {"workload": WORKLOAD, "sites_per_step": threads},
+    return {"metric": METRIC, "value": v, "unit": UNIT, "n_gpus": args.gpus, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": dt_tot * 1e3 / max(1, steps), "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic grid of sites",
+            "impl": "reference",
+            "config": {"workload": WORKLOAD, "sites_per_step": threads,
+                       "devices": "host cores of rank 0 only; no GPU work"},
             "cpu_baseline": {"value": v, "unit": UNIT, "cores": threads, "kind": "port",
                              "sample": f"{threads} sites x {N_RIG} rigidities per step, one site per thread"},
             "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
