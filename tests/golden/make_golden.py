@@ -9,7 +9,7 @@ and driven two ways:
     giving the printed rows and the CUTOFF line of whole rigidity scans.
 
 Run here (where the reference tree exists):  python tests/golden/make_golden.py [section ...]
-Sections: setup field scan0 scan_t96 scan_ts05 scan_chaos field_cli trajectory_cli nudge nudge_extra.  The fixtures are small JSON
+Sections: setup field scan0 scan_t96 scan_ts05 scan_chaos field_cli trajectory_cli cli_errors nudge nudge_extra.  The fixtures are small JSON
 files; nothing on the GPU side reads the reference.
 """
 from __future__ import annotations
@@ -316,6 +316,47 @@ def make_trajectory_cli() -> dict:
     return out
 
 
+OK_INFILE = infile(50.0, 15.0, 50.0, 15.0, 0.05, 20.0, 0.05, [2020, 1, 1, 1, 0, 0, 0])
+CLI_ERROR_CASES = [
+    # (name, args before the INFILE, INFILE text or None for a missing file)
+    ("unknown_internal", ["-i", "igrf99"], OK_INFILE),
+    ("unknown_external", ["-e", "t01"], OK_INFILE),
+    ("unknown_crustal", ["-c", "nochaos"], OK_INFILE),
+    ("bad_steps", ["-s", "abc"], OK_INFILE),
+    ("bad_tu", ["-u", "x"], OK_INFILE),
+    ("bad_mode", ["-m", "bogus"], OK_INFILE),
+    ("missing_infile", [], None),
+    ("empty_infile", [], ""),
+    ("truncated_infile", [], "0.05 1 20\n"),
+    ("zero_step", [], OK_INFILE.replace("100 0 0 0.05", "100 0 0 0")),
+    ("t96_without_parmod", ["-e", "t96"], OK_INFILE),
+    ("ts05_short_parmod", ["-e", "ts05"], OK_INFILE + "-20 2 0 -1\n1 1 1\n"),
+    ("trajectory_without_output", ["-m", "trajectory"], OK_INFILE),
+    ("trajectory_rigidity_range", ["-m", "trajectory", "-o", "out.txt"], OK_INFILE),
+    ("field_empty", ["-m", "field"], ""),
+    ("field_t96_without_parmod", ["-m", "field", "-e", "t96"], "1.0 -90 0\n10 10 90 360\n2020 1 1 1 0 0 0\n"),
+]
+
+
+def make_cli_errors() -> dict:
+    """The reference `cor` on malformed command lines and INFILEs: exit code,
+    stderr and stdout, for the drop-in CLI to reproduce (src/main.c:14-49,
+    src/args.c, src/io.c).  Every case is one the reference rejects."""
+    import subprocess
+    import tempfile
+    out = {}
+    for name, args, text in CLI_ERROR_CASES:
+        with tempfile.TemporaryDirectory() as td:
+            if text is not None:
+                with open(os.path.join(td, "t.in"), "w") as fh:
+                    fh.write(text)
+            r = subprocess.run([os.path.join(pyoracle.REF_DIR, "cor"), *args, "t.in"], cwd=td, capture_output=True,
+                               text=True, timeout=60)
+        assert r.returncode != 0, name
+        out[name] = {"args": args, "infile": text, "rc": r.returncode, "stderr": r.stderr, "stdout": r.stdout}
+    return out
+
+
 # ---- the reference's own sensitivity to a one-ulp libm change ------------------
 def _scan_agreement(g, res):
     """Flag agreement and sites within one step of a scan result vs a golden set."""
@@ -440,6 +481,7 @@ def main(sections):
         "scan_chaos": ("scan_chaos.json", make_scan_chaos),
         "field_cli": ("field_cli.json", make_field_cli),
         "trajectory_cli": ("trajectory_cli.json", make_trajectory_cli),
+        "cli_errors": ("cli_errors.json", make_cli_errors),
         "nudge": ("nudge_sensitivity.json", make_nudge),
         "nudge_extra": ("nudge_sensitivity.json", make_nudge_extra),
     }
