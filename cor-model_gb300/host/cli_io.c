@@ -10,7 +10,10 @@ int read_cutoff_infile_header(FILE *f, InfileHeader *h) {
     const int items = fscanf(f, "%lf %lf %lf\n%lf %lf %lf\n%lf %lf\n%d %d %d %d %d %d %d\n%d %d %d %lf", &h->rig,
                              &h->zn, &h->rk, &h->r0, &h->the0, &h->fi0, &h->the1, &h->fi1, &h->iy, &h->mes, &h->ide,
                              &h->id, &h->ih, &h->min, &h->is, &h->nk1, &h->iopt, &h->ist, &h->del);
-    return items < 0 ? -1 : 0;
+    /* The reference rejects only an empty file (items < 0); a header cut short
+     * leaves the rest of its stack struct unset and what follows depends on
+     * that memory.  Here every one of the 19 items is required. */
+    return items != 19 ? -1 : 0;
 }
 
 int write_cutoff_outfile_header(FILE *out, const InfileHeader *h, const Model **models, uint64_t steps_count) {
@@ -51,7 +54,7 @@ int read_field_infile_header(FILE *f, InfileHeader *h) {
     const int items = fscanf(f, "%lf %lf %lf\n%lf %lf %lf %lf\n%d %d %d %d %d %d %d\n", &h->r0, &h->the0, &h->fi0,
                              &h->lat_step, &h->lon_step, &h->the1, &h->fi1, &h->iy, &h->mes, &h->ide, &h->id, &h->ih,
                              &h->min, &h->is);
-    return items < 0 ? -1 : 0;
+    return items != 14 ? -1 : 0;  /* all 14 items, as for the cutoff header */
 }
 
 int write_field_outfile_header(FILE *out, const InfileHeader *h, const Model **models) {

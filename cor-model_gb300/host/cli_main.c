@@ -130,7 +130,7 @@ static int load_infile(const char *path, const Model **models, InfileHeader *h, 
 static int cutoff(const CLIArguments *args, const Model **models) {
     RunOptions o;
     if (run_options(args, &o)) return 1;
-    InfileHeader h;
+    InfileHeader h = {0};
     ModelsParams p;
     if (load_infile(args->input_file_name, models, &h, &p)) return 1;
     FILE *out = stdout;
@@ -161,7 +161,7 @@ static int field(const CLIArguments *args, const Model **models) {
         perror("Error: Cannot open input file for reading");
         return 1;
     }
-    InfileHeader h;
+    InfileHeader h = {0};
     ModelsParams p;
     memset(&h, 0, sizeof h);
     memset(&p, 0, sizeof p);
@@ -209,7 +209,7 @@ static int trajectory(const CLIArguments *args, const Model **models) {
         perror("Error: Cannot open input file for reading");
         return 1;
     }
-    InfileHeader h;
+    InfileHeader h = {0};
     ModelsParams p;
     memset(&h, 0, sizeof h);
     memset(&p, 0, sizeof p);

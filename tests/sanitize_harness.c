@@ -54,9 +54,11 @@ int main(void) {
     f = mem("");
     CHECK(read_cutoff_infile_header(f, &h) != 0, "empty cutoff INFILE accepted");
     fclose(f);
-    f = mem("0.05 1");
-    memset(&h, 0, sizeof h);
-    read_cutoff_infile_header(f, &h);        /* truncated: whatever it returns, no UB */
+    f = mem("0.05 1 20\n1.0031391260673028 50 15\n50 15\n2020 1 1\n");
+    CHECK(read_cutoff_infile_header(f, &h) != 0, "cutoff header cut short accepted");
+    fclose(f);
+    f = mem("1.0 -90 0\n10 10 90\n");
+    CHECK(read_field_infile_header(f, &h) != 0, "field header cut short accepted");
     fclose(f);
     f = mem("1.0 -90 0\n10 10 90 360\n2020 1 1 1 0 0 0\n");
     CHECK(read_field_infile_header(f, &h) == 0 && h.lat_step == 10. && h.fi1 == 360., "field header");
