@@ -16,7 +16,11 @@ the batch that completed it; results are per site-direction P(S), P(C), P(M),
 identical whether a request ran alone or in a mix (trajectories are
 independent and deterministic).
 
-    python cor-model_gb300/serve.py --rate 2 --requests 40 [--window FILE]
+With a request log (RequestLog) every queued, rejected and completed request
+is on disk, and a stopped server resumes from it without losing work (only
+the batches in flight at the stop run again).
+
+    python cor-model_gb300/serve.py --rate 2 --requests 40 [--window FILE] [--log FILE [--resume]]
 """
 from __future__ import annotations
 
@@ -107,6 +111,108 @@ def request_jobs(req: Request, param_index: int) -> np.ndarray:
     return np.concatenate(jobs)
 
 
+_REQ_FIELDS = ("rid", "arrival", "sites", "directions", "time7", "parmod", "external", "rig")
+_SITE_FLOATS = ("r_lower", "r_upper", "r_cutoff")
+_SITE_INTS = ("n_forbidden", "n_traj")
+
+
+def request_to_json(r: Request) -> dict:
+    return {k: getattr(r, k) for k in _REQ_FIELDS}
+
+
+def request_from_json(d: dict) -> Request:
+    return Request(d["rid"], d["arrival"], [tuple(s) for s in d["sites"]], [tuple(s) for s in d["directions"]],
+                   list(d["time7"]), list(d["parmod"]), d["external"], tuple(d["rig"]))
+
+
+def result_to_json(sites: np.ndarray) -> dict:
+    """Per site-direction results, floats as exact hex."""
+    out = {k: [float(v).hex() for v in sites[k]] for k in _SITE_FLOATS}
+    return out | {k: [int(v) for v in sites[k]] for k in _SITE_INTS}
+
+
+def result_from_json(d: dict) -> np.ndarray:
+    n = len(d["r_lower"])
+    sites = np.zeros(n, ct.SITE_DTYPE)
+    for k in _SITE_FLOATS:
+        sites[k] = [float.fromhex(v) for v in d[k]]
+    for k in _SITE_INTS:
+        sites[k] = d[k]
+    return sites
+
+
+class RequestLog:
+    """Append-only JSON-lines log of a server's requests, so that a server
+    that stopped (crash, restart, preemption) can be resumed without losing
+    work, re-running at most the batches that were in flight when it stopped
+    (their results are deterministic, so a re-run gives the same bytes).  One
+    "submit" line when a request is queued, one
+    "rejected" line when it is over the budget, one "done" line with its
+    result when the batch that held it completes.  Each line is written
+    whole, flushed and (durable=True) fsync'ed before the server moves on, so
+    the log never says more than happened; a torn last line, the mark of a
+    write cut off by the stop, is ignored by replay()."""
+
+    def __init__(self, path: str, durable: bool = True):
+        self.path = path
+        self.durable = durable
+        self.lock = threading.Lock()
+        torn = False
+        if os.path.exists(path) and os.path.getsize(path) > 0:
+            with open(path, "rb") as f:
+                f.seek(-1, os.SEEK_END)
+                torn = f.read(1) != b"\n"
+        self.f = open(path, "a", encoding="utf-8")
+        if torn:
+            self.f.write("\n")        # end the torn line so the next record starts clean
+
+    def _write(self, recs: list[dict]):
+        with self.lock:
+            self.f.write("".join(json.dumps(r, separators=(",", ":")) + "\n" for r in recs))
+            self.f.flush()
+            if self.durable:
+                os.fsync(self.f.fileno())
+
+    def submitted(self, req: Request):
+        self._write([{"event": "submit", "request": request_to_json(req)}])
+
+    def rejected(self, req: Request):
+        self._write([{"event": "rejected", "rid": req.rid}])
+
+    def completed(self, reqs: list[Request]):
+        self._write([{"event": "done", "rid": r.rid, "fallback": r.fallback, "result": result_to_json(r.result)}
+                     for r in reqs])
+
+    def close(self):
+        with self.lock:
+            self.f.close()
+
+    @staticmethod
+    def replay(path: str) -> tuple[dict, list[Request]]:
+        """-> ({rid: (result, fallback)} of the completed requests, the
+        requests submitted but neither completed nor rejected, in arrival
+        order).  Lines that do not parse (a torn write) are skipped."""
+        submitted, done, rejected = {}, {}, set()
+        if not os.path.exists(path):
+            return done, []
+        with open(path, encoding="utf-8") as f:
+            for line in f:
+                try:
+                    rec = json.loads(line)
+                    ev = rec["event"]
+                    if ev == "submit":
+                        req = request_from_json(rec["request"])
+                        submitted[req.rid] = req
+                    elif ev == "done":
+                        done[rec["rid"]] = (result_from_json(rec["result"]), rec["fallback"])
+                    elif ev == "rejected":
+                        rejected.add(rec["rid"])
+                except (ValueError, KeyError, TypeError):
+                    continue
+        pending = [r for rid, r in submitted.items() if rid not in done and rid not in rejected]
+        return done, sorted(pending, key=lambda r: r.arrival)
+
+
 def request_features(req: Request, params: np.ndarray) -> np.ndarray:
     tilt = window.dipole_tilt(params)
     ep = window.decimal_epoch(req.time7)
@@ -118,8 +224,9 @@ class Server:
     """Continuous batching over `slots` contexts under an HBM budget."""
 
     def __init__(self, device: int = 0, slots: int = 3, hbm_budget: float = 40e9, max_batch_traj: int = 2_000_000,
-                 window_model: window.WindowModel | None = None, executor=None):
+                 window_model: window.WindowModel | None = None, executor=None, log: RequestLog | None = None):
         self.budget = int(hbm_budget)
+        self.log = log
         self.in_flight = 0
         self.max_batch_traj = max_batch_traj
         self.window_model = window_model
@@ -160,11 +267,16 @@ class Server:
         return time.perf_counter() - self.t0
 
     def submit(self, req: Request):
-        with self.lock:
-            if req.device_bytes() > self.budget:
-                req.done_at = self.now()
+        if req.device_bytes() > self.budget:
+            req.done_at = self.now()
+            if self.log:
+                self.log.rejected(req)
+            with self.lock:
                 self.rejected.append(req)
-                return
+            return
+        if self.log:
+            self.log.submitted(req)       # logged before any slot can take it
+        with self.lock:
             self.waiting.append(req)
             self.lock.notify_all()
 
@@ -223,6 +335,8 @@ class Server:
                     r.fallback = int(fb[o:o + r.n_scans].sum())
                     r.done_at = t
                     o += r.n_scans
+                if self.log:
+                    self.log.completed(reqs)
             with self.lock:
                 self.in_flight -= sum(r.device_bytes() for r in batch)
                 self.batches += 1
@@ -249,6 +363,29 @@ def run_stream(server: Server, reqs: list[Request]) -> dict:
             "fallbacks": int(sum(r.fallback for r in reqs))}
 
 
+def resume(log_path: str, reqs: list[Request]) -> tuple[list[Request], list[Request]]:
+    """Splits a stream against the log of an earlier run of it -> (restored,
+    to_run).  Requests whose results the log holds get them back and are not
+    run again.  The rest are to run: first those the log shows queued but
+    unfinished (arrival 0: they are overdue), then those it never saw, their
+    arrivals shifted so that the first of them arrives at 0."""
+    done, pending = RequestLog.replay(log_path)
+    restored = []
+    for r in reqs:
+        if r.rid in done:
+            r.result, r.fallback = done[r.rid]
+            r.done_at = r.arrival
+            restored.append(r)
+    seen = set(done) | {r.rid for r in pending}
+    for r in pending:
+        r.arrival = 0.0
+    fresh = [r for r in reqs if r.rid not in seen]
+    t0 = min((r.arrival for r in fresh), default=0.0)
+    for r in fresh:
+        r.arrival -= t0
+    return restored, pending + fresh
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--rate", type=float, default=1.0, help="requests per second")
@@ -259,15 +396,26 @@ def main():
     ap.add_argument("--external", default="ts05", choices=["t96", "ts05"])
     ap.add_argument("--window", default=None, help="trained window model (train_window.py output)")
     ap.add_argument("--max-box-sites", type=int, default=16)
+    ap.add_argument("--log", default=None, help="request log (JSON lines) to append to")
+    ap.add_argument("--resume", action="store_true",
+                    help="with --log: take the results the log holds and run only what it shows unfinished")
     args = ap.parse_args()
     ext = ct.EXTERNAL_TS05 if args.external == "ts05" else ct.EXTERNAL_T96
     reqs = poisson_stream(args.seed, args.rate, args.requests, ext, args.max_box_sites)
+    restored = []
+    if args.resume:
+        if not args.log:
+            ap.error("--resume needs --log")
+        restored, reqs = resume(args.log, reqs)
     wm = window.WindowModel(args.window) if args.window else None
-    srv = Server(0, args.slots, args.budget_gb * 1e9, window_model=wm)
+    log = RequestLog(args.log) if args.log else None
+    srv = Server(0, args.slots, args.budget_gb * 1e9, window_model=wm, log=log)
     out = run_stream(srv, reqs)
     out.update({"rate": args.rate, "seed": args.seed, "slots": args.slots, "external": args.external,
-                "window": bool(args.window)})
+                "window": bool(args.window), "restored_from_log": len(restored)})
     print(json.dumps(out), flush=True)
+    if log:
+        log.close()
     if wm:
         wm.close()
 

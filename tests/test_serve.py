@@ -79,3 +79,69 @@ def test_request_over_budget_is_rejected():
     budget = min(r.device_bytes() for r in reqs) - 1
     out, _, srv = _run(reqs, budget=budget)
     assert out["rejected"] == 3 and out["completed"] == 0
+
+
+def _run_logged(reqs, log_path, durable=False):
+    ref = [None]
+    log = serve.RequestLog(str(log_path), durable=durable)
+    srv = serve.Server(slots=2, executor=_Oracle(ref), log=log)
+    ref[0] = srv
+    out = serve.run_stream(srv, reqs)
+    log.close()
+    return out
+
+
+def test_request_log_resumes_a_stopped_server(tmp_path):
+    """A log cut as if the server had stopped: requests 0-5 queued, the even
+    ones finished, a torn "done" line at the end, requests 6-7 never seen.
+    Resuming restores the finished results, runs the rest, and every result
+    equals the uninterrupted run's bit for bit."""
+    import json
+    reqs = _small(serve.poisson_stream(13, 500.0, 8, max_box_sites=4))
+    full = tmp_path / "full.jsonl"
+    out = _run_logged(reqs, full)
+    assert out["completed"] == 8
+    done, pending = serve.RequestLog.replay(str(full))
+    assert sorted(done) == list(range(8)) and pending == []
+    for r in reqs:
+        assert np.array_equal(done[r.rid][0].view(np.uint8), r.result.view(np.uint8))
+
+    keep, torn = [], None
+    for line in full.read_text().splitlines():
+        rec = json.loads(line)
+        rid = rec["request"]["rid"] if rec["event"] == "submit" else rec["rid"]
+        if rid >= 6:
+            continue
+        if rec["event"] == "done" and rid % 2:
+            torn = torn or line[:len(line) // 2]
+            continue
+        keep.append(line)
+    stopped = tmp_path / "stopped.jsonl"
+    stopped.write_text("\n".join(keep) + "\n" + torn)
+
+    fresh = _small(serve.poisson_stream(13, 500.0, 8, max_box_sites=4))
+    restored, todo = serve.resume(str(stopped), fresh)
+    assert sorted(r.rid for r in restored) == [0, 2, 4]
+    assert [r.rid for r in todo][:3] == [1, 3, 5] and all(r.arrival == 0.0 for r in todo[:3])
+    assert sorted(r.rid for r in todo[3:]) == [6, 7] and min(r.arrival for r in todo[3:]) == 0.0
+    out2 = _run_logged(todo, stopped, durable=True)
+    assert out2["completed"] == 5
+    by_rid = {r.rid: r for r in restored + todo}
+    for r in reqs:
+        assert np.array_equal(by_rid[r.rid].result.view(np.uint8), r.result.view(np.uint8)), r.rid
+    done2, pending2 = serve.RequestLog.replay(str(stopped))
+    assert sorted(done2) == list(range(8)) and pending2 == []
+
+
+def test_rejected_requests_are_not_owed_after_a_stop(tmp_path):
+    reqs = _small(serve.poisson_stream(11, 100.0, 3, max_box_sites=4))
+    log = tmp_path / "log.jsonl"
+    ref = [None]
+    srv = serve.Server(slots=1, hbm_budget=min(r.device_bytes() for r in reqs) - 1, executor=_Oracle(ref),
+                       log=serve.RequestLog(str(log)))
+    ref[0] = srv
+    out = serve.run_stream(srv, reqs)
+    srv.log.close()
+    assert out["rejected"] == 3
+    done, pending = serve.RequestLog.replay(str(log))
+    assert done == {} and pending == []
