@@ -2,6 +2,8 @@
 pinned against golden fixtures made by the reference itself."""
 from __future__ import annotations
 
+import os
+
 import numpy as np
 import pytest
 
@@ -81,6 +83,36 @@ def test_oracle_scan_matches_reference_config0_subset():
         st = res.status[res.offsets[j]:res.offsets[j + 1]]
         allowed = np.nonzero(st == ct.TRAJ_ALLOWED)[0].tolist()
         assert allowed == s["allowed"], (s["lat"], s["lon"])
+        site = res.sites[j]
+        assert [fmt5(site["r_lower"]), fmt5(site["r_upper"]), fmt5(site["r_cutoff"])] == s["cutoff"]
+
+
+EXT_SCANS = {
+    "scan_t96.json": (ct.INTERNAL_SH, ct.EXTERNAL_T96, ct.CRUSTAL_NONE, 4),
+    "scan_ts05.json": (ct.INTERNAL_SH, ct.EXTERNAL_TS05, ct.CRUSTAL_NONE, 4),
+    "scan_chaos.json": (ct.INTERNAL_SH, ct.EXTERNAL_NONE, ct.CRUSTAL_CHAOS, 2),
+}
+
+
+@pytest.mark.parametrize("name", sorted(EXT_SCANS))
+def test_oracle_scan_with_external_and_crustal_fields_matches_reference(name):
+    """The oracle, built with the reference's compiler flags against the same C
+    library, gives the reference's own allowed/forbidden flags and P(S)/P(C)/P(M)
+    lines on the T96, TS05 and CHAOS scan fixtures: every stride-th site by
+    default, every site with COR_ORACLE_ALL_SITES=1 (200 + 200 + 12 sites, a
+    few minutes on 8 threads)."""
+    internal, external, crustal, stride = EXT_SCANS[name]
+    if os.environ.get("COR_ORACLE_ALL_SITES") == "1":
+        stride = 1
+    g = golden(name)
+    sites = g["sites"][::stride]
+    p = ct.internal_setup(g["model"], g["time"], parmod=g.get("parmod"))
+    jobs = config0_jobs(sites, g["rig"], g["rk"], g["del"])
+    res = pyoracle.scan_batch(jobs, p, models=ct.model_set(internal, external, crustal), threads=8,
+                              step_limit=g.get("step_limit", 25000))
+    for j, s in enumerate(sites):
+        st = res.status[res.offsets[j]:res.offsets[j + 1]]
+        assert np.nonzero(st == ct.TRAJ_ALLOWED)[0].tolist() == s["allowed"], (s["lat"], s["lon"])
         site = res.sites[j]
         assert [fmt5(site["r_lower"]), fmt5(site["r_upper"]), fmt5(site["r_cutoff"])] == s["cutoff"]
 
