@@ -385,6 +385,13 @@ extern "C" int cor_batch_count(const cor_scan_job* jobs, int32_t n_jobs, uint64_
     for (int32_t j = 0; j < n_jobs; j++) {
         const cor_scan_job& jb = jobs[j];
         if (!(jb.del > 0.) || !isfinite(jb.rig) || !isfinite(jb.rk)) return COR_ERR_INVALID;
+        // The step loop needs a positive nk1 (the turn-angle halving doubles
+        // nk0 while nk0 <= 50000) and a finite, non-zero charge and start
+        // vectors; the reference does not check these and runs on with
+        // inf/NaN or wrapped integers.
+        if (jb.nk1 <= 0 || !(jb.zn != 0.) || !isfinite(jb.zn) || !isfinite(jb.r0) || !isfinite(jb.the0) ||
+            !isfinite(jb.fi0) || !isfinite(jb.the1) || !isfinite(jb.fi1))
+            return COR_ERR_INVALID;
         // src/trajectory.c:7,12: i = 0 .. (int)round((rk-rig)/del)
         const double nr = round((jb.rk - jb.rig) / jb.del);
         if (!(nr >= 0.) || nr > 1e8) return COR_ERR_INVALID;
@@ -791,7 +798,7 @@ extern "C" int cor_trace_batch(cor_ctx* ctx, const cor_batch_req* req, cor_batch
     if (rc != COR_OK) {
         free(offsets);
         free(trig);
-        return fail(ctx, rc, "invalid rigidity grid in a job");
+        return fail(ctx, rc, "invalid job: rigidity grid or window, nk1 <= 0, zero charge or non-finite start");
     }
     cudaStream_t s = ctx->stream;
     do {
@@ -839,7 +846,7 @@ extern "C" int cor_trace_steps(cor_ctx* ctx, const cor_batch_req* req, cor_batch
     if (!steps || step_capacity == 0) return fail(ctx, COR_ERR_INVALID, "no step record buffer");
     uint64_t n_traj = 0;
     if (cor_batch_count(req->jobs, req->n_jobs, &n_traj, nullptr) != COR_OK)
-        return fail(ctx, COR_ERR_INVALID, "invalid rigidity grid in a job");
+        return fail(ctx, COR_ERR_INVALID, "invalid job: rigidity grid or window, nk1 <= 0, zero charge or non-finite start");
     const size_t bytes = sizeof(cor_step_record) * (size_t)n_traj * step_capacity;
     CUDA_TRY(ctx, cudaSetDevice(ctx->device));
     int rc = ensure(ctx, ctx->steps, bytes ? bytes : 1);

@@ -95,8 +95,8 @@ typedef struct {
     double rig;    /* first rigidity [GV]                             */
     double del;    /* rigidity step [GV], > 0                         */
     double rk;     /* last rigidity [GV]                              */
-    double zn;     /* charge number                                   */
-    int32_t nk1;   /* steps per gyro period (initial)                 */
+    double zn;     /* charge number, non-zero                         */
+    int32_t nk1;   /* steps per gyro period (initial), > 0            */
     int32_t param_index; /* which cor_model_params block this scan uses */
     int32_t i_first; /* first grid index traced (0: from the grid's start) */
     int32_t i_count; /* indices traced (0: to the grid's end)             */
@@ -240,9 +240,10 @@ int cor_ctx_set_queue_order(cor_ctx *ctx, int32_t rigidity_major);
 int cor_upload_crustal(cor_ctx *ctx, const double *g, const double *h, int32_t nmax);
 
 /* Same scan with every buffer already in device memory (jobs, trig from
- * cor_prepare_trig, offsets from cor_batch_count, sites, status, records) and
- * the parameter blocks of the last cor_upload_params; `stream` is a
- * cudaStream_t (NULL = the legacy default stream).  The scan runs in
+ * cor_prepare_trig, offsets from cor_batch_count, sites, status, records),
+ * using the parameter blocks of the last cor_upload_params.  The jobs are not
+ * checked again here: they must be ones that cor_batch_count accepted.
+ * `stream` is a cudaStream_t (NULL = the legacy default stream).  The scan runs in
  * generations: between two of them the host reads how many trajectories the
  * kernel parked for regrouping, so the call synchronises `stream` a few
  * times and returns with the last generation and the reduction queued.

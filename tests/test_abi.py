@@ -52,6 +52,21 @@ def test_batch_count_rejects_bad_grid():
         ct.batch_offsets(ct.make_job(0, 0, rig=20.0, rk=0.05, dele=0.05))
 
 
+def test_batch_count_rejects_jobs_the_step_loop_cannot_run():
+    """nk1 <= 0 (the turn-angle halving doubles nk0 while nk0 <= 50000), a
+    zero charge and non-finite start values are rejected before any device
+    work; negative charges are valid."""
+    for bad in (dict(nk1=0), dict(nk1=-100), dict(zn=0.0), dict(zn=float("nan")), dict(r0=float("inf"))):
+        with pytest.raises(ct.CorError):
+            ct.batch_offsets(ct.make_job(50.0, 15.0, **bad))
+    j = ct.make_job(50.0, 15.0)
+    j["the1"] = float("nan")
+    with pytest.raises(ct.CorError):
+        ct.batch_offsets(j)
+    n, _ = ct.batch_offsets(ct.make_job(50.0, 15.0, zn=-1.0, nk1=1))
+    assert n == 400
+
+
 def test_prepare_trig_uses_host_libm():
     j = ct.make_job(50.0, 15.0)
     t = ct.prepare_trig(j)[0]
