@@ -871,6 +871,9 @@ extern "C" int cor_field_batch(cor_ctx* ctx, cor_model_set models, const cor_mod
                     models.external_model, models.crustal_model);
     if (n < 0 || n_params < 1 || !params || (n > 0 && (!gsm_pos || !geo_field)))
         return fail(ctx, COR_ERR_INVALID, "bad field request");
+    for (int64_t i = 0; param_index && i < n; i++)
+        if (param_index[i] < 0 || param_index[i] >= n_params)
+            return fail(ctx, COR_ERR_INVALID, "point %lld: param_index %d out of range", (long long)i, param_index[i]);
     if (n == 0) return COR_OK;
     CUDA_TRY(ctx, cudaSetDevice(ctx->device));
     cudaStream_t s = ctx->stream;

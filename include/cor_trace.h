@@ -317,7 +317,8 @@ int cor_trace_steps(cor_ctx *ctx, const cor_batch_req *req, cor_batch_result *ou
 /* ---- field ------------------------------------------------------------ */
 /* calculate_field (src/models.c:194-207) at n points: gsm_pos is n x 3 GSM
  * positions in metres; geo_field gets n x 3 GEO field components in nT.
- * param_index gives, per point, the parameter block (NULL = block 0). */
+ * param_index gives, per point, the parameter block (NULL = block 0); an
+ * index outside 0 .. n_params-1 gives COR_ERR_INVALID before any GPU work. */
 int cor_field_batch(cor_ctx *ctx, cor_model_set models,
                     const cor_model_params *params, int32_t n_params,
                     const int32_t *param_index, const double *gsm_pos,
