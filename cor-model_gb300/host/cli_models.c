@@ -31,7 +31,7 @@ const Model *get_model(const Model **models, const char *version) {
     return NULL;
 }
 
-/* The setup_fun loop of cutoff() (src/main.c:52-62): internal_recalc for the
+/* The setup_fun loop of cutoff() (src/main.c:51-61): internal_recalc for the
  * internal model, PARMOD from the INFILE for the external one.  Without an
  * internal model the GSM axes come from the IGRF-14 dipole at the date (the
  * reference leaves them uninitialised, src/main.c:51). */

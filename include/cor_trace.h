@@ -166,13 +166,22 @@ typedef struct {
 typedef struct cor_ctx cor_ctx;
 
 /* ---- context ---------------------------------------------------------- */
+/* No counterpart in the reference, which keeps no state between INFILEs and
+ * reports errors by printing to stderr and returning 1 from main
+ * (src/main.c:14-49).  A context holds one device's stream, the resident
+ * parameter blocks and crustal table, and reusable buffers; every call on it
+ * sets the string cor_last_error_string returns when it fails. */
 int cor_ctx_create(int device, cor_ctx **out);
 int cor_ctx_destroy(cor_ctx *ctx);
 const char *cor_last_error_string(const cor_ctx *ctx);
 int cor_abi_version(void);
 
 /* Number of trajectories of a batch and, optionally, the exclusive prefix
- * offsets of each job's trajectories (offsets has n_jobs+1 entries). */
+ * offsets of each job's trajectories (offsets has n_jobs+1 entries).  A scan
+ * has (int)round((rk-rig)/del)+1 of them, as the loop of src/trajectory.c:7,12
+ * counts, or i_count for a window.  Also the one check of every job: it
+ * returns COR_ERR_INVALID for a bad grid or window, nk1 <= 0, a zero charge
+ * or a non-finite start value. */
 int cor_batch_count(const cor_scan_job *jobs, int32_t n_jobs,
                     uint64_t *n_trajectories, uint64_t *offsets);
 
@@ -200,8 +209,10 @@ int cor_trace_batch(cor_ctx *ctx, const cor_batch_req *req, cor_batch_result *ou
 
 /* Uploads n_params parameter blocks to the device, where they stay for the
  * following cor_trace_batch_device calls (cor_trace_batch uploads its own).
- * Per-condition constants of the external models are derived here on the
- * host. */
+ * Each block is the ModelsParams the reference passes to
+ * trajectory_simulation_cutoff (src/models.h:9-17, filled by the setup_fun
+ * loop of src/main.c:51-61).  Per-condition constants of the external models
+ * are derived here on the host. */
 int cor_upload_params(cor_ctx *ctx, const cor_model_params *params, int32_t n_params);
 
 /* Regrouping of the scan kernel on this context (no counterpart in the
@@ -239,7 +250,8 @@ int cor_ctx_set_queue_order(cor_ctx *ctx, int32_t rigidity_major);
  * has no counterpart: its table is a compile-time constant. */
 int cor_upload_crustal(cor_ctx *ctx, const double *g, const double *h, int32_t nmax);
 
-/* Same scan with every buffer already in device memory (jobs, trig from
+/* trajectory_simulation_cutoff (src/trajectory.c:6-161), as cor_trace_batch,
+ * with every buffer already in device memory (jobs, trig from
  * cor_prepare_trig, offsets from cor_batch_count, sites, status, records),
  * using the parameter blocks of the last cor_upload_params.  The jobs are not
  * checked again here: they must be ones that cor_batch_count accepted.
@@ -304,7 +316,8 @@ typedef struct {
     uint32_t reserved;
 } cor_step_record;
 
-/* Traces every rigidity of the jobs like cor_trace_batch and also records
+/* Replaces trajectory_simulation (src/trajectory.c:163-273, `cor -m
+ * trajectory`).  Traces every rigidity of the jobs like cor_trace_batch and also records
  * each accepted step: trajectory t (in batch order) writes its steps 1..k to
  * steps[t * step_capacity .. t * step_capacity + k - 1] for k up to
  * step_capacity (steps beyond the capacity are traced but not recorded).
