@@ -9,7 +9,7 @@ and driven two ways:
     giving the printed rows and the CUTOFF line of whole rigidity scans.
 
 Run here (where the reference tree exists):  python tests/golden/make_golden.py [section ...]
-Sections: setup field scan0 scan_t96 scan_ts05 scan_chaos field_cli trajectory_cli cli_errors nudge nudge_extra.  The fixtures are small JSON
+Sections: setup field field_storm scan0 scan_t96 scan_ts05 scan_chaos scan_storm field_cli trajectory_cli cli_errors nudge nudge_extra.  The fixtures are small JSON
 files; nothing on the GPU side reads the reference.
 """
 from __future__ import annotations
@@ -177,6 +177,42 @@ def make_field(lib) -> dict:
     return out
 
 
+def make_field_storm(lib) -> dict:
+    """T96 and TS05, alone and composed with IGRF-14 by calculate_field, at
+    seeded storm-range conditions (window.sample_conditions: the ranges the
+    learned window is trained on and the serving streams use), 8 conditions
+    per model, 40 points each."""
+    import window
+    rng = np.random.default_rng(20241203)
+    out = {}
+    for name, fn, emod in (("t96", lib.t96_gsm, "t96"), ("ts05", lib.ts05_gsm, "ts05")):
+        cases = []
+        for cond in window.sample_conditions(rng, 8, name):
+            pmod = np.zeros(10)
+            pmod[:len(cond["parmod"])] = cond["parmod"]
+            pts = field_points(rng, 40, 1.0, 25.0)
+            b = np.zeros(3)
+            vals = []
+            for x, y, z in pts:
+                fn(pmod.ctypes.data, x, y, z, b[0:].ctypes.data, b[1:].ctypes.data, b[2:].ctypes.data)
+                vals.append(b.copy())
+            pp = ref_setup(lib, "igrf14", cond["time7"])
+            pp["parmod"][0] = pmod
+            models = (C.c_void_p * 3)()
+            models[0] = lib.get_model(sym(lib, "internal_models"), b"igrf14")
+            models[1] = lib.get_model(sym(lib, "external_models"), emod.encode())
+            pts_m = field_points(rng, 40, 1.0, 25.0) * ct.DEF_RE
+            o = Vector()
+            comp = []
+            for x, y, z in pts_m:
+                lib.calculate_field(Vector(x, y, z), C.byref(o), C.addressof(models), pp.ctypes.data)
+                comp.append([o.x, o.y, o.z])
+            cases.append({"time": cond["time7"], "parmod": hx(pmod), "points": hx(pts), "b": hx(vals),
+                          "points_m": hx(pts_m), "b_composed": hx(comp)})
+        out[name] = cases
+    return out
+
+
 # ---- whole scans through the reference binary ------------------------------
 def infile(lat, lon, the1, fi1, rig, rk, dele, time7, nk1=100, r0=1.0031391260673028, ext_lines=()):
     lines = [f"{rig!r} 1 {rk!r}", f"{r0!r} {lat!r} {lon!r}", f"{the1!r} {fi1!r}",
@@ -250,6 +286,31 @@ def make_scan_ext(kind: str, n_sites: int = 200, rig: float = 0.05, dele: float 
     return {"config": f"IGRF-14 + {kind.upper()} at 2020-06-21 12 UT, vertical, 20 km, 20 -> {rig} GV by {dele}",
             "rig": rig, "rk": 20.0, "del": dele, "time": t7, "model": "igrf14", "external": kind,
             "parmod": pm, "sites": recs}
+
+
+def make_scan_storm(n_cond: int = 4, n_sites: int = 6, rig: float = 0.1, dele: float = 0.1) -> dict:
+    """IGRF-14 + TS05 scans at seeded storm-range conditions
+    (window.sample_conditions), sites uniform on the sphere, arriving
+    vertically or at 30 deg zenith (window.arrival_direction), like the storm
+    configuration's site-directions."""
+    import window
+    rng = np.random.default_rng(20241204)
+    dirs = [(0.0, 0.0), (30.0, 90.0), (30.0, 225.0)]
+    out = []
+    for c in window.sample_conditions(rng, n_cond, "ts05"):
+        pm = [float(v) for v in c["parmod"]]
+        ext = [f"{pm[1]!r} {pm[0]!r} {pm[2]!r} {pm[3]!r}", " ".join(repr(w) for w in pm[4:10])]  # src/io.c:98-113
+        sites = []
+        for k in range(n_sites):
+            lat = float(np.degrees(np.arcsin(rng.uniform(-1, 1))))
+            lon = float(rng.uniform(0, 360))
+            the1, fi1 = window.arrival_direction(lat, lon, *dirs[k % len(dirs)])
+            sites.append((lat, lon, float(the1), float(fi1)))
+        recs = run_scan_set(sites, rig, 20.0, dele, c["time7"], ["-i", "igrf14", "-e", "ts05"], ext_lines=ext)
+        out.append({"time": c["time7"], "parmod": pm, "sites": recs})
+    return {"config": f"IGRF-14 + TS05 at seeded storm conditions, 20 km, vertical and 30 deg zenith, "
+                      f"{rig} -> 20 GV by {dele}",
+            "rig": rig, "rk": 20.0, "del": dele, "model": "igrf14", "external": "ts05", "conditions": out}
 
 
 def make_scan_chaos(n_sites: int = 12) -> dict:
@@ -475,10 +536,12 @@ def main(sections):
     todo = {
         "setup": ("setup_params.json", lambda: make_setup(lib)),
         "field": ("field_kats.json", lambda: make_field(lib)),
+        "field_storm": ("field_storm.json", lambda: make_field_storm(lib)),
         "scan0": ("scan_config0.json", make_scan0),
         "scan_t96": ("scan_t96.json", lambda: make_scan_ext("t96")),
         "scan_ts05": ("scan_ts05.json", lambda: make_scan_ext("ts05")),
         "scan_chaos": ("scan_chaos.json", make_scan_chaos),
+        "scan_storm": ("scan_storm.json", make_scan_storm),
         "field_cli": ("field_cli.json", make_field_cli),
         "trajectory_cli": ("trajectory_cli.json", make_trajectory_cli),
         "cli_errors": ("cli_errors.json", make_cli_errors),

@@ -117,6 +117,23 @@ def test_oracle_scan_with_external_and_crustal_fields_matches_reference(name):
         assert [fmt5(site["r_lower"]), fmt5(site["r_upper"]), fmt5(site["r_cutoff"])] == s["cutoff"]
 
 
+def test_oracle_scans_match_reference_at_storm_conditions():
+    """IGRF-14 + TS05 at 4 seeded storm-range conditions, 6 site-directions
+    each (vertical and 30 deg zenith): the reference's own flags and
+    P(S)/P(C)/P(M) lines."""
+    g = golden("scan_storm.json")
+    models = ct.model_set(ct.INTERNAL_SH, ct.EXTERNAL_TS05)
+    for c in g["conditions"]:
+        p = ct.internal_setup(g["model"], c["time"], parmod=c["parmod"])
+        jobs = config0_jobs(c["sites"], g["rig"], g["rk"], g["del"])
+        res = pyoracle.scan_batch(jobs, p, models=models, threads=8)
+        for j, s in enumerate(c["sites"]):
+            st = res.status[res.offsets[j]:res.offsets[j + 1]]
+            assert np.nonzero(st == ct.TRAJ_ALLOWED)[0].tolist() == s["allowed"], (c["time"], s["lat"], s["lon"])
+            site = res.sites[j]
+            assert [fmt5(site["r_lower"]), fmt5(site["r_upper"]), fmt5(site["r_cutoff"])] == s["cutoff"]
+
+
 def test_oracle_flop_model():
     """The op-count model of the SH field follows the degree truncation."""
     assert pyoracle.internal_geo_flops(1.5) > pyoracle.internal_geo_flops(2.5) > pyoracle.internal_geo_flops(20.0)
@@ -152,6 +169,27 @@ def test_oracle_calculate_field_external_bit_exact():
         want = unhex(case["b"]).reshape(-1, 3)
         got = pyoracle.calculate_field(pts, p, models=ct.model_set(ct.INTERNAL_SH, ext))
         assert np.array_equal(got.view(np.uint64), want.view(np.uint64)), key
+
+
+@pytest.mark.parametrize("model", ["t96", "ts05"])
+def test_oracle_external_fields_bit_exact_at_storm_conditions(model):
+    """T96 / TS05 alone and composed with IGRF-14 at 8 seeded storm-range
+    conditions each (Pdyn to 10 nPa, Dst to -300 nT, IMF to +-20 nT, W to 5):
+    the oracle equals the reference bit for bit."""
+    lib = pyoracle.load()
+    fn = lib.orc_t96_gsm if model == "t96" else lib.orc_ts05_gsm
+    ext = ct.EXTERNAL_T96 if model == "t96" else ct.EXTERNAL_TS05
+    for case in golden("field_storm.json")[model]:
+        pm = unhex(case["parmod"])
+        want = unhex(case["b"]).reshape(-1, 3)
+        b = np.zeros(3)
+        for i, (x, y, z) in enumerate(unhex(case["points"]).reshape(-1, 3)):
+            fn(pm.ctypes.data, x, y, z, b[0:].ctypes.data, b[1:].ctypes.data, b[2:].ctypes.data)
+            assert np.array_equal(b.view(np.uint64), want[i].view(np.uint64)), (model, case["time"], i)
+        p = ct.internal_setup("igrf14", case["time"], parmod=pm)
+        got = pyoracle.calculate_field(unhex(case["points_m"]).reshape(-1, 3), p, models=ct.model_set(ct.INTERNAL_SH, ext))
+        want = unhex(case["b_composed"]).reshape(-1, 3)
+        assert np.array_equal(got.view(np.uint64), want.view(np.uint64)), (model, case["time"])
 
 
 def test_oracle_calculate_field_crustal_bit_exact():
