@@ -162,7 +162,7 @@ static __device__ __noinline__ Vec3 t96_intercon(const double x, const double y,
     return {bx, by, bz};
 }
 
-// shlcar3x3_t96, :500-617, for shield table t (0 ARC, 1 ATAIL2, 2 ATAIL3)
+// shlcar3x3_t96, :501-617, for shield table t (0 ARC, 1 ATAIL2, 2 ATAIL3)
 static __device__ __noinline__ Vec3 t96_shlcar3x3(const int t, const double x, const double y, const double z) {
     double sz[3], cz[3];
 #pragma unroll
@@ -352,7 +352,7 @@ static __device__ __noinline__ Vec3 t96_crosslp(const double x, const double y, 
     return {b1.x + b2.x, (b1.y + b2.y) * cal + (b1.z - b2.z) * sal, -(b1.y - b2.y) * sal + (b1.z + b2.z) * cal};
 }
 
-// dipxyz, :909-928 -> the field of unit x, y and z dipoles
+// dipxyz, :907-927 -> the field of unit x, y and z dipoles
 struct Dip3 {
     Vec3 dx, dy, dz;
 };
@@ -625,7 +625,7 @@ static __device__ __noinline__ Vec3 t96_birk2shl(const double x, const double y,
     return {hx, hy, hz};
 }
 
-// xksi and tksi, :1595-1643
+// xksi and tksi, :1587-1643
 __device__ __forceinline__ double t96_xksi(const double x, const double y, const double z) {
     const double x2 = x * x, y2 = y * y, z2 = z * z;
     const double r2 = x2 + y2 + z2;
@@ -664,7 +664,7 @@ __device__ __forceinline__ double t96_tksi(const double xk, const double x0, con
     return 1.0 + 1.5 * br3 / (tdz3 - br3);
 }
 
-// loops4, :1445-1509, fixed tilt index il into c_t96.loop_cs
+// loops4, :1415-1470, fixed tilt index il into c_t96.loop_cs
 static __device__ __noinline__ Vec3 t96_loops4(const double x, const double y, const double z, const double xc,
                                           const double yc, const double zc, const double R, const int il) {
     const double st = c_t96.loop_cs[il][0], ct = c_t96.loop_cs[il][1];
@@ -778,7 +778,7 @@ static __device__ __noinline__ Vec3 t96_r2inner(const double x, const double y, 
             bz + 29.9996 * d6.z + 262.886 * d7.z + 99.9132 * d8.z};
 }
 
-// r2outer, :1394-1414
+// r2outer, :1396-1413
 static __device__ __noinline__ Vec3 t96_r2outer(const double x, const double y, const double z) {
     const Vec3 d1 = t96_crosslp(x, y, z, 0.55, 0.694, 1);
     const Vec3 d2 = t96_crosslp(x, y, z, 1.55, 2.8, 2);
@@ -790,7 +790,18 @@ static __device__ __noinline__ Vec3 t96_r2outer(const double x, const double y, 
             -34.105 * d1.z + -2.00019 * d2.z + 628.639 * d3.z + 73.4847 * d4.z + 12.5162 * d5.z};
 }
 
-// r2sheet, :1511-1593, with xksi passed in (the reference evaluates the same
+// u^5 in the T3 terms of r2sheet.  The reference takes pow(u, 5)
+// (:1479,1483,1487); four multiplications replace three pow calls per field
+// evaluation here.  A build that defines COR_T96_POW5 takes the reference's
+// pow instead: the host build of this file does, to check the rest of the
+// model against the reference bit for bit.
+#ifdef COR_T96_POW5
+#define T96_POW5(u) ol_pow((u), 5)
+#else
+#define T96_POW5(u) ((u) * (u) * (u) * (u) * (u))
+#endif
+
+// r2sheet, :1472-1586, with xksi passed in (the reference evaluates the same
 // xksi(X, Y, Z) again).
 static __device__ __noinline__ Vec3 t96_r2sheet(const double x, const double y, const double z, const double xks) {
     constexpr double CX[5][4][4] = {
@@ -832,19 +843,19 @@ static __device__ __noinline__ Vec3 t96_r2sheet(const double x, const double y, 
     const double qx = sqrt(xks2 + px72);
     const double t2x = (px72 * 0.396953e-01) / (qx * qx * qx);
     const double ux = sqrt(xks2 + 0.579023e-01 * 0.579023e-01);
-    const double t3x = xks / (ux * ux * ux * ux * ux) * 3.493856 * c_t96.r2s_k[5];
+    const double t3x = xks / T96_POW5(ux) * 3.493856 * c_t96.r2s_k[5];
     const double t1y = xks / sqrt(xks2 + 0.478750e-01 * 0.478750e-01);
     const double py72 = 0.363750e-01 * 0.363750e-01;
     const double qy = sqrt(xks2 + py72);
     const double t2y = (py72 * 0.363750e-01) / (qy * qy * qy);
     const double uy = sqrt(xks2 + 0.567500e-01 * 0.567500e-01);
-    const double t3y = xks / (uy * uy * uy * uy * uy) * 3.493856 * c_t96.r2s_k[6];
+    const double t3y = xks / T96_POW5(uy) * 3.493856 * c_t96.r2s_k[6];
     const double t1z = xks / sqrt(xks2 + 0.355625e-01 * 0.355625e-01);
     const double pz72 = 0.318750e-01 * 0.318750e-01;
     const double qz = sqrt(xks2 + pz72);
     const double t2z = (pz72 * 0.318750e-01) / (qz * qz * qz);
     const double uz = sqrt(xks2 + 0.538750e-01 * 0.538750e-01);
-    const double t3z = xks / (uz * uz * uz * uz * uz) * 3.493856 * c_t96.r2s_k[7];
+    const double t3z = xks / T96_POW5(uz) * 3.493856 * c_t96.r2s_k[7];
     const double rho2 = x * x + y * y;
     const double r = sqrt(rho2 + z * z);
     const double rho = sqrt(rho2);

@@ -1,0 +1,160 @@
+"""The device field code and RK step of libcortrace, compiled as host C++
+(tests/device_on_host/) with the reference's floating-point flags and the host
+C library, against the reference's own field vectors.
+
+On the GPU the field models call CUDA's transcendental functions, and the
+external- and crustal-field units are compiled with FMA contraction; both
+change last bits, so the GPU tests hold T96/TS05 to the reference's own
+one-ulp sensitivity.  Here both are taken away: the same expression trees are
+evaluated with glibc and without contraction, so they must give the
+reference's bits.  With COR_T96_POW5 (the reference's pow(u, 5) in r2sheet)
+every golden field vector is reproduced bit for bit: IGRF, T96 and TS05,
+alone and composed, at the quiet and the storm-range conditions.  The default
+build, which multiplies u out, differs only in T96, by a few ulp.  No GPU."""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import shutil
+import subprocess
+
+import numpy as np
+import pytest
+
+from conftest import ROOT, golden, unhex
+import cortrace as ct
+import pyoracle
+
+SRC = os.path.join(ROOT, "tests", "device_on_host", "field_host.cpp")
+# the reference's flags (CMakeLists.txt:17, without -march=native)
+FLAGS = ["-std=c++17", "-O3", "-fno-math-errno", "-fno-trapping-math", "-ffp-contract=off", "-fPIC", "-shared",
+         "-Wno-unknown-pragmas"]
+
+
+def _build(out_dir, defines=()) -> C.CDLL:
+    so = os.path.join(out_dir, "field_host%s.so" % ("".join(d.lower() for d in defines)))
+    r = subprocess.run(["g++", *FLAGS, *[f"-D{d}" for d in defines], SRC, "-o", so, "-lm"], capture_output=True,
+                       text=True)
+    assert r.returncode == 0, r.stderr[-3000:]
+    lib = C.CDLL(so)
+    vp = C.c_void_p
+    lib.host_internal_geo.argtypes = [vp, vp, C.c_int64, vp]
+    lib.host_external.argtypes = [C.c_int, vp, vp, C.c_int64, vp]
+    lib.host_calculate_field.argtypes = [C.c_int, C.c_int, vp, vp, C.c_int64, vp]
+    lib.host_rk_step.argtypes = [C.c_double, C.c_double, vp, vp, vp]
+    lib.host_tables()
+    return lib
+
+
+@pytest.fixture(scope="module")
+def builds(tmp_path_factory):
+    if shutil.which("g++") is None:
+        pytest.skip("no g++")
+    d = str(tmp_path_factory.mktemp("device_on_host"))
+    return {"default": _build(d), "reference_pow": _build(d, ["COR_T96_POW5"])}
+
+
+def _p(a):
+    return a.ctypes.data_as(C.c_void_p)
+
+
+def _external(lib, ext, parmod, pts):
+    out = np.zeros_like(pts)
+    lib.host_external(ext, _p(parmod), _p(pts), len(pts), _p(out))
+    return out
+
+
+def _composed(lib, internal, ext, params, pts_m):
+    out = np.zeros_like(pts_m)
+    assert lib.host_calculate_field(internal, ext, _p(params), _p(pts_m), len(pts_m), _p(out)) == 0
+    return out
+
+
+def _cases():
+    """(name, model, function of lib -> (got, want)) over every golden field vector
+    the host build can evaluate (all but the crustal model)."""
+    g = golden("field_kats.json")
+    st = golden("field_storm.json")
+    out = []
+    ig = g["internal_geo"]
+
+    def igrf(lib):
+        p = ct.internal_setup(ig["version"], ig["time"])
+        pts = unhex(ig["points"]).reshape(-1, 3)
+        got = np.zeros_like(pts)
+        lib.host_internal_geo(_p(p), _p(pts), len(pts), _p(got))
+        return got, unhex(ig["b"]).reshape(-1, 3)
+    out.append(("internal_geo", "igrf", igrf))
+    for key, ext, model in (("t96_gsm", ct.EXTERNAL_T96, "t96"), ("ts05_gsm", ct.EXTERNAL_TS05, "ts05")):
+        k = g[key]
+        out.append((key, model, lambda lib, k=k, ext=ext: (
+            _external(lib, ext, unhex(k["parmod"]), unhex(k["points"]).reshape(-1, 3)), unhex(k["b"]).reshape(-1, 3))))
+    cf = g["calculate_field"]
+    for key, ext, model in (("igrf14", ct.EXTERNAL_NONE, "igrf"), ("igrf14+t96", ct.EXTERNAL_T96, "t96"),
+                            ("igrf14+ts05", ct.EXTERNAL_TS05, "ts05")):
+        case = cf["cases"][key]
+
+        def comp(lib, case=case, ext=ext):
+            p = ct.internal_setup("igrf14", cf["time"], parmod=unhex(case["parmod"]))
+            return (_composed(lib, 1, ext, p, unhex(cf["points_m"]).reshape(-1, 3)), unhex(case["b"]).reshape(-1, 3))
+        out.append(("calculate_field " + key, model, comp))
+    for model, ext in (("t96", ct.EXTERNAL_T96), ("ts05", ct.EXTERNAL_TS05)):
+        for n, case in enumerate(st[model]):
+            pm = unhex(case["parmod"])
+            out.append((f"storm {model} {n}", model, lambda lib, case=case, pm=pm, ext=ext: (
+                _external(lib, ext, pm, unhex(case["points"]).reshape(-1, 3)), unhex(case["b"]).reshape(-1, 3))))
+
+            def scomp(lib, case=case, pm=pm, ext=ext):
+                p = ct.internal_setup("igrf14", case["time"], parmod=pm)
+                return (_composed(lib, 1, ext, p, unhex(case["points_m"]).reshape(-1, 3)),
+                        unhex(case["b_composed"]).reshape(-1, 3))
+            out.append((f"storm igrf14+{model} {n}", model, scomp))
+    return out
+
+
+def _bits_equal(a, b):
+    return (a.view(np.uint64) == b.view(np.uint64)).all(axis=1)
+
+
+def test_device_field_code_is_the_references_arithmetic(builds):
+    """With the reference's pow(u, 5): every point of every golden field case bit for bit."""
+    lib = builds["reference_pow"]
+    n = 0
+    for name, _, fn in _cases():
+        got, want = fn(lib)
+        eq = _bits_equal(got, want)
+        assert eq.all(), (name, int((~eq).sum()), len(eq))
+        n += len(eq)
+    assert n > 2800   # 2,902 points: 410 IGRF, 612 T96/TS05, 600 composed, 1,280 at storm conditions
+
+
+def test_default_build_differs_only_in_t96_r2sheet(builds):
+    """The device's own form: IGRF and TS05 stay bit for bit; T96 (u^5 by
+    multiplication) stays within 1e-14 of |B|."""
+    lib = builds["default"]
+    for name, model, fn in _cases():
+        got, want = fn(lib)
+        if model != "t96":
+            assert _bits_equal(got, want).all(), name
+        else:
+            rel = np.linalg.norm(got - want, axis=1) / np.maximum(np.linalg.norm(want, axis=1), 1e-300)
+            assert rel.max() <= 1e-14, (name, rel.max())
+
+
+def test_rk_step_is_the_oracles(builds):
+    """rk_velocity + rk_position against the oracle's restatement of
+    calculate_position_and_speed (src/trajectory.c:275-356), bit for bit."""
+    lib = builds["default"]
+    olib = pyoracle.load()
+    rng = np.random.default_rng(5)
+    for _ in range(2000):
+        h = 10.0 ** rng.uniform(-6, -1)
+        d = rng.uniform(-1, 1) * 10.0 ** rng.uniform(-3, 3)
+        f = rng.normal(0, 3e4, 3)
+        v = rng.normal(0, 1e8, 3)
+        x = rng.normal(0, 3e7, 3)
+        v1, x1, v2, x2 = v.copy(), x.copy(), v.copy(), x.copy()
+        lib.host_rk_step(h, d, _p(f), _p(v1), _p(x1))
+        olib.orc_rk_step(h, d, _p(f), _p(v2), _p(x2))
+        assert np.array_equal(v1.view(np.uint64), v2.view(np.uint64)) and \
+            np.array_equal(x1.view(np.uint64), x2.view(np.uint64))
