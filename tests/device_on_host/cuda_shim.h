@@ -21,6 +21,7 @@
 #define __forceinline__ inline __attribute__((always_inline))
 #define __noinline__ __attribute__((noinline))
 #define __restrict__ __restrict
+#define __launch_bounds__(...)
 
 template <class T>
 static inline T __ldg(const T* p) { return *p; }
@@ -29,16 +30,26 @@ static inline T __ldg(const T* p) { return *p; }
 static inline double __dmul_rn(double a, double b) { return a * b; }
 static inline double __fma_rn(double a, double b, double c) { return std::fma(a, b, c); }
 
-// Warp intrinsics of the crustal field's warp-cooperative sum (chaos.cuh).
-// They let the header compile; the crustal model is not evaluated on the
-// host (its sum needs a whole warp), and these abort if it ever is.
+// Warp and block intrinsics of the crustal field's warp-cooperative sum
+// (chaos.cuh) and of the scan kernel's queue and block-wide decisions
+// (trace.cuh).  They let those headers compile; neither the crustal model nor
+// the kernel runs on the host (field_host.cpp drives the per-trajectory
+// functions directly), and these abort if they ever are called.
 struct ShimDim3 {
     unsigned x, y, z;
 };
-static const ShimDim3 threadIdx = {0, 0, 0};
+static const ShimDim3 threadIdx = {0, 0, 0}, blockIdx = {0, 0, 0}, blockDim = {1, 1, 1};
 static inline unsigned __ballot_sync(unsigned, int) { abort(); }
 static inline int __ffs(unsigned) { abort(); }
 template <class T>
 static inline T __shfl_sync(unsigned, T, int, int = 32) { abort(); }
 template <class T>
 static inline T __shfl_xor_sync(unsigned, T, int, int = 32) { abort(); }
+template <class T>
+static inline T __shfl_down_sync(unsigned, T, unsigned, int = 32) { abort(); }
+static inline int __popc(unsigned) { abort(); }
+static inline void __syncwarp(unsigned = 0xffffffffu) { abort(); }
+static inline int __syncthreads_count(int) { abort(); }
+static inline int __syncthreads_or(int) { abort(); }
+template <class T>
+static inline T atomicAdd(T*, T) { abort(); }

@@ -1,5 +1,6 @@
-// field_host.cpp -- TEST INFRASTRUCTURE: the device field code and RK step of
-// libcortrace compiled as host C++ (cuda_shim.h) with the reference's
+// field_host.cpp -- TEST INFRASTRUCTURE: the device field code, RK step and
+// per-trajectory scan logic of libcortrace compiled as host C++ (cuda_shim.h)
+// with the reference's
 // floating-point flags, so that its expression trees can be compared with
 // the reference bit for bit: here the transcendental functions are the host
 // C library's, as in the reference, where on the GPU they are CUDA's.
@@ -7,6 +8,7 @@
 #include "cuda_shim.h"
 
 #include "../../cor-model_gb300/csrc/model_prep.h"
+#include "../../cor-model_gb300/csrc/trace.cuh"
 
 using namespace cor;
 
@@ -17,6 +19,24 @@ Vec3 field_of(const Vec3 gsm_m) {
     const CrustalTables none{};
     return calculate_field<ModelSet<I, E, 0>>(true, gsm_m, &g_dp, none);
 }
+template <int I, int E>
+void trace_all(const TraceArgs& a) {
+    const CrustalTables none{};
+    for (uint64_t t = 0; t < a.n_traj; t++) {
+        Lane L;
+        lane_init(L, a, t);
+        for (;;) {
+            L.field = calculate_field<ModelSet<I, E, 0>>(true, L.gsm, L.par, none);
+            L.b = 1.E-09 * sqrt(L.field.x * L.field.x + L.field.y * L.field.y + L.field.z * L.field.z);
+            const int st = lane_advance(L, a);
+            if (st != 0) {
+                lane_finish(L, a, st);
+                break;
+            }
+        }
+    }
+}
+
 }  // namespace
 
 extern "C" {
@@ -73,6 +93,44 @@ int host_calculate_field(int internal, int external, const cor_model_params* p, 
         out[3 * i + 2] = b.z;
     }
     return 0;
+}
+
+// The scan kernel's work for every trajectory of a batch, one after the other:
+// lane_init, then the kernel loop of trace_kernel -- the field at the lane's
+// GSM position whenever it needs one, lane_advance, lane_finish at the
+// termination -- for the model sets without the crustal field.  The turn test
+// is the reference's atan2 predicate (turn_exact = 0), which on the host is
+// the reference's own decision.  status/records get n_traj entries; returns
+// -1 for a model set it does not cover.
+int host_trace(int internal, int external, const cor_scan_job* jobs, const cor_job_trig* trig, int32_t n_jobs,
+               const uint64_t* offsets, uint64_t n_traj, const cor_model_params* params, int32_t n_params,
+               uint64_t step_limit, double tu_angle, double mass, uint8_t* status, cor_traj_record* records) {
+    DevParams* dp = (DevParams*)calloc((size_t)n_params, sizeof(DevParams));
+    if (!dp) return -2;
+    prepare_params(params, n_params, dp);
+    TraceArgs a;
+    memset(&a, 0, sizeof a);
+    a.jobs = jobs;
+    a.trig = reinterpret_cast<const JobTrig*>(trig);
+    a.offsets = offsets;
+    a.n_jobs = n_jobs;
+    a.n_traj = n_traj;
+    a.params = dp;
+    a.step_limit = step_limit;
+    a.tu_angle = tu_angle;
+    a.turn_exact = 0;
+    a.mass = mass;
+    a.status = status;
+    a.records = records;
+    int rc = 0;
+    if (internal && external == COR_EXTERNAL_NONE) trace_all<1, 0>(a);
+    else if (internal && external == COR_EXTERNAL_T96) trace_all<1, 1>(a);
+    else if (internal && external == COR_EXTERNAL_TS05) trace_all<1, 2>(a);
+    else if (!internal && external == COR_EXTERNAL_T96) trace_all<0, 1>(a);
+    else if (!internal && external == COR_EXTERNAL_TS05) trace_all<0, 2>(a);
+    else rc = -1;
+    free(dp);
+    return rc;
 }
 
 // One RK step (rk_velocity then rk_position): vel and pos in/out.

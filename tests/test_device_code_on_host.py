@@ -10,7 +10,10 @@ evaluated with glibc and without contraction, so they must give the
 reference's bits.  With COR_T96_POW5 (the reference's pow(u, 5) in r2sheet)
 every golden field vector is reproduced bit for bit: IGRF, T96 and TS05,
 alone and composed, at the quiet and the storm-range conditions.  The default
-build, which multiplies u out, differs only in T96, by a few ulp.  No GPU."""
+build, which multiplies u out, differs only in T96, by a few ulp.  The scan
+kernel's per-trajectory functions (lane_init, lane_advance, lane_finish), run
+trajectory by trajectory as the kernel's loop runs them, give every
+trajectory's class and final record bit for bit as the reference does.  No GPU."""
 from __future__ import annotations
 
 import ctypes as C
@@ -42,6 +45,8 @@ def _build(out_dir, defines=()) -> C.CDLL:
     lib.host_external.argtypes = [C.c_int, vp, vp, C.c_int64, vp]
     lib.host_calculate_field.argtypes = [C.c_int, C.c_int, vp, vp, C.c_int64, vp]
     lib.host_rk_step.argtypes = [C.c_double, C.c_double, vp, vp, vp]
+    lib.host_trace.argtypes = [C.c_int, C.c_int, vp, vp, C.c_int32, vp, C.c_uint64, vp, C.c_int32, C.c_uint64,
+                               C.c_double, C.c_double, vp, vp]
     lib.host_tables()
     return lib
 
@@ -158,3 +163,64 @@ def test_rk_step_is_the_oracles(builds):
         olib.orc_rk_step(h, d, _p(f), _p(v2), _p(x2))
         assert np.array_equal(v1.view(np.uint64), v2.view(np.uint64)) and \
             np.array_equal(x1.view(np.uint64), x2.view(np.uint64))
+
+
+def _host_scan(lib, internal, external, jobs, params, step_limit=25000):
+    """host_trace one job per call, 8 calls at a time (ctypes releases the GIL;
+    the host build reads no mutable global)."""
+    from concurrent.futures import ThreadPoolExecutor
+    n, off = ct.batch_offsets(jobs)
+    status = np.zeros(n, np.uint8)
+    rec = np.zeros(n, ct.RECORD_DTYPE)
+    params = np.ascontiguousarray(params, ct.PARAMS_DTYPE)
+
+    def one(j):
+        job = np.ascontiguousarray(jobs[j:j + 1])
+        trig = ct.prepare_trig(job)
+        m, o1 = ct.batch_offsets(job)
+        st = np.zeros(m, np.uint8)
+        r = np.zeros(m, ct.RECORD_DTYPE)
+        rc = lib.host_trace(internal, external, _p(job), _p(trig), 1, _p(o1), m, _p(params), len(params), step_limit,
+                            0.01, ct.DEF_HM0_P, _p(st), _p(r))
+        status[off[j]:off[j + 1]] = st
+        rec[off[j]:off[j + 1]] = r
+        return rc
+    with ThreadPoolExecutor(8) as ex:
+        assert all(rc == 0 for rc in ex.map(one, range(len(jobs))))
+    return status, rec, off
+
+
+def _scan_cases():
+    """(name, internal, external, jobs, params, sites) from the golden scans."""
+    out = []
+    for fn, ext, stride in (("scan_config0.json", ct.EXTERNAL_NONE, 38), ("scan_t96.json", ct.EXTERNAL_T96, 100),
+                            ("scan_ts05.json", ct.EXTERNAL_TS05, 100)):
+        g = golden(fn)
+        sites = g["sites"][::stride]
+        p = ct.internal_setup(g["model"], g["time"], parmod=g.get("parmod"))
+        jobs = np.concatenate([ct.make_job(s["lat"], s["lon"], rig=g["rig"], rk=g["rk"], dele=g["del"],
+                                           the1=s["the1"], fi1=s["fi1"]) for s in sites])
+        out.append((fn, ext, jobs, p, sites))
+    g = golden("scan_storm.json")
+    c = g["conditions"][0]
+    jobs = np.concatenate([ct.make_job(s["lat"], s["lon"], rig=g["rig"], rk=g["rk"], dele=g["del"], the1=s["the1"],
+                                       fi1=s["fi1"]) for s in c["sites"]])
+    out.append(("scan_storm.json", ct.EXTERNAL_TS05, jobs, ct.internal_setup(g["model"], c["time"],
+                                                                             parmod=c["parmod"]), c["sites"]))
+    return out
+
+
+def test_device_scan_logic_is_the_references(builds):
+    """Every trajectory of sites from the IGRF, T96, TS05 and storm-condition
+    golden scans: the allowed/forbidden flags equal the reference's, and the
+    class and final record (position, velocity, time, length, step and trial
+    counts) equal the oracle's -- the reference's arithmetic -- bit for bit."""
+    lib = builds["reference_pow"]
+    for name, ext, jobs, p, sites in _scan_cases():
+        status, rec, off = _host_scan(lib, 1, ext, jobs, p)
+        for j, s in enumerate(sites):
+            allowed = np.nonzero(status[off[j]:off[j + 1]] == ct.TRAJ_ALLOWED)[0].tolist()
+            assert allowed == s["allowed"], (name, s["lat"], s["lon"])
+        o = pyoracle.scan_batch(jobs, p, models=ct.model_set(ct.INTERNAL_SH, ext), threads=8, want_records=True)
+        assert np.array_equal(status, o.status), name
+        assert np.array_equal(rec.view(np.uint8), o.records.view(np.uint8)), name
