@@ -366,41 +366,14 @@ static int launch_scan(cor_ctx* ctx, const TraceArgs& a, cor_model_set models, c
 }
 
 // ---- crustal model tables --------------------------------------------------
-// One device block: g, h, k1, k2 (packed lower triangles of nmax(nmax+1)/2
-// entries each), then kd (nmax entries).  k1, k2 and kd are the recursion
-// factors of lib/chaos/chaos.c:163-180, computed with its expressions.
+// One device block, built on the host by crustal_block (model_prep.h).
 static int upload_crustal(cor_ctx* ctx, const double* g, const double* h, int32_t nmax) {
     if (nmax < 2 || nmax > kChaosMaxN)
         return fail(ctx, COR_ERR_RANGE, "crustal table nmax %d outside [2, %d]", nmax, kChaosMaxN);
-    const size_t nt = (size_t)nmax * (size_t)(nmax + 1) / 2;
-    const size_t total = 4 * nt + (size_t)nmax;
+    const size_t total = crustal_block_size(nmax);
     double* host = (double*)calloc(total, sizeof(double));
     if (!host) return fail(ctx, COR_ERR_NOMEM, "host allocation");
-    double* hk1 = host + 2 * nt;
-    double* hk2 = host + 3 * nt;
-    double* hkd = host + 4 * nt;
-    memcpy(host, g, sizeof(double) * nt);
-    memcpy(host + nt, h, sizeof(double) * nt);
-    int n_first = nmax;
-    for (int n = 0; n < nmax && n_first == nmax; n++)
-        for (int m = 0; m <= n; m++)
-            if (g[n * (n + 1) / 2 + m] != 0. || h[n * (n + 1) / 2 + m] != 0.) {
-                n_first = n;
-                break;
-            }
-    for (int n = 2; n < nmax; n++) {
-        const double n2 = n * 2;
-        const double n21 = n2 - 1;
-        const int n1 = n - 1;
-        hkd[n] = sqrt(n21 / n2);
-        const double nn = (double)n * n;
-        for (int m = 0; m < n; m++) {
-            const double mm = m * m;
-            const double nnmm = nn - mm;
-            hk1[n * (n + 1) / 2 + m] = n21 / sqrt(nnmm);
-            hk2[n * (n + 1) / 2 + m] = sqrt((n1 * n1 - mm) / nnmm);
-        }
-    }
+    const int n_first = crustal_block(g, h, nmax, host);
     int rc = COR_OK;
     double* dev = nullptr;
     do {

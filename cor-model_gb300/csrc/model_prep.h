@@ -232,4 +232,43 @@ static void prepare_params(const cor_model_params* in, int32_t n, DevParams* out
     }
 }
 
+// The crustal model's tables, as one block: g, h, k1, k2 (packed lower
+// triangles of nmax(nmax+1)/2 entries each), then kd (nmax entries).  k1, k2
+// and kd are the recursion factors of lib/chaos/chaos.c:163-180, computed with
+// its expressions.  `host` holds crustal_block_size(nmax) zeroed doubles.
+// Returns the first degree with a non-zero coefficient (nmax if none).
+static size_t crustal_block_size(int32_t nmax) {
+    return 4 * ((size_t)nmax * (size_t)(nmax + 1) / 2) + (size_t)nmax;
+}
+
+static int crustal_block(const double* g, const double* h, int32_t nmax, double* host) {
+    const size_t nt = (size_t)nmax * (size_t)(nmax + 1) / 2;
+    double* hk1 = host + 2 * nt;
+    double* hk2 = host + 3 * nt;
+    double* hkd = host + 4 * nt;
+    memcpy(host, g, sizeof(double) * nt);
+    memcpy(host + nt, h, sizeof(double) * nt);
+    int n_first = nmax;
+    for (int n = 0; n < nmax && n_first == nmax; n++)
+        for (int m = 0; m <= n; m++)
+            if (g[n * (n + 1) / 2 + m] != 0. || h[n * (n + 1) / 2 + m] != 0.) {
+                n_first = n;
+                break;
+            }
+    for (int n = 2; n < nmax; n++) {
+        const double n2 = n * 2;
+        const double n21 = n2 - 1;
+        const int n1 = n - 1;
+        hkd[n] = sqrt(n21 / n2);
+        const double nn = (double)n * n;
+        for (int m = 0; m < n; m++) {
+            const double mm = m * m;
+            const double nnmm = nn - mm;
+            hk1[n * (n + 1) / 2 + m] = n21 / sqrt(nnmm);
+            hk2[n * (n + 1) / 2 + m] = sqrt((n1 * n1 - mm) / nnmm);
+        }
+    }
+    return n_first;
+}
+
 }  // namespace cor

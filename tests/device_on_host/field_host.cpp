@@ -133,6 +133,73 @@ int host_trace(int internal, int external, const cor_scan_job* jobs, const cor_j
     return rc;
 }
 
+// chaos_geo_warp at n GEO points [R_E] for the packed tables g/h of nmax
+// degrees (the tables built by crustal_block, as cor_upload_crustal builds
+// them), 32 points at a time by an emulated warp (the last one partly idle).
+int host_chaos(const double* g, const double* h, int32_t nmax, const double* pts, int64_t n, double* out) {
+    std::vector<double> block(crustal_block_size(nmax), 0.);
+    const int n_first = crustal_block(g, h, nmax, block.data());
+    const size_t nt = (size_t)nmax * (size_t)(nmax + 1) / 2;
+    const double* b0 = block.data();
+    const CrustalTables t{b0, b0 + nt, b0 + 2 * nt, b0 + 3 * nt, b0 + 4 * nt, nmax, n_first, 1, 0};
+    ShimWarp w;
+    shim_warp = &w;
+    for (int64_t base = 0; base < n; base += 32) {
+        std::thread lanes[32];
+        for (int l = 0; l < 32; l++)
+            lanes[l] = std::thread([&, l] {
+                threadIdx.x = (unsigned)l;
+                const int64_t i = base + l;
+                const bool want = i < n;
+                const Vec3 x = want ? Vec3{pts[3 * i], pts[3 * i + 1], pts[3 * i + 2]} : Vec3{0., 0., 0.};
+                const Vec3 f = chaos_geo_warp(want, x, t);
+                if (want) {
+                    out[3 * i] = f.x;
+                    out[3 * i + 1] = f.y;
+                    out[3 * i + 2] = f.z;
+                }
+            });
+        for (std::thread& th : lanes) th.join();
+    }
+    shim_warp = nullptr;
+    return 0;
+}
+
+// calculate_field of the crustal model set (internal and external chosen at
+// run time, as the one crustal instantiation does) at n GSM points [m], 32
+// points at a time by an emulated warp.
+int host_calculate_field_crustal(int internal, int external, const cor_model_params* p, const double* g,
+                                 const double* h, int32_t nmax, const double* pts, int64_t n, double* out) {
+    prepare_params(p, 1, &g_dp);
+    std::vector<double> block(crustal_block_size(nmax), 0.);
+    const int n_first = crustal_block(g, h, nmax, block.data());
+    const size_t nt = (size_t)nmax * (size_t)(nmax + 1) / 2;
+    const double* b0 = block.data();
+    const CrustalTables t{b0, b0 + nt, b0 + 2 * nt, b0 + 3 * nt, b0 + 4 * nt, nmax, n_first, internal, external};
+    ShimWarp w;
+    shim_warp = &w;
+    for (int64_t base = 0; base < n; base += 32) {
+        std::thread lanes[32];
+        for (int l = 0; l < 32; l++)
+            lanes[l] = std::thread([&, l] {
+                threadIdx.x = (unsigned)l;
+                const int64_t i = base + l;
+                const bool want = i < n;
+                const Vec3 x = want ? Vec3{pts[3 * i], pts[3 * i + 1], pts[3 * i + 2]} : Vec3{0., 0., 0.};
+                const Vec3 f =
+                    calculate_field<ModelSet<kModelAtRunTime, kModelAtRunTime, 1>>(want, x, &g_dp, t);
+                if (want) {
+                    out[3 * i] = f.x;
+                    out[3 * i + 1] = f.y;
+                    out[3 * i + 2] = f.z;
+                }
+            });
+        for (std::thread& th : lanes) th.join();
+    }
+    shim_warp = nullptr;
+    return 0;
+}
+
 // One RK step (rk_velocity then rk_position): vel and pos in/out.
 void host_rk_step(double h, double d, const double* field, double* vel, double* pos) {
     const Vec3 f{field[0], field[1], field[2]};

@@ -13,7 +13,11 @@ alone and composed, at the quiet and the storm-range conditions.  The default
 build, which multiplies u out, differs only in T96, by a few ulp.  The scan
 kernel's per-trajectory functions (lane_init, lane_advance, lane_finish), run
 trajectory by trajectory as the kernel's loop runs them, give every
-trajectory's class and final record bit for bit as the reference does.  No GPU."""
+trajectory's class and final record bit for bit as the reference does.  The
+crustal model's warp-cooperative sum runs on 32 host threads standing for a
+warp: it sums in another order than the reference, so it agrees to a few ulp,
+and composed with IGRF-14 (and T96) the golden field vectors come out bit for
+bit.  No GPU."""
 from __future__ import annotations
 
 import ctypes as C
@@ -30,8 +34,8 @@ import pyoracle
 
 SRC = os.path.join(ROOT, "tests", "device_on_host", "field_host.cpp")
 # the reference's flags (CMakeLists.txt:17, without -march=native)
-FLAGS = ["-std=c++17", "-O3", "-fno-math-errno", "-fno-trapping-math", "-ffp-contract=off", "-fPIC", "-shared",
-         "-Wno-unknown-pragmas"]
+FLAGS = ["-std=c++20", "-O3", "-fno-math-errno", "-fno-trapping-math", "-ffp-contract=off", "-fPIC", "-shared",
+         "-pthread", "-Wno-unknown-pragmas"]
 
 
 def _build(out_dir, defines=()) -> C.CDLL:
@@ -45,6 +49,8 @@ def _build(out_dir, defines=()) -> C.CDLL:
     lib.host_external.argtypes = [C.c_int, vp, vp, C.c_int64, vp]
     lib.host_calculate_field.argtypes = [C.c_int, C.c_int, vp, vp, C.c_int64, vp]
     lib.host_rk_step.argtypes = [C.c_double, C.c_double, vp, vp, vp]
+    lib.host_chaos.argtypes = [vp, vp, C.c_int32, vp, C.c_int64, vp]
+    lib.host_calculate_field_crustal.argtypes = [C.c_int, C.c_int, vp, vp, vp, C.c_int32, vp, C.c_int64, vp]
     lib.host_trace.argtypes = [C.c_int, C.c_int, vp, vp, C.c_int32, vp, C.c_uint64, vp, C.c_int32, C.c_uint64,
                                C.c_double, C.c_double, vp, vp]
     lib.host_tables()
@@ -224,3 +230,34 @@ def test_device_scan_logic_is_the_references(builds):
         o = pyoracle.scan_batch(jobs, p, models=ct.model_set(ct.INTERNAL_SH, ext), threads=8, want_records=True)
         assert np.array_equal(status, o.status), name
         assert np.array_equal(rec.view(np.uint8), o.records.view(np.uint8)), name
+
+
+def test_crustal_warp_sum_within_ulps(builds):
+    """chaos_geo_warp on an emulated warp (40 points: a full warp and a partly
+    idle one) against the reference's chaos_geo: per order, then across the
+    lanes, instead of degree by degree -- a few ulp of the crustal field."""
+    lib = builds["default"]
+    g, h, nmax = ct.chaos_table()
+    k = golden("field_kats.json")["chaos_geo"]
+    pts = unhex(k["points"]).reshape(-1, 3)
+    want = unhex(k["b"]).reshape(-1, 3)
+    got = np.zeros_like(pts)
+    assert lib.host_chaos(_p(g), _p(h), nmax, _p(pts), len(pts), _p(got)) == 0
+    rel = np.linalg.norm(got - want, axis=1) / np.linalg.norm(want, axis=1)
+    assert rel.max() <= 1e-13, rel.max()
+
+
+def test_crustal_model_set_composes_bit_for_bit(builds):
+    """calculate_field of the crustal model set (IGRF-14 + CHAOS-7.16, with and
+    without T96) at the 200 golden points: the crustal part's last bits are far
+    below the total's, so the composed field is the reference's bit for bit."""
+    lib = builds["reference_pow"]
+    g, h, nmax = ct.chaos_table()
+    cf = golden("field_kats.json")["calculate_field"]
+    pts = unhex(cf["points_m"]).reshape(-1, 3)
+    for key, ext in (("igrf14+chaos7.16", ct.EXTERNAL_NONE), ("igrf14+t96+chaos7.16", ct.EXTERNAL_T96)):
+        case = cf["cases"][key]
+        p = ct.internal_setup("igrf14", cf["time"], parmod=unhex(case["parmod"]))
+        got = np.zeros_like(pts)
+        assert lib.host_calculate_field_crustal(1, ext, _p(p), _p(g), _p(h), nmax, _p(pts), len(pts), _p(got)) == 0
+        assert _bits_equal(got, unhex(case["b"]).reshape(-1, 3)).all(), key
