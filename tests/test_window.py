@@ -138,3 +138,37 @@ def test_window_scan_widens_to_the_whole_scans_cutoffs():
     for k in ("r_lower", "r_upper", "r_cutoff", "n_forbidden"):
         assert np.array_equal(sites[k], whole.sites[k]), k
     assert redone.all()
+
+
+def test_trained_window_gains_over_the_full_scan():
+    """What the trained network gains over the method without it, on CPU: its
+    weights (window_t96.npz) run through the numpy restatement of the
+    tensor-core forward pass, and the oracle traces both the learned windows
+    (with the edge-hit widening) and the full scans, on 8 sites of the
+    benchmark's grid (IGRF-14 + T96, 0.01 -> 20 GV by 0.01).  Every site's R_C
+    is within one grid step (0.01 GV) of the full scan's, for a fraction of
+    the trajectories and of the accepted steps."""
+    import os
+    import bench
+
+    class Ctx:
+        def trace_batch(self, jobs, params, models=None, **kw):
+            import pyoracle
+            return pyoracle.scan_batch(jobs, params, models=models, threads=8)
+
+    d = np.load(os.path.join(os.path.dirname(window.__file__), "window_t96.npz"))
+    sites = bench.grid_sites()[::333]
+    x = (bench.site_features(sites) - d["feat_mean"]) / d["feat_std"]
+    y = mlp_oracle.forward(d["params"], x)[0] * d["y_std"] + d["y_mean"]
+    b = window.band_of(y[:, 1], d["band_edges"])
+    i_lo, i_hi = window.window_indices(y[:, 0], y[:, 1], d["band_sigma"][b, 0], d["band_sigma"][b, 1])
+    jobs, p, models = bench.make_jobs(sites), bench.params(), bench.models()
+    full = Ctx().trace_batch(jobs, p, models=models)
+    got, redone, traced, steps = window.trace_windows(Ctx(), jobs, p, models, i_lo, i_hi)
+    d_rc = np.abs(got["r_cutoff"] - full.sites["r_cutoff"])
+    frac_traj = traced / full.counters["trajectories"]
+    frac_steps = steps / full.counters["accepted_steps"]
+    print(f"learned window on {len(sites)} sites: max |dRc| {d_rc.max():.4f} GV, {int(redone.sum())} widened, "
+          f"{frac_traj:.3f} of the trajectories, {frac_steps:.3f} of the accepted steps")
+    assert (d_rc <= 0.01 + 1e-9).all(), d_rc
+    assert frac_traj < 0.35 and frac_steps < 0.7
