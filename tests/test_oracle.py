@@ -88,9 +88,9 @@ def test_oracle_scan_matches_reference_config0_subset():
 
 
 EXT_SCANS = {
-    "scan_t96.json": (ct.INTERNAL_SH, ct.EXTERNAL_T96, ct.CRUSTAL_NONE, 4),
-    "scan_ts05.json": (ct.INTERNAL_SH, ct.EXTERNAL_TS05, ct.CRUSTAL_NONE, 4),
-    "scan_chaos.json": (ct.INTERNAL_SH, ct.EXTERNAL_NONE, ct.CRUSTAL_CHAOS, 2),
+    "scan_t96.json": (ct.INTERNAL_SH, ct.EXTERNAL_T96, ct.CRUSTAL_NONE, 8),
+    "scan_ts05.json": (ct.INTERNAL_SH, ct.EXTERNAL_TS05, ct.CRUSTAL_NONE, 8),
+    "scan_chaos.json": (ct.INTERNAL_SH, ct.EXTERNAL_NONE, ct.CRUSTAL_CHAOS, 3),
 }
 
 
