@@ -5,9 +5,15 @@
 1. Seeded site-directions (uniform over the sphere; half vertical, half at
    30 deg zenith and one of 8 azimuths) and conditions (window.sample_conditions:
    Pdyn, Dst, By, Bz over storm ranges, the tilt through the date), IGRF-14 + T96.
-2. Labels from the plain tracer: a coarse scan (20 -> 0.1 GV by 0.1) of every
-   sample, then the 0.01 GV grid traced over the coarse penumbra plus a margin;
-   R_U and R_L of that window are the labels (log GV).
+2. Labels from the plain tracer (log GV), by one of two methods:
+   * full (the default): the whole 0.01 GV scan of every sample; its R_U and
+     R_L are exactly what the window has to hold;
+   * coarse: a coarse scan (20 -> 0.1 GV by 0.1), then the 0.01 GV grid over
+     the coarse penumbra plus a margin, about a seventh of the trajectories.
+     The coarse scan cannot see penumbra structure finer than its step: over
+     seeded storm-range samples, 9 of 48 came out with R_L too high (an allowed
+     rigidity far below the main penumbra, up to 3.5 GV) and 1 with R_U too
+     low, against the full scan.
 3. The network (include/cor_window.h) is trained on the GPU with its own
    tensor-core kernels (AdamW, minibatches), on standardised features and
    targets.
@@ -62,14 +68,27 @@ def build_samples(rng, n, external="t96"):
     return {"lat": lat, "lon": lon, "dirs": dirs, "params": params, "features": np.array(feats)}
 
 
-def label(ctx, s, models, chunk=4000):
-    """(log R_U, log R_L, trajectories traced) of every sample."""
+def label(ctx, s, models, chunk=4000, method="full"):
+    """(log R_U, log R_L, trajectories traced) of every sample, by the
+    full 0.01 GV scan or the coarse-then-fine method (module docstring)."""
     n = len(s["lat"])
     traced = 0
     ru = np.zeros(n)
     rl = np.zeros(n)
     for a in range(0, n, chunk):
         b = min(n, a + chunk)
+        if method == "full":
+            jobs = np.concatenate([ct.make_job(s["lat"][k], s["lon"][k], rig=window.GRID_RIG, rk=20.0,
+                                               dele=window.GRID_DEL, r0=R0, the1=s["dirs"][k][0],
+                                               fi1=s["dirs"][k][1], param_index=k - a) for k in range(a, b)])
+            res = ctx.trace_batch(jobs, s["params"][a:b], models=models, want_status=False)
+            traced += int(res.counters["trajectories"])
+            ru[a:b] = np.log(np.maximum(res.sites["r_upper"], window.GRID_RIG))
+            rl[a:b] = np.log(np.maximum(res.sites["r_lower"], window.GRID_RIG))
+            print(f"  labelled {b}/{n} ({traced} trajectories)", flush=True)
+            continue
+        if method != "coarse":
+            raise ValueError(f"label method {method!r}")
         jobs = np.concatenate([ct.make_job(s["lat"][k], s["lon"][k], rig=COARSE[0], rk=COARSE[1], dele=COARSE[2],
                                            r0=R0, the1=s["dirs"][k][0], fi1=s["dirs"][k][1], param_index=k - a)
                                for k in range(a, b)])
@@ -127,9 +146,14 @@ def main():
     ap.add_argument("--epochs", type=int, default=200)
     ap.add_argument("--batch", type=int, default=512)
     ap.add_argument("--out", default=os.path.join(HERE, "window_t96.npz"))
-    ap.add_argument("--labels", default=os.path.join(HERE, "window_t96_labels.npz"),
-                    help="labelled set: loaded when the file exists, else traced and saved there")
+    ap.add_argument("--label-method", default="full", choices=["full", "coarse"])
+    ap.add_argument("--labels", default=None,
+                    help="labelled set: loaded when the file exists, else traced and saved there (default: "
+                         "window_t96_labels.npz for the coarse method, window_t96_labels_full.npz for full)")
     args = ap.parse_args()
+    if args.labels is None:
+        args.labels = os.path.join(HERE, "window_t96_labels.npz" if args.label_method == "coarse"
+                                   else "window_t96_labels_full.npz")
     rng = np.random.default_rng(args.seed)
     models = ct.model_set(ct.INTERNAL_SH, ct.EXTERNAL_T96)
     t0 = time.time()
@@ -138,16 +162,18 @@ def main():
     if args.labels and os.path.exists(args.labels):
         d = np.load(args.labels)
         assert d["features"].shape == tr["features"].shape, "labels were made for other samples"
+        made = str(d["method"]) if "method" in d else "coarse"
+        assert made == args.label_method, f"{args.labels} holds {made} labels"
         ru, rl, vru, vrl = d["ru"], d["rl"], d["vru"], d["vrl"]
         n1, n2 = int(d["n1"]), int(d["n2"])
     else:
         ctx = ct.Context(0)
-        ru, rl, n1 = label(ctx, tr, models)
-        vru, vrl, n2 = label(ctx, va, models)
+        ru, rl, n1 = label(ctx, tr, models, method=args.label_method)
+        vru, vrl, n2 = label(ctx, va, models, method=args.label_method)
         ctx.close()
         if args.labels:
             np.savez(args.labels, features=tr["features"], ru=ru, rl=rl, val_features=va["features"], vru=vru,
-                     vrl=vrl, n1=n1, n2=n2)
+                     vrl=vrl, n1=n1, n2=n2, method=args.label_method)
     t_label = time.time() - t0
     print(f"labels: {n1 + n2} trajectories in {t_label:.0f} s", flush=True)
     fm, fs = tr["features"].mean(0), tr["features"].std(0)
@@ -174,7 +200,8 @@ def main():
     info = {"samples": args.samples, "val": args.val, "seed": args.seed, "epochs": args.epochs, "steps": steps,
             "batch": args.batch, "sigma_log_ru": float(sigma[0]), "sigma_log_rl": float(sigma[1]),
             "band_sigma": band_sigma.round(4).tolist(), "heldout_window_miss": float(miss),
-            "model": "igrf14+t96", "label_trajectories": n1 + n2, "label_seconds": t_label,
+            "model": "igrf14+t96", "label_method": args.label_method, "label_trajectories": n1 + n2,
+            "label_seconds": t_label,
             "total_seconds": time.time() - t0}
     np.savez(args.out, params=params, feat_mean=fm, feat_std=fs, y_mean=ym, y_std=ys, sigma=sigma,
              band_edges=edges, band_sigma=band_sigma,

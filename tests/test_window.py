@@ -172,3 +172,30 @@ def test_trained_window_gains_over_the_full_scan():
           f"{frac_traj:.3f} of the trajectories, {frac_steps:.3f} of the accepted steps")
     assert (d_rc <= 0.01 + 1e-9).all(), d_rc
     assert frac_traj < 0.35 and frac_steps < 0.7
+
+
+def test_training_labels_equal_the_full_scans():
+    """train_window.label (the default, full-scan method) gives each seeded
+    storm-range sample its whole 0.01 GV scan's log R_U and log R_L, across
+    label chunks (chunk=3 over 4 samples: the parameter blocks are indexed per
+    chunk); oracle as the tracer.  (The coarse method is the cheaper
+    approximation; its misses against the full scan are recorded in
+    train_window.py's docstring.)"""
+    import cortrace as ct
+    import train_window as tw
+
+    class Ctx:
+        def trace_batch(self, jobs, params, models=None, **kw):
+            import pyoracle
+            return pyoracle.scan_batch(jobs, params, models=models, threads=8)
+
+    s = tw.build_samples(np.random.default_rng(11), 4, "t96")
+    models = ct.model_set(ct.INTERNAL_SH, ct.EXTERNAL_T96)
+    ru, rl, traced = tw.label(Ctx(), s, models, chunk=3)
+    full = np.concatenate([ct.make_job(s["lat"][k], s["lon"][k], rig=window.GRID_RIG, rk=20.0, dele=window.GRID_DEL,
+                                       r0=tw.R0, the1=s["dirs"][k][0], fi1=s["dirs"][k][1], param_index=k)
+                           for k in range(len(s["lat"]))])
+    res = Ctx().trace_batch(full, s["params"], models=models)
+    assert np.array_equal(ru, np.log(np.maximum(res.sites["r_upper"], window.GRID_RIG)))
+    assert np.array_equal(rl, np.log(np.maximum(res.sites["r_lower"], window.GRID_RIG)))
+    assert traced == res.counters["trajectories"]
