@@ -10,8 +10,9 @@ cap, and traces them in one call while the other slots' batches run on the
 GPU.  A request is admitted when its device memory (jobs, start vectors,
 offsets, classes, results, parameter block) fits in what the HBM budget has
 left after the requests in flight.  With a window model, each site-direction
-is first scanned over its predicted window and falls back to the full scan
-on an edge hit.  Each request's latency runs from its arrival to the end of
+of a request with the field model the network was trained with is first
+scanned over its predicted window and falls back to the full scan on an edge
+hit; requests with another field model get the full scan.  Each request's latency runs from its arrival to the end of
 the batch that completed it; results are per site-direction P(S), P(C), P(M),
 identical whether a request ran alone or in a mix (trajectories are
 independent and deterministic).
@@ -325,7 +326,8 @@ class Server:
                 params = np.concatenate([ct.internal_setup("igrf14", r.time7, parmod=r.parmod) for r in reqs])
                 jobs = np.concatenate([request_jobs(r, k) for k, r in enumerate(reqs)])
                 feats = None
-                if self.window_model is not None:
+                # windows only for requests of the field model the network was trained with
+                if self.window_model is not None and getattr(self.window_model, "external", None) == ext:
                     feats = np.concatenate([request_features(r, params[k:k + 1]) for k, r in enumerate(reqs)])
                 sites, fb = self.executor(ctx, jobs, params, ct.model_set(ct.INTERNAL_SH, ext), feats)
                 o = 0

@@ -285,9 +285,22 @@ def trace_windows(ctx, jobs, params, models, i_lo, i_hi, widen: int = 3, **kw):
     return sites, redone, traced, steps
 
 
+def trained_external(info: str) -> int | None:
+    """The external field model (COR_EXTERNAL_*) a window network was trained
+    with, from the provenance train_window.py stores ("igrf14+t96" ...); None
+    when it names none the scan knows."""
+    import json
+    try:
+        model = json.loads(info).get("model", "")
+    except (ValueError, AttributeError):
+        return None
+    return {"igrf14+t96": ct.EXTERNAL_T96, "igrf14+ts05": ct.EXTERNAL_TS05, "igrf14": ct.EXTERNAL_NONE}.get(model)
+
+
 class WindowModel:
     """A trained window network with its standardisation and sigmas (the
-    file train_window.py writes)."""
+    file train_window.py writes).  `external` is the external field model it
+    was trained with: its windows are meant for scans with that model only."""
 
     def __init__(self, path: str, device: int = 0, max_batch: int = 8192):
         d = np.load(path, allow_pickle=False)
@@ -300,6 +313,7 @@ class WindowModel:
         self.band_edges = d["band_edges"] if "band_edges" in d else np.zeros(0)
         self.band_sigma = d["band_sigma"] if "band_sigma" in d else self.sigma[None, :]
         self.info = str(d["info"])
+        self.external = trained_external(self.info)
         self.net = Network(device, max_batch=max_batch)
         self.net.set_params(self.params)
         import threading

@@ -145,3 +145,32 @@ def test_rejected_requests_are_not_owed_after_a_stop(tmp_path):
     assert out["rejected"] == 3
     done, pending = serve.RequestLog.replay(str(log))
     assert done == {} and pending == []
+
+
+def test_windows_only_for_the_trained_field_model():
+    """A window network trained with T96 is used for T96 requests only; TS05
+    requests in the same stream get the full scan (their executor call has no
+    features)."""
+    import window
+    assert window.trained_external('{"model": "igrf14+t96"}') == ct.EXTERNAL_T96
+    assert window.trained_external('{"model": "igrf14+ts05"}') == ct.EXTERNAL_TS05
+    assert window.trained_external("not json") is None
+
+    class _Model:
+        external = ct.EXTERNAL_T96
+    seen = []
+
+    def executor(ctx, jobs, params, models, feats):
+        seen.append((models.external_model, feats is not None))
+        res = pyoracle.scan_batch(jobs, params, models=models, threads=2)
+        return res.sites, np.zeros(len(jobs), bool)
+    reqs = _small(serve.poisson_stream(17, 500.0, 6, max_box_sites=4))
+    for k, r in enumerate(reqs):
+        r.external = ct.EXTERNAL_T96 if k % 2 else ct.EXTERNAL_TS05
+        if r.external == ct.EXTERNAL_TS05:
+            r.parmod = list(r.parmod[:4]) + [1.0] * 6
+    srv = serve.Server(slots=1, executor=executor, window_model=_Model())
+    out = serve.run_stream(srv, reqs)
+    assert out["completed"] == 6
+    assert all(used == (ext == ct.EXTERNAL_T96) for ext, used in seen)
+    assert {ext for ext, _ in seen} == {ct.EXTERNAL_T96, ct.EXTERNAL_TS05}
