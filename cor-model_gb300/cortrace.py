@@ -158,7 +158,7 @@ def batch_offsets(jobs: np.ndarray) -> tuple[int, np.ndarray]:
     n = C.c_uint64(0)
     rc = lib.cor_batch_count(_ptr(jobs), len(jobs), C.byref(n), _ptr(off))
     if rc != COR_OK:
-        raise CorError(rc, "bad rigidity grid")
+        raise CorError(rc, "invalid job: rigidity grid or window, nk1 <= 0, zero charge or non-finite start")
     return int(n.value), off
 
 
