@@ -9,7 +9,7 @@ and driven two ways:
     giving the printed rows and the CUTOFF line of whole rigidity scans.
 
 Run here (where the reference tree exists):  python tests/golden/make_golden.py [section ...]
-Sections: setup field field_storm scan0 scan_t96 scan_ts05 scan_chaos scan_storm field_cli trajectory_cli cli_errors nudge nudge_extra.  The fixtures are small JSON
+Sections: setup field field_storm scan0 scan_t96 scan_ts05 scan_chaos scan_storm field_cli trajectory_cli cli_errors nudge nudge_extra nudge_storm.  The fixtures are small JSON
 files; nothing on the GPU side reads the reference.
 """
 from __future__ import annotations
@@ -473,6 +473,59 @@ def make_nudge() -> dict:
     return out
 
 
+def make_nudge_storm() -> dict:
+    """The storm-condition scans (scan_storm.json) and field points
+    (field_storm.json) of nudge_sensitivity.json: how far the reference's own
+    results move under a one-ulp change of its math library at storm-range
+    conditions (the bar for GPU tests at those conditions)."""
+    path = os.path.join(HERE, "nudge_sensitivity.json")
+    with open(path) as f:
+        out = json.load(f)
+    with open(os.path.join(HERE, "scan_storm.json")) as f:
+        g = json.load(f)
+    models = ct.model_set(ct.INTERNAL_SH, ct.EXTERNAL_TS05)
+    stats = []
+    for seed in out["seeds"]:
+        n_agree = n_traj = ok = n_sites = 0
+        for c in g["conditions"]:
+            p = ct.internal_setup(g["model"], c["time"], parmod=c["parmod"])
+            jobs = np.concatenate([ct.make_job(s["lat"], s["lon"], rig=g["rig"], rk=g["rk"], dele=g["del"],
+                                               the1=s["the1"], fi1=s["fi1"]) for s in c["sites"]])
+            res = pyoracle.scan_batch_nudged(jobs, p, models, seed)
+            fa, so = _scan_agreement({"del": g["del"], "sites": c["sites"]}, res)
+            nt = len(res.status)
+            n_agree += fa * nt
+            n_traj += nt
+            ok += so * len(c["sites"])
+            n_sites += len(c["sites"])
+        stats.append((n_agree / n_traj, ok / n_sites))
+    out["scans"]["scan_storm.json"] = {"flag_agreement": [a for a, _ in stats],
+                                       "sites_within_one_step": [b for _, b in stats]}
+    print("scan_storm.json", stats)
+    with open(os.path.join(HERE, "field_storm.json")) as f:
+        st = json.load(f)
+    lib = pyoracle.load_nudge()
+    out["fields_storm"] = {}
+    for model, fn in (("t96", lib.orc_t96_gsm), ("ts05", lib.orc_ts05_gsm)):
+        per_case = []
+        for case in st[model]:
+            pm = np.array([float.fromhex(v) for v in case["parmod"]])
+            pts = np.array([float.fromhex(v) for v in case["points"]]).reshape(-1, 3)
+            want = np.array([float.fromhex(v) for v in case["b"]]).reshape(-1, 3)
+            b = np.zeros(3)
+            worst = np.zeros(len(pts))
+            for seed in range(1, 9):
+                lib.orc_nudge_seed(seed)
+                for i, (x, y, z) in enumerate(pts):
+                    fn(pm.ctypes.data, x, y, z, b[0:].ctypes.data, b[1:].ctypes.data, b[2:].ctypes.data)
+                    rel = np.linalg.norm(b - want[i]) / max(np.linalg.norm(want[i]), 1e-300)
+                    worst[i] = max(worst[i], rel)
+            per_case.append(hx(worst))
+            print(model, case["time"], "median", np.median(worst), "max", worst.max())
+        out["fields_storm"][model] = per_case
+    return out
+
+
 def make_nudge_extra() -> dict:
     """The CHAOS scan and field and the calculate_field cases of
     nudge_sensitivity.json (kept apart from `nudge`: each nudged crustal scan
@@ -547,6 +600,7 @@ def main(sections):
         "cli_errors": ("cli_errors.json", make_cli_errors),
         "nudge": ("nudge_sensitivity.json", make_nudge),
         "nudge_extra": ("nudge_sensitivity.json", make_nudge_extra),
+        "nudge_storm": ("nudge_sensitivity.json", make_nudge_storm),
     }
     for s in sections or list(todo):
         fn, mk = todo[s]
