@@ -21,7 +21,7 @@ With a request log (RequestLog) every queued, rejected and completed request
 is on disk, and a stopped server resumes from it without losing work (only
 the batches in flight at the stop run again).
 
-    python cor-model_gb300/serve.py --rate 2 --requests 40 [--window FILE] [--log FILE [--resume]]
+    python cor-model_gb300/serve.py --rate 2 --requests 40 [--window FILE ...] [--log FILE [--resume]]
 """
 from __future__ import annotations
 
@@ -225,12 +225,15 @@ class Server:
     """Continuous batching over `slots` contexts under an HBM budget."""
 
     def __init__(self, device: int = 0, slots: int = 3, hbm_budget: float = 40e9, max_batch_traj: int = 2_000_000,
-                 window_model: window.WindowModel | None = None, executor=None, log: RequestLog | None = None):
+                 window_model=None, executor=None, log: RequestLog | None = None):
         self.budget = int(hbm_budget)
         self.log = log
         self.in_flight = 0
         self.max_batch_traj = max_batch_traj
-        self.window_model = window_model
+        # one window network per external field model (WindowModel.external):
+        # a single network or several
+        models = window_model if isinstance(window_model, (list, tuple)) else [window_model]
+        self.window_models = {getattr(m, "external", None): m for m in models if m is not None}
         self.lock = threading.Condition()
         self.waiting: list[Request] = []
         self.closed = False
@@ -252,10 +255,11 @@ class Server:
 
     # -- the GPU path: one call per batch, windows first when a model is loaded
     def _gpu_execute(self, ctx, jobs, params, models, feats):
-        if self.window_model is None or feats is None:
+        wm = self.window_models.get(models.external_model)
+        if wm is None or feats is None:
             res = ctx.trace_batch(jobs, params, models=models, want_status=False)
             return res.sites, np.zeros(len(jobs), bool)
-        i_lo, i_hi = self.window_model.windows(feats)
+        i_lo, i_hi = wm.windows(feats)
         sites, fb, _, _ = window.trace_windows(ctx, jobs, params, models, i_lo, i_hi)
         return sites, fb
 
@@ -327,7 +331,7 @@ class Server:
                 jobs = np.concatenate([request_jobs(r, k) for k, r in enumerate(reqs)])
                 feats = None
                 # windows only for requests of the field model the network was trained with
-                if self.window_model is not None and getattr(self.window_model, "external", None) == ext:
+                if ext in self.window_models:
                     feats = np.concatenate([request_features(r, params[k:k + 1]) for k, r in enumerate(reqs)])
                 sites, fb = self.executor(ctx, jobs, params, ct.model_set(ct.INTERNAL_SH, ext), feats)
                 o = 0
@@ -396,7 +400,8 @@ def main():
     ap.add_argument("--slots", type=int, default=3)
     ap.add_argument("--budget-gb", type=float, default=40.0)
     ap.add_argument("--external", default="ts05", choices=["t96", "ts05"])
-    ap.add_argument("--window", default=None, help="trained window model (train_window.py output)")
+    ap.add_argument("--window", action="append", default=[],
+                    help="trained window model (train_window.py output); repeat for one per field model")
     ap.add_argument("--max-box-sites", type=int, default=16)
     ap.add_argument("--log", default=None, help="request log (JSON lines) to append to")
     ap.add_argument("--resume", action="store_true",
@@ -409,16 +414,16 @@ def main():
         if not args.log:
             ap.error("--resume needs --log")
         restored, reqs = resume(args.log, reqs)
-    wm = window.WindowModel(args.window) if args.window else None
+    wms = [window.WindowModel(f) for f in args.window]
     log = RequestLog(args.log) if args.log else None
-    srv = Server(0, args.slots, args.budget_gb * 1e9, window_model=wm, log=log)
+    srv = Server(0, args.slots, args.budget_gb * 1e9, window_model=wms, log=log)
     out = run_stream(srv, reqs)
     out.update({"rate": args.rate, "seed": args.seed, "slots": args.slots, "external": args.external,
-                "window": bool(args.window), "restored_from_log": len(restored)})
+                "window": [os.path.basename(f) for f in args.window], "restored_from_log": len(restored)})
     print(json.dumps(out), flush=True)
     if log:
         log.close()
-    if wm:
+    for wm in wms:
         wm.close()
 
 

@@ -4,7 +4,8 @@
 
 1. Seeded site-directions (uniform over the sphere; half vertical, half at
    30 deg zenith and one of 8 azimuths) and conditions (window.sample_conditions:
-   Pdyn, Dst, By, Bz over storm ranges, the tilt through the date), IGRF-14 + T96.
+   Pdyn, Dst, By, Bz (and W1..W6 for TS05) over storm ranges, the tilt through
+   the date), IGRF-14 + T96 or, with --external ts05, IGRF-14 + TS05.
 2. Labels from the plain tracer (log GV), by one of two methods:
    * full (the default): the whole 0.01 GV scan of every sample; its R_U and
      R_L are exactly what the window has to hold;
@@ -138,27 +139,41 @@ def train(x, y, xv, yv, seed, epochs, batch=512, lr=2e-3):
     return params, pv, steps
 
 
+EXTERNALS = {"t96": ct.EXTERNAL_T96, "ts05": ct.EXTERNAL_TS05}
+
+
+def default_paths(external: str, label_method: str) -> tuple[str, str]:
+    """(network file, labels file) for a field model and label method:
+    window_<ext>.npz, and window_<ext>_labels.npz (coarse) or
+    window_<ext>_labels_full.npz (full)."""
+    labels = f"window_{external}_labels.npz" if label_method == "coarse" else f"window_{external}_labels_full.npz"
+    return os.path.join(HERE, f"window_{external}.npz"), os.path.join(HERE, labels)
+
+
 def main():
     ap = argparse.ArgumentParser()
+    ap.add_argument("--external", default="t96", choices=sorted(EXTERNALS),
+                    help="external field model of the samples and labels (IGRF-14 is the internal one)")
     ap.add_argument("--samples", type=int, default=8000)
     ap.add_argument("--val", type=int, default=1000)
     ap.add_argument("--seed", type=int, default=2024)
     ap.add_argument("--epochs", type=int, default=200)
     ap.add_argument("--batch", type=int, default=512)
-    ap.add_argument("--out", default=os.path.join(HERE, "window_t96.npz"))
+    ap.add_argument("--out", default=None, help="default: window_<external>.npz")
     ap.add_argument("--label-method", default="full", choices=["full", "coarse"])
     ap.add_argument("--labels", default=None,
                     help="labelled set: loaded when the file exists, else traced and saved there (default: "
-                         "window_t96_labels.npz for the coarse method, window_t96_labels_full.npz for full)")
+                         "window_<external>_labels.npz for the coarse method, window_<external>_labels_full.npz "
+                         "for full)")
     args = ap.parse_args()
-    if args.labels is None:
-        args.labels = os.path.join(HERE, "window_t96_labels.npz" if args.label_method == "coarse"
-                                   else "window_t96_labels_full.npz")
+    out_default, labels_default = default_paths(args.external, args.label_method)
+    args.out = args.out or out_default
+    args.labels = args.labels or labels_default
     rng = np.random.default_rng(args.seed)
-    models = ct.model_set(ct.INTERNAL_SH, ct.EXTERNAL_T96)
+    models = ct.model_set(ct.INTERNAL_SH, EXTERNALS[args.external])
     t0 = time.time()
-    tr = build_samples(rng, args.samples)
-    va = build_samples(rng, args.val)
+    tr = build_samples(rng, args.samples, args.external)
+    va = build_samples(rng, args.val, args.external)
     if args.labels and os.path.exists(args.labels):
         d = np.load(args.labels)
         assert d["features"].shape == tr["features"].shape, "labels were made for other samples"
@@ -200,7 +215,7 @@ def main():
     info = {"samples": args.samples, "val": args.val, "seed": args.seed, "epochs": args.epochs, "steps": steps,
             "batch": args.batch, "sigma_log_ru": float(sigma[0]), "sigma_log_rl": float(sigma[1]),
             "band_sigma": band_sigma.round(4).tolist(), "heldout_window_miss": float(miss),
-            "model": "igrf14+t96", "label_method": args.label_method, "label_trajectories": n1 + n2,
+            "model": f"igrf14+{args.external}", "label_method": args.label_method, "label_trajectories": n1 + n2,
             "label_seconds": t_label,
             "total_seconds": time.time() - t0}
     np.savez(args.out, params=params, feat_mean=fm, feat_std=fs, y_mean=ym, y_std=ys, sigma=sigma,

@@ -174,3 +174,22 @@ def test_windows_only_for_the_trained_field_model():
     assert out["completed"] == 6
     assert all(used == (ext == ct.EXTERNAL_T96) for ext, used in seen)
     assert {ext for ext, _ in seen} == {ct.EXTERNAL_T96, ct.EXTERNAL_TS05}
+
+
+def test_one_window_network_per_field_model():
+    """With a T96 and a TS05 network, both kinds of request are windowed."""
+    class _M:
+        def __init__(self, ext):
+            self.external = ext
+    seen = []
+
+    def executor(ctx, jobs, params, models, feats):
+        seen.append((models.external_model, feats is not None))
+        res = pyoracle.scan_batch(jobs, params, models=models, threads=2)
+        return res.sites, np.zeros(len(jobs), bool)
+    reqs = _small(serve.poisson_stream(19, 500.0, 4, max_box_sites=4))
+    for k, r in enumerate(reqs):
+        r.external = ct.EXTERNAL_T96 if k % 2 else ct.EXTERNAL_TS05
+    srv = serve.Server(slots=1, executor=executor, window_model=[_M(ct.EXTERNAL_T96), _M(ct.EXTERNAL_TS05)])
+    assert serve.run_stream(srv, reqs)["completed"] == 4
+    assert {ext for ext, _ in seen} == {ct.EXTERNAL_T96, ct.EXTERNAL_TS05} and all(used for _, used in seen)
