@@ -4,10 +4,14 @@ global grid with IGRF-14 + T96 (Pdyn 2 nPa, Dst -20 nT, By 0, Bz -1 nT,
 steps (2,664 sites x 2,000 rigidities = 5.33 M trajectories), FP64.
 
 One step = one batch of sites (the grid split into --batches interleaved
-slices of equal size, taken in turn).  `value` is the device-resident rate
-(inputs uploaded before the timed region, CUDA events on the launch stream);
-`e2e` is the same work through the C ABI call cor_trace_batch with host
-buffers, the host<->device copies inside the timed region.
+slices of equal size, taken in turn).  Every step's batch is one segment of a
+scan stream (cor_stream_*): one resident launch of the scan kernel serves all
+timed steps, its lanes refilling from the next segment as trajectories end.
+`value` is the device-resident rate (inputs in device memory before the timed
+region; the launch timed with CUDA events on its own stream); `e2e` is the
+same work through cor_stream_submit / cor_stream_wait with host buffers, the
+host<->device copies inside the timed region.  `learned_window` scans only the
+windows the trained network predicts, through the same stream.
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
 
@@ -20,6 +24,7 @@ import argparse
 import ctypes as C
 import json
 import os
+import platform
 import statistics
 import subprocess
 import sys
@@ -157,94 +162,114 @@ class ClockSampler:
                 "reasons": sorted(reasons), "samples": len(sm)}
 
 
-def cpu_baseline(n_batches: int, seconds_hint: float = 20.0) -> dict:
-    """The oracle (CPU restatement) on a bounded sample of the same workload,
-    all host threads, one site per thread."""
+def cpu_info() -> dict:
+    """The host's CPU model and its logical and physical core counts (lscpu)."""
+    info = {"model": platform.processor() or platform.machine(), "logical_cpus": os.cpu_count() or 1,
+            "physical_cores": None}
+    try:
+        out = subprocess.run(["lscpu"], capture_output=True, text=True, timeout=10).stdout
+    except (OSError, subprocess.SubprocessError):
+        out = ""
+    f = {}
+    for ln in out.splitlines():
+        k, _, v = ln.partition(":")
+        f.setdefault(k.strip(), v.strip())
+    if f.get("Model name"):
+        info["model"] = f["Model name"]
+    try:
+        info["physical_cores"] = int(f["Core(s) per socket"]) * int(f.get("Socket(s)", "1"))
+    except (KeyError, ValueError):
+        info["physical_cores"] = info["logical_cpus"]
+    return info
+
+
+def reference_params():
+    """The bench condition's parameter block for the CPU arms, taken from the
+    reference's own set-up output (tests/golden/setup_params.json, made by the
+    reference's internal_recalc) so that no product code runs on them."""
+    with open(os.path.join(ROOT, "tests", "golden", "setup_params.json")) as f:
+        cases = json.load(f)["cases"]
+    case = next(c for c in cases if c["version"] == "igrf14" and c["time"] == TIME7)
+    p = np.zeros(1, ct.PARAMS_DTYPE)
+    for k in ("g", "h", "rec", "a1", "a2", "a3"):
+        p[k][0] = [float.fromhex(v) for v in case[k]]
+    p["parmod"][0, :4] = PARMOD
+    return p
+
+
+def cpu_sample_sites(n_batches: int, k: int, n: int) -> list[tuple[float, float]]:
+    """n sites of step k's batch, spread over its latitudes."""
+    sites = batch_sites(k % n_batches, n_batches)
+    stride = max(1, len(sites) // n)
+    return sites[::stride][:n]
+
+
+def cpu_scan(sample, threads: int) -> tuple[float, int]:
+    """The oracle port on `threads` host threads over the sample (chunks of
+    rigidities handed out dynamically); returns (seconds, accepted steps)."""
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import pyoracle
-    threads = os.cpu_count() or 1
-    sites = batch_sites(0, n_batches)
-    # spread the sample over latitudes
-    step = max(1, len(sites) // threads)
-    sample = sites[::step][:threads]
     jobs = make_jobs(sample)
     t = time.perf_counter()
-    res = pyoracle.scan_batch(jobs, params(), models=models(), threads=threads)
-    dt = time.perf_counter() - t
+    res = pyoracle.scan_batch(jobs, reference_params(), models=models(), threads=threads)
+    return time.perf_counter() - t, res.counters["accepted_steps"]
+
+
+CPU_SAMPLE_SITES = 32
+
+
+def cpu_baseline(n_batches: int) -> dict:
+    """The oracle (CPU restatement) on a bounded sample of the same workload,
+    all host threads, rigidities handed out in small chunks as the reference's
+    OpenMP loop does."""
+    info = cpu_info()
+    threads = info["logical_cpus"]
+    sample = cpu_sample_sites(n_batches, 0, CPU_SAMPLE_SITES)
+    dt, steps = cpu_scan(sample, threads)
     return {"value": len(sample) / dt, "unit": UNIT, "cores": threads, "kind": "port",
-            "sample": f"{len(sample)} sites x {N_RIG} rigidities of the same grid and conditions "
-                      f"({res.counters['trajectories']} trajectories, {dt:.1f} s wall)",
-            "steps_per_s": res.counters["accepted_steps"] / dt}
+            "sample": f"{len(sample)} sites x {N_RIG} rigidities of the first step's batch "
+                      f"({len(sample) * N_RIG} trajectories, {dt:.1f} s wall, 4-rigidity chunks over all threads)",
+            "steps_per_s": steps / dt, "cpu": info}
 
 
 # ---- the GPU arm -------------------------------------------------------------
-class Lane:
-    """One in-flight slot: a context with its own stream, work queue and park
-    buffers.  Batches on different slots overlap on the GPU, so one batch's
-    tail of long trajectories runs beside the next batch's bulk."""
-
-    def __init__(self, dev: int, p, tune: dict | None = None):
-        import torch
-        self.torch = torch
-        self.ctx = ct.Context(dev)
-        self.flags = ct.FLAG_UNIFORM_GRID
-        if tune:
-            self.ctx.set_regroup(tune["park_below"], tune["max_generations"], tune["min_park"])
-            self.ctx.set_queue_order(bool(tune["rigidity_major"]))
-            self.flags = ct.FLAG_UNIFORM_GRID if tune["rigidity_major"] else 0
-        self.stream = torch.cuda.Stream(device=dev)
-        rc = self.ctx.lib.cor_upload_params(self.ctx.h, p.ctypes.data, len(p))
-        if rc != 0:
-            raise ct.CorError(rc, self.ctx.error())
-        self.cnt = torch.zeros(5, dtype=torch.int64, device=f"cuda:{dev}")
-
-    def run(self, bf, step_limit: int = 25000) -> None:
-        """Scan one batch (device buffers) on this slot's stream; returns when done."""
-        lib = self.ctx.lib
-        e0 = self.torch.cuda.Event(enable_timing=True)
-        e1 = self.torch.cuda.Event(enable_timing=True)
-        e0.record(self.stream)
-        rc = lib.cor_trace_batch_device(
-            self.ctx.h, bf["jobs"].data_ptr(), bf["trig"].data_ptr(), bf["n_jobs"], bf["off"].data_ptr(), bf["n"],
-            models(), step_limit, 0.01, ct.DEF_HM0_P, bf["sites"].data_ptr(), bf["status"].data_ptr(), None,
-            self.cnt.data_ptr(), self.flags, C.c_void_p(self.stream.cuda_stream))
-        if rc != 0:
-            raise ct.CorError(rc, self.ctx.error())
-        e1.record(self.stream)
-        self.stream.synchronize()
-        bf["counters"] = self.cnt.cpu().numpy().copy()
-        bf["kernel_ms"] = e0.elapsed_time(e1)
-        bf["generations"] = self.ctx.generation_log()
+def stream_settings(n_jobs: int, n_traj: int) -> dict:
+    return {"slots": 8, "max_jobs": max(1, n_jobs), "max_trajectories": max(1, n_traj), "max_params": 1,
+            "fixed_params": 4, "pool_params": 64, "idle_limit_s": 120.0}
 
 
-def run_batches(slots, bufs, order) -> None:
-    """Runs the batches in `order` over the slots, each slot taking the next
-    batch as soon as it is free (one host thread per slot)."""
-    import queue
-    q = queue.Queue()
-    for i in order:
-        q.put(i)
-    errors = []
+def run_device_segments(s, segs) -> list:
+    """Publishes device-resident segments as the ring allows and collects them
+    in order; returns (counters, completion ns) per segment."""
+    from collections import deque
+    out = [None] * len(segs)
+    inflight = deque()
+    nxt = 0
+    while nxt < len(segs) or inflight:
+        while nxt < len(segs) and len(inflight) < s.config.slots:
+            bf = segs[nxt]
+            t = s.submit_device(bf["jobs"].data_ptr(), bf["trig"].data_ptr(), bf["off"].data_ptr(), bf["off_host"],
+                                bf["n_jobs"], bf["sites"].data_ptr(), bf["status"].data_ptr())
+            inflight.append((t, nxt))
+            nxt += 1
+        t, i = inflight.popleft()
+        out[i] = s.wait(t, -1)
+    return out
 
-    def worker(slot):
-        while True:
-            try:
-                i = q.get_nowait()
-            except queue.Empty:
-                return
-            try:
-                slot.run(bufs[i])
-            except Exception as e:  # noqa: BLE001
-                errors.append(e)
-                return
 
-    ts = [threading.Thread(target=worker, args=(s,)) for s in slots]
-    for t in ts:
-        t.start()
-    for t in ts:
-        t.join()
-    if errors:
-        raise errors[0]
+def run_host_segments(s, jobs_list, p) -> list:
+    """cor_stream_submit of host batches, results copied back to the host."""
+    from collections import deque
+    out = [None] * len(jobs_list)
+    inflight = deque()
+    nxt = 0
+    while nxt < len(jobs_list) or inflight:
+        while nxt < len(jobs_list) and len(inflight) < s.config.slots:
+            inflight.append((s.submit(jobs_list[nxt], p), nxt))
+            nxt += 1
+        t, i = inflight.popleft()
+        out[i] = s.wait(t, -1)[0]
+    return out
 
 
 def site_features(latlon) -> np.ndarray:
@@ -255,42 +280,28 @@ def site_features(latlon) -> np.ndarray:
     return np.array([window.features(lat, lon, 0.0, 0.0, ep, PARMOD, tilt) for lat, lon in latlon])
 
 
-def measure_window(args, slots, bufs, p, plain_e2e: float) -> dict:
-    """The learned window on the timed batches: predicted windows traced
-    through cor_trace_batch (host buffers, like e2e), full-scan fallback on
-    an edge hit, R_C compared with the plain scan of the same sites."""
-    import queue
+def measure_window(args, s, bufs, plain, p, plain_e2e: float) -> dict:
+    """The learned window on the timed segments: windows predicted by the
+    network (tensor cores) and traced through the scan stream with host
+    buffers (like e2e), widened on an edge hit (full scan after 3 widenings),
+    R_C compared with the plain scan of the same sites."""
     wm = window.WindowModel(args.window)
     timed = list(range(args.warmup, args.warmup + args.steps))
     feats = {i: site_features(bufs[i]["latlon"]) for i in timed}
     wm.windows(feats[timed[0]])                     # load the network's kernels before timing
-    q = queue.Queue()
-    for i in timed:
-        q.put(i)
-    out = {}
-
-    def worker(slot):
-        while True:
-            try:
-                i = q.get_nowait()
-            except queue.Empty:
-                return
-            i_lo, i_hi = wm.windows(feats[i])
-            out[i] = window.trace_windows(slot.ctx, bufs[i]["host_jobs"], p, models(), i_lo, i_hi)
-
     t0 = time.perf_counter()
-    ths = [threading.Thread(target=worker, args=(s,)) for s in slots]
-    for t in ths:
-        t.start()
-    for t in ths:
-        t.join()
-    wall = time.perf_counter() - t0
-    n_sites = agree = fallback = traced = 0
-    full_traj = 0
-    worst = 0.0
+    items = []
     for i in timed:
-        full = bufs[i]["sites"].cpu().numpy().view(ct.SITE_DTYPE)
-        sites, fb, tr, _ = out[i]
+        i_lo, i_hi = wm.windows(feats[i])           # no stream kernel runs now: the network has the SMs
+        items.append((bufs[i]["host_jobs"], p, i_lo, i_hi))
+    out = window.trace_windows_stream(s, items)
+    launch_ms = s.drain()
+    wall = time.perf_counter() - t0
+    n_sites = agree = fallback = traced = full_traj = 0
+    worst = 0.0
+    for k, i in enumerate(timed):
+        full = plain[k].sites
+        sites, fb, tr, _ = out[k]
         d = np.abs(sites["r_cutoff"] - full["r_cutoff"])
         agree += int(np.sum(d <= 0.01 + 1e-9))
         worst = max(worst, float(d.max()))
@@ -303,10 +314,11 @@ def measure_window(args, slots, bufs, p, plain_e2e: float) -> dict:
     return {"value": v, "unit": UNIT, "speedup_vs_plain_e2e": v / plain_e2e if plain_e2e else None,
             "sites": n_sites, "agree_frac_dRc_le_0.01GV": agree / n_sites, "max_abs_dRc_GV": worst,
             "widened_frac": fallback / n_sites, "trajectories_frac_of_full_scan": traced / full_traj,
+            "stream_launch_ms": launch_ms,
             "model": json.loads(wm.info) if wm.info.startswith("{") else wm.info,
             "how": "predicted window +-3 sigma on the 0.01 GV grid, widened on the hit side on an edge hit (full scan "
-                   "after 3 widenings); host buffers through cor_trace_batch, network inference on the tensor cores "
-                   "inside the timed region"}
+                   "after 3 widenings); every timed step's windows through one scan stream with host buffers, "
+                   "network inference on the tensor cores inside the timed region"}
 
 
 def reduce_over_ranks(dist, seconds: float, counts: list, device: str) -> list:
@@ -323,89 +335,86 @@ def reduce_over_ranks(dist, seconds: float, counts: list, device: str) -> list:
     return out
 
 
+def device_segments(torch, dev: int, jobs_list, base: int) -> list:
+    """Each step's inputs and outputs in device memory (jobs refer to the
+    stream's fixed parameter block `base`)."""
+    out = []
+    t = lambda a: torch.from_numpy(np.ascontiguousarray(a).view(np.uint8).copy()).to(f"cuda:{dev}")
+    for jobs, latlon in jobs_list:
+        n, off = ct.batch_offsets(jobs)
+        dj = jobs.copy()
+        dj["param_index"] = base
+        out.append({"n_jobs": len(jobs), "n": n, "jobs": t(dj), "trig": t(ct.prepare_trig(jobs)), "off": t(off),
+                    "off_host": off,
+                    "sites": torch.zeros(len(jobs) * ct.SITE_DTYPE.itemsize, dtype=torch.uint8,
+                                         device=f"cuda:{dev}"),
+                    "status": torch.zeros(n, dtype=torch.uint8, device=f"cuda:{dev}"),
+                    "host_jobs": jobs, "latlon": latlon})
+    return out
+
+
 def run_ours(args, rank: int, world: int, dist) -> dict | None:
     import torch
     dev = int(os.environ.get("LOCAL_RANK", "0"))
     torch.cuda.set_device(dev)
     p = params()
     tune = tuning()
-    if args.inflight is None:
-        args.inflight = tune["inflight"]
-    slots = [Lane(dev, p, tune) for _ in range(args.inflight)]
     mine = rank_batches(rank, world, args.batches)
     n_steps = args.warmup + args.steps
-    bufs = []
-    for k in range(n_steps):
-        b = mine[k % len(mine)]
-        jobs = make_jobs(batch_sites(b, args.batches))
-        n, off = ct.batch_offsets(jobs)
-        trig = ct.prepare_trig(jobs)
-        t = lambda a: torch.from_numpy(a.view(np.uint8).copy()).to(f"cuda:{dev}")
-        bufs.append({
-            "n_jobs": len(jobs), "n": n, "jobs": t(jobs), "trig": t(trig), "off": t(off),
-            "sites": torch.zeros(len(jobs) * ct.SITE_DTYPE.itemsize, dtype=torch.uint8, device=f"cuda:{dev}"),
-            "status": torch.zeros(n, dtype=torch.uint8, device=f"cuda:{dev}"),
-            "host_jobs": jobs, "latlon": batch_sites(b, args.batches),
-        })
+    steps = [(make_jobs(batch_sites(mine[k % len(mine)], args.batches)), batch_sites(mine[k % len(mine)],
+                                                                                   args.batches))
+             for k in range(n_steps)]
+    ctx = ct.Context(dev)
+    ctx.set_queue_order(bool(tune["rigidity_major"]))
     peak = C.c_double(0.0)
-    slots[0].ctx.lib.cor_probe_fp64_peak(slots[0].ctx.h, C.byref(peak))
-
-    run_batches(slots, bufs, range(args.warmup))
+    ctx.lib.cor_probe_fp64_peak(ctx.h, C.byref(peak))
+    max_jobs = max(len(j) for j, _ in steps)
+    s = ct.Stream(ctx, models(), **stream_settings(max_jobs, max_jobs * N_RIG))
+    base = s.upload_params(p)
+    bufs = device_segments(torch, dev, steps, base)
     torch.cuda.synchronize()
+
+    run_device_segments(s, bufs[:args.warmup])      # warm-up launch
+    s.drain()
     if dist:
         dist.barrier(device_ids=[dev])
     torch.cuda.synchronize()
     with ClockSampler(dev) as clocks:
         t0 = time.perf_counter()
-        run_batches(slots, bufs, range(args.warmup, n_steps))
-        torch.cuda.synchronize()
-        dev_s = time.perf_counter() - t0
+        res = run_device_segments(s, bufs[args.warmup:])
+        launch_ms = s.drain()                           # CUDA events around the launch, on its stream
+        host_s = time.perf_counter() - t0
+    dev_s = launch_ms / 1e3
     timed = bufs[args.warmup:]
-    steps_acc = sum(int(b["counters"][0]) for b in timed)
-    trials_acc = sum(int(b["counters"][1]) for b in timed)
-    traj_done = sum(int(b["counters"][2]) for b in timed)
+    steps_acc = sum(int(c["accepted_steps"]) for c, _ in res)
+    trials_acc = sum(int(c["trials"]) for c, _ in res)
+    traj_done = sum(int(c["trajectories"]) for c, _ in res)
     sites_done = sum(b["n_jobs"] for b in timed)
-    launch_ms = [b["kernel_ms"] for b in timed]
+    done_ns = [t_ns for _, t_ns in res]
     if dist:
         dev_s, sites_done, traj_done, steps_acc, trials_acc = reduce_over_ranks(
             dist, dev_s, [sites_done, traj_done, steps_acc, trials_acc], f"cuda:{dev}")
 
-    # e2e through the public C ABI with host buffers (same overlap, one host
-    # thread per slot, cor_trace_batch copies in and out inside the call)
-    h2d = d2h = 0
-    import queue
-    qe = queue.Queue()
-    for i in range(args.warmup, n_steps):
-        qe.put(i)
-    sizes = []
-
-    def e2e_worker(slot):
-        while True:
-            try:
-                i = qe.get_nowait()
-            except queue.Empty:
-                return
-            jobs = bufs[i]["host_jobs"]
-            r = slot.ctx.trace_batch(jobs, p, models=models())
-            sizes.append((jobs.nbytes + len(jobs) * ct.TRIG_DTYPE.itemsize + (len(jobs) + 1) * 8 + p.nbytes,
-                          r.sites.nbytes + r.status.nbytes + 40))
-
+    # e2e through the public C ABI with host buffers: cor_stream_submit copies
+    # each step's inputs in and cor_stream_wait its results out, inside the
+    # timed region
     t0 = time.perf_counter()
-    ths = [threading.Thread(target=e2e_worker, args=(s,)) for s in slots]
-    for t in ths:
-        t.start()
-    for t in ths:
-        t.join()
+    plain = run_host_segments(s, [b["host_jobs"] for b in timed], p)
+    e2e_launch_ms = s.drain()
     e2e_s = time.perf_counter() - t0
-    h2d = sum(a for a, _ in sizes)
-    d2h = sum(b for _, b in sizes)
+    h2d = sum(b["host_jobs"].nbytes + b["n_jobs"] * ct.TRIG_DTYPE.itemsize + (b["n_jobs"] + 1) * 8 + 96 + 8
+              for b in timed) + 3840
+    d2h = sum(r.sites.nbytes + r.status.nbytes + 64 for r in plain)
     if dist:
         e2e_s = reduce_over_ranks(dist, e2e_s, [], f"cuda:{dev}")[0]
+    for r, b in zip(plain, timed):
+        # the device-resident run and the host-buffer run are the same scans
+        assert np.array_equal(r.sites.view(np.uint8), b["sites"].cpu().numpy()), "e2e and device results differ"
     learned = None
     if args.window and os.path.exists(args.window) and world == 1:
-        learned = measure_window(args, slots, bufs, p, sites_done / e2e_s)
-    for s in slots:
-        s.ctx.close()
+        learned = measure_window(args, s, bufs, plain, p, sites_done / e2e_s)
+    s.close()
+    ctx.close()
     if rank != 0:
         return None
     wm = work_model()
@@ -419,12 +428,15 @@ def run_ours(args, rank: int, world: int, dist) -> dict | None:
         "data": "synthetic grid of sites (the configuration's own sites; no dataset)",
         "config": {"workload": WORKLOAD, "sites_per_step": sites_done // max(1, args.steps * world),
                    "trajectories_per_step": traj_done // max(1, args.steps * world),
-                   "batches": args.batches, "inflight": args.inflight, "tuning": tune,
+                   "batches": args.batches, "tuning": tune,
+                   "execution": "one persistent scan-stream launch per timed run: every step's batch is a segment "
+                                "published to the resident kernel, whose lanes refill from the next segment as "
+                                "trajectories end",
                    "l2": "no L2 flush: the kernel is FP64-bound and its state lives in registers; inputs and "
                          "outputs are MB-sized", "parallelism": f"sites split over {world} GPU(s)"},
         "trajectories_per_s": traj_done / dev_s, "steps_per_s": steps_acc / dev_s,
-        "batch_kernel_ms": launch_ms,
-        "batch_generations": [[(n, round(ms, 1)) for n, ms in b.get("generations", [])] for b in timed[:1]],
+        "timing": {"launch_ms_cuda_events": launch_ms, "host_wall_s": host_s,
+                   "segment_done_s": [round((t - done_ns[0]) / 1e9, 3) for t in done_ns]},
         "roofline": {"bound": "fp64", "achieved": achieved, "peak": peak.value / 1e12, "unit": "TFLOP/s",
                      "frac": achieved / (peak.value / 1e12) if peak.value else None,
                      "traffic": DRAM_BYTES_PER_TRAJ * traj_done / max(1, args.steps * world),
@@ -434,8 +446,9 @@ def run_ours(args, rank: int, world: int, dist) -> dict | None:
                      "flops_per_step": wm["flops_per_step"],
                      "peak_source": "DFMA microbenchmark in libcortrace (cor_probe_fp64_peak), FMA = 2 flops"},
         "e2e": {"value": sites_done / e2e_s, "unit": UNIT,
-                "h2d_bytes_per_step": h2d // args.steps, "d2h_bytes_per_step": d2h // args.steps},
-        "gpu_launches": sum(int(b["counters"][4]) for b in timed),
+                "h2d_bytes_per_step": h2d // args.steps, "d2h_bytes_per_step": d2h // args.steps,
+                "stream_launch_ms": e2e_launch_ms},
+        "gpu_launches": 1,
         "clocks": clocks.summary(),
     }
     if learned is not None:
@@ -445,7 +458,7 @@ def run_ours(args, rank: int, world: int, dist) -> dict | None:
     return out
 
 
-# ---- small case of the same kernel, for profiler captures ---------------------
+# ---- small cases of the same kernels, for profiler captures -------------------
 PROFILE_SITES = 32
 PROFILE_STEP_LIMIT = 2500
 
@@ -453,50 +466,76 @@ PROFILE_STEP_LIMIT = 2500
 def run_profile_case(args) -> dict:
     """PROFILE_SITES sites spread over all latitudes x the 2,000 rigidities, with
     the step limit lowered to PROFILE_STEP_LIMIT so that a launch lasts about a
-    second: the bulk of the scan kernel's work without the 25,000-step tail.
+    second: the bulk of the scan's work without the 25,000-step tail.  With
+    --profile-stream the same scans go through a scan stream staged before its
+    launch (launch_on_drain), so the launch never waits on the host and a
+    profiler can replay it; otherwise through cor_trace_batch_device.
     Not a bench line; it exists to be captured under ncu."""
     import torch
     dev = int(os.environ.get("LOCAL_RANK", "0"))
     torch.cuda.set_device(dev)
     p = params()
-    slot = Lane(dev, p)
     sites = grid_sites()[::len(grid_sites()) // PROFILE_SITES][:PROFILE_SITES]
     jobs = make_jobs(sites)
-    n, off = ct.batch_offsets(jobs)
-    t = lambda a: torch.from_numpy(a.view(np.uint8).copy()).to(f"cuda:{dev}")
-    bf = {"n_jobs": len(jobs), "n": n, "jobs": t(jobs), "trig": t(ct.prepare_trig(jobs)), "off": t(off),
-          "sites": torch.zeros(len(jobs) * ct.SITE_DTYPE.itemsize, dtype=torch.uint8, device=f"cuda:{dev}"),
-          "status": torch.zeros(n, dtype=torch.uint8, device=f"cuda:{dev}")}
+    ctx = ct.Context(dev)
     ms = []
-    for _ in range(args.warmup + args.steps):
-        slot.run(bf, step_limit=PROFILE_STEP_LIMIT)
-        ms.append(bf["kernel_ms"])
-    c = bf["counters"]
-    slot.ctx.close()
+    if args.profile_stream:
+        parts = [jobs[k::4] for k in range(4)]
+        s = ct.Stream(ctx, models(), step_limit=PROFILE_STEP_LIMIT, launch_on_drain=1,
+                      **stream_settings(len(parts[0]), len(parts[0]) * N_RIG))
+        base = s.upload_params(p)
+        bufs = device_segments(torch, dev, [(j, None) for j in parts], base)
+        for _ in range(args.warmup + args.steps):
+            ts = [s.submit_device(b["jobs"].data_ptr(), b["trig"].data_ptr(), b["off"].data_ptr(), b["off_host"],
+                                  b["n_jobs"], b["sites"].data_ptr(), b["status"].data_ptr()) for b in bufs]
+            ms.append(s.drain())
+            c = [s.wait(t, 0)[0] for t in ts]
+        s.close()
+        c = {k: sum(x[k] for x in c) for k in c[0]}
+    else:
+        n, off = ct.batch_offsets(jobs)
+        t = lambda a: torch.from_numpy(a.view(np.uint8).copy()).to(f"cuda:{dev}")
+        ctx._check(ctx.lib.cor_upload_params(ctx.h, p.ctypes.data, len(p)), "cor_upload_params")
+        dj, dt, do = t(jobs), t(ct.prepare_trig(jobs)), t(off)
+        sites_d = torch.zeros(len(jobs) * ct.SITE_DTYPE.itemsize, dtype=torch.uint8, device=f"cuda:{dev}")
+        status = torch.zeros(n, dtype=torch.uint8, device=f"cuda:{dev}")
+        cnt = torch.zeros(5, dtype=torch.int64, device=f"cuda:{dev}")
+        st = torch.cuda.current_stream()
+        for _ in range(args.warmup + args.steps):
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(st)
+            rc = ctx.lib.cor_trace_batch_device(ctx.h, dj.data_ptr(), dt.data_ptr(), len(jobs), do.data_ptr(), n,
+                                                models(), PROFILE_STEP_LIMIT, 0.01, ct.DEF_HM0_P,
+                                                sites_d.data_ptr(), status.data_ptr(), None, cnt.data_ptr(),
+                                                ct.FLAG_UNIFORM_GRID, C.c_void_p(st.cuda_stream))
+            ctx._check(rc, "cor_trace_batch_device")
+            e1.record(st)
+            torch.cuda.synchronize()
+            ms.append(e0.elapsed_time(e1))
+        v = cnt.cpu().numpy()
+        c = dict(zip(("accepted_steps", "trials", "trajectories", "watchdog", "kernel_launches"), v.tolist()))
+    ctx.close()
     return {"profile_case": f"{len(sites)} sites x {N_RIG} rigidities, step limit {PROFILE_STEP_LIMIT}",
-            "trajectories": int(c[2]), "accepted_steps": int(c[0]), "trials": int(c[1]),
-            "kernel_launches": int(c[4]), "call_ms": ms}
+            "path": "stream" if args.profile_stream else "batch",
+            "trajectories": int(c["trajectories"]), "accepted_steps": int(c["accepted_steps"]),
+            "trials": int(c["trials"]), "call_ms": ms}
 
 
 def run_reference(args, rank: int) -> dict | None:
-    """CPU reference arm: the oracle port on the host cores, bounded samples."""
+    """CPU reference arm: the oracle port on all host threads, one bounded
+    sample per step (CPU_SAMPLE_SITES sites of that step's batch)."""
     if rank != 0:
         return None
-    sys.path.insert(0, os.path.join(ROOT, "oracle"))
-    import pyoracle
-    threads = os.cpu_count() or 1
-    sites = batch_sites(0, args.batches)
-    stride = max(1, len(sites) // (threads * max(1, args.steps + args.warmup)))
-    p = params()
+    info = cpu_info()
+    threads = info["logical_cpus"]
     done = 0
     dt_tot = 0.0
     steps = 0
+    n_sample = 0
     for i in range(args.warmup + args.steps):
-        sample = sites[(i * threads) % len(sites)::stride][:threads]
-        jobs = make_jobs(sample)
-        t = time.perf_counter()
-        pyoracle.scan_batch(jobs, p, models=models(), threads=threads)
-        dt = time.perf_counter() - t
+        sample = cpu_sample_sites(args.batches, i, CPU_SAMPLE_SITES)
+        n_sample = len(sample)
+        dt, _ = cpu_scan(sample, threads)
         if i >= args.warmup:
             done += len(sample)
             dt_tot += dt
@@ -506,10 +545,11 @@ def run_reference(args, rank: int) -> dict | None:
             "warmup": args.warmup, "ms_per_step": dt_tot * 1e3 / max(1, steps), "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic grid of sites",
             "impl": "reference",
-            "config": {"workload": WORKLOAD, "sites_per_step": threads,
+            "config": {"workload": WORKLOAD, "sites_per_step": n_sample,
                        "devices": "host cores of rank 0 only; no GPU work"},
-            "cpu_baseline": {"value": v, "unit": UNIT, "cores": threads, "kind": "port",
-                             "sample": f"{threads} sites x {N_RIG} rigidities per step, one site per thread"},
+            "cpu_baseline": {"value": v, "unit": UNIT, "cores": threads, "kind": "port", "cpu": info,
+                             "sample": f"{n_sample} sites x {N_RIG} rigidities of each step's batch, "
+                                       f"4-rigidity chunks handed out over all threads"},
             "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
 
 
@@ -518,15 +558,16 @@ def main():
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=4)
     ap.add_argument("--warmup", type=int, default=3)
-    ap.add_argument("--batches", type=int, default=16)
-    ap.add_argument("--inflight", type=int, default=None,
-                    help="batches in flight at once (one stream each; default: the autotuner's choice, else 3)")
+    ap.add_argument("--batches", type=int, default=32,
+                    help="the grid is split into this many interleaved batches; one step scans one batch")
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--window", default=WINDOW_FILE, help="trained window model for the learned-window line "
                     "(train_window.py output); skipped when the file is absent")
     ap.add_argument("--profile-case", action="store_true",
                     help="run only the small profiling case of the scan kernel (prints its own JSON, not a bench line)")
+    ap.add_argument("--profile-stream", action="store_true",
+                    help="with --profile-case: through a scan stream launched with everything staged")
     args = ap.parse_args()
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))

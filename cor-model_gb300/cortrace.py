@@ -17,7 +17,9 @@ PKG = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(PKG, "libcortrace.so")
 
 COR_OK = 0
-ERRORS = {-1: "invalid", -2: "nomem", -3: "cuda", -4: "watchdog", -5: "nodev", -6: "unsupported", -7: "range"}
+ERRORS = {-1: "invalid", -2: "nomem", -3: "cuda", -4: "watchdog", -5: "nodev", -6: "unsupported", -7: "range",
+          -8: "busy"}
+COR_PENDING = 1
 
 INTERNAL_NONE, INTERNAL_SH = 0, 1
 EXTERNAL_NONE, EXTERNAL_T96, EXTERNAL_TS05 = 0, 1, 2
@@ -76,6 +78,14 @@ class BatchReq(C.Structure):
                 ("particle_mass", C.c_double)]
 
 
+class StreamConfig(C.Structure):
+    """cor_stream_config (include/cor_trace.h)."""
+    _fields_ = [("slots", C.c_int32), ("max_jobs", C.c_int32), ("max_trajectories", C.c_int64),
+                ("max_params", C.c_int32), ("want_records", C.c_int32), ("reserve_sms", C.c_int32),
+                ("fixed_params", C.c_int32), ("pool_params", C.c_int32), ("segments_per_launch", C.c_int32),
+                ("idle_limit_s", C.c_double), ("launch_on_drain", C.c_int32), ("reserved", C.c_int32)]
+
+
 class BatchResult(C.Structure):
     _fields_ = [("sites", C.c_void_p), ("status", C.c_void_p), ("records", C.c_void_p), ("counters", Counters)]
 
@@ -86,7 +96,9 @@ EXPORTS = [
     "cor_prepare_trig", "cor_trace_batch", "cor_trace_batch_device", "cor_upload_params", "cor_field_batch",
     "cor_internal_setup", "cor_gsm_setup", "cor_probe_fp64_peak", "cor_upload_crustal",
     "cor_trace_batch_device_noalloc", "cor_ctx_set_regroup", "cor_trace_steps", "cor_ctx_set_queue_order",
-    "cor_ctx_generation_log",
+    "cor_ctx_generation_log", "cor_stream_config_default", "cor_stream_create", "cor_stream_submit",
+    "cor_stream_upload_params", "cor_stream_submit_device", "cor_stream_wait", "cor_stream_drain",
+    "cor_stream_close",
 ]
 NOALLOC_MAX_TRAJ = 1048576  # COR_NOALLOC_MAX_TRAJ
 
@@ -125,6 +137,15 @@ def load(path: str = LIB_PATH) -> C.CDLL:
     lib.cor_field_batch.argtypes = [vp, ModelSet, vp, i32, vp, vp, i64, vp]
     lib.cor_internal_setup.argtypes = [C.c_char_p, vp, vp]
     lib.cor_gsm_setup.argtypes = [vp, vp]
+    lib.cor_stream_config_default.argtypes = [C.POINTER(StreamConfig)]
+    lib.cor_stream_config_default.restype = None
+    lib.cor_stream_create.argtypes = [vp, ModelSet, u64, dbl, dbl, C.POINTER(StreamConfig), C.POINTER(vp)]
+    lib.cor_stream_submit.argtypes = [vp, vp, i32, vp, i32, C.POINTER(i64)]
+    lib.cor_stream_upload_params.argtypes = [vp, vp, i32, C.POINTER(i32)]
+    lib.cor_stream_submit_device.argtypes = [vp, vp, vp, vp, vp, i32, vp, vp, vp, C.POINTER(i64)]
+    lib.cor_stream_wait.argtypes = [vp, i64, i32, C.POINTER(BatchResult), C.POINTER(u64)]
+    lib.cor_stream_drain.argtypes = [vp, C.POINTER(C.c_double)]
+    lib.cor_stream_close.argtypes = [vp]
     _lib = lib
     return lib
 
@@ -294,6 +315,104 @@ class Context:
                                       _ptr(pos), len(pos), _ptr(out))
         self._check(rc, "field_batch")
         return out
+
+
+class Stream:
+    """A persistent scan stream (cor_stream_*): one resident launch of the scan
+    kernel that traces every submitted batch of scans as it arrives.  Results
+    are those of Context.trace_batch, bit for bit."""
+
+    def __init__(self, ctx: Context, models: ModelSet | None = None, step_limit: int = 25000,
+                 tu_angle: float = 0.01, particle_mass: float = DEF_HM0_P, **cfg):
+        self.ctx = ctx
+        self.lib = ctx.lib
+        c = StreamConfig()
+        self.lib.cor_stream_config_default(C.byref(c))
+        for k, v in cfg.items():
+            if not hasattr(c, k):
+                raise TypeError(f"unknown stream setting {k}")
+            setattr(c, k, v)
+        self.config = c
+        h = C.c_void_p()
+        ctx._check(self.lib.cor_stream_create(ctx.h, models or model_set(), step_limit, tu_angle, particle_mass,
+                                              C.byref(c), C.byref(h)), "cor_stream_create")
+        self.h = h
+        self._pending: dict[int, tuple] = {}
+
+    def submit(self, jobs: np.ndarray, params: np.ndarray, want_status: bool = True,
+               want_records: bool = False) -> int:
+        """cor_stream_submit: publishes a batch; returns its ticket."""
+        if want_records and not self.config.want_records:
+            raise ValueError("records need a stream created with want_records=1")
+        jobs = np.ascontiguousarray(jobs, JOB_DTYPE)
+        params = np.ascontiguousarray(params, PARAMS_DTYPE)
+        n, off = batch_offsets(jobs) if len(jobs) else (0, np.zeros(1, np.uint64))
+        t = C.c_int64(-1)
+        self.ctx._check(self.lib.cor_stream_submit(self.h, _ptr(jobs), len(jobs), _ptr(params), len(params),
+                                                   C.byref(t)), "cor_stream_submit")
+        self._pending[t.value] = (len(jobs), n, off, want_status, want_records)
+        return t.value
+
+    def upload_params(self, params: np.ndarray) -> int:
+        """cor_stream_upload_params: fixed pool index of params[0]."""
+        params = np.ascontiguousarray(params, PARAMS_DTYPE)
+        first = C.c_int32(-1)
+        self.ctx._check(self.lib.cor_stream_upload_params(self.h, _ptr(params), len(params), C.byref(first)),
+                        "cor_stream_upload_params")
+        return first.value
+
+    def submit_device(self, jobs_dev: int, trig_dev: int, offsets_dev: int, offsets_host: np.ndarray, n_jobs: int,
+                      sites_dev: int, status_dev: int, records_dev: int | None = None) -> int:
+        """cor_stream_submit_device: buffers already in device memory (pointers)."""
+        offsets_host = np.ascontiguousarray(offsets_host, np.uint64)
+        t = C.c_int64(-1)
+        self.ctx._check(self.lib.cor_stream_submit_device(self.h, jobs_dev, trig_dev, offsets_dev,
+                                                          _ptr(offsets_host), n_jobs, sites_dev, status_dev,
+                                                          records_dev, C.byref(t)), "cor_stream_submit_device")
+        self._pending[t.value] = None
+        return t.value
+
+    def wait(self, ticket: int, timeout_ms: int = -1):
+        """cor_stream_wait: None while pending; else (ScanResult or None for a
+        device segment, completion time [ns of the device clock])."""
+        meta = self._pending.get(ticket, ())
+        t_ns = C.c_uint64(0)
+        if meta:
+            n_jobs, n, off, want_status, want_records = meta
+            sites = np.zeros(n_jobs, SITE_DTYPE)
+            status = np.zeros(n, np.uint8) if want_status else None
+            records = np.zeros(n, RECORD_DTYPE) if want_records else None
+            res = BatchResult(_ptr(sites), _ptr(status), _ptr(records), Counters())
+        else:
+            res = BatchResult(None, None, None, Counters())
+        rc = self.lib.cor_stream_wait(self.h, ticket, timeout_ms, C.byref(res), C.byref(t_ns))
+        if rc == COR_PENDING:
+            return None
+        self.ctx._check(rc, "cor_stream_wait")
+        self._pending.pop(ticket, None)
+        if meta:
+            return ScanResult(sites, status, records, off, res.counters.as_dict()), int(t_ns.value)
+        return res.counters.as_dict(), int(t_ns.value)
+
+    def drain(self) -> float:
+        """cor_stream_drain: ends the current launch once everything published
+        has finished; returns its duration in ms (CUDA events on the kernel's
+        stream)."""
+        ms = C.c_double(0.0)
+        self.ctx._check(self.lib.cor_stream_drain(self.h, C.byref(ms)), "cor_stream_drain")
+        return ms.value
+
+    def close(self):
+        if getattr(self, "h", None):
+            rc = self.lib.cor_stream_close(self.h)
+            self.h = None
+            self.ctx._check(rc, "cor_stream_close")
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
 
 
 def make_job(lat, lon, rig=0.05, rk=20.0, dele=0.05, r0=1.0031391260673028, the1=None, fi1=None,

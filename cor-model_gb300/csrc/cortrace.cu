@@ -10,9 +10,10 @@
 #include <stdio.h>
 #include <stdlib.h>
 #include <string.h>
+#include <time.h>
 
 #include "model_ops.h"
-#include "reduce.cuh"
+#include "reduce_kernels.cuh"
 #include "model_prep.h"
 #include "ts05_tables.h"
 
@@ -339,17 +340,23 @@ static int launch_trace(cor_ctx* ctx, const ModelOps* ops, TraceArgs a, cudaStre
 static int launch_scan(cor_ctx* ctx, const TraceArgs& a, cor_model_set models, cor_site_result* sites, cudaStream_t s) {
     CUDA_TRY(ctx, cudaMemsetAsync(a.queue, 0, sizeof(unsigned long long), s));
     CUDA_TRY(ctx, cudaMemsetAsync(a.counters, 0, sizeof(cor_counters), s));
+    unsigned long long checks = 0;
+    if (a.rig_major && a.grid_ok) {
+        grid_check_kernel<<<1, 256, 0, s>>>(a.offsets, a.n_jobs, a.n_traj, const_cast<unsigned int*>(a.grid_ok));
+        CUDA_TRY(ctx, cudaGetLastError());
+        checks = 1;
+    }
     if (a.n_traj > 0) {
         const ModelOps* ops = find_ops(models);
         if (!ops) return fail(ctx, COR_ERR_UNSUPPORTED, "model set not available");
         const int rc = launch_trace(ctx, ops, a, s);
         if (rc != COR_OK) return rc;
     }
-    unsigned long long launches = a.n_traj > 0 ? (unsigned long long)ctx->generations : 0ull;
+    unsigned long long launches = checks + (a.n_traj > 0 ? (unsigned long long)ctx->generations : 0ull);
     if (a.n_jobs > 0) {
         const int threads = 256;
         const int blocks = (int)(((int64_t)a.n_jobs * 32 + threads - 1) / threads);
-        reduce_kernel<<<blocks, threads, 0, s>>>(a.jobs, a.offsets, a.n_jobs, a.status, sites);
+        reduce_kernel<<<blocks, threads, 0, s>>>(a.jobs, a.offsets, a.n_jobs, a.n_traj, a.status, sites);
         CUDA_TRY(ctx, cudaGetLastError());
         launches += 1;
     }
@@ -524,6 +531,9 @@ extern "C" int cor_trace_batch_device(cor_ctx* ctx, const cor_scan_job* jobs_dev
         if (rc != COR_OK) return rc;
     }
     a.rig_major = ((flags & COR_FLAG_UNIFORM_GRID) && a.n_rig > 0) ? 1 : 0;
+    // the flag is checked on the device against the offsets (grid_check_kernel)
+    // in the 256-byte scratch block of the work-queue counter
+    a.grid_ok = a.rig_major ? reinterpret_cast<const unsigned int*>(ctx->queue + 1) : nullptr;
     return launch_scan(ctx, a, models, sites_dev, (cudaStream_t)stream);
 }
 
@@ -798,6 +808,7 @@ extern "C" int cor_trace_batch_device_noalloc(cor_ctx* ctx, const cor_scan_job* 
     a.n_rig = 0;
     if (n_jobs > 0 && n_traj % (uint64_t)n_jobs == 0) a.n_rig = (uint32_t)(n_traj / (uint64_t)n_jobs);
     a.rig_major = ((flags & COR_FLAG_UNIFORM_GRID) && a.n_rig > 0) ? 1 : 0;
+    a.grid_ok = a.rig_major ? reinterpret_cast<const unsigned int*>(&head->pad0[0]) : nullptr;
     a.mass = particle_mass;
     a.status = status;
     a.records = records_dev;
@@ -815,6 +826,11 @@ extern "C" int cor_trace_batch_device_noalloc(cor_ctx* ctx, const cor_scan_job* 
     CUDA_TRY(ctx, cudaMemsetAsync(scratch, 0, kNoAllocHead, s));
     if (counters_dev) CUDA_TRY(ctx, cudaMemsetAsync(counters_dev, 0, sizeof(cor_counters), s));
     unsigned long long launches = 0;
+    if (a.rig_major) {
+        grid_check_kernel<<<1, 256, 0, s>>>(offsets_dev, n_jobs, n_traj, reinterpret_cast<unsigned int*>(&head->pad0[0]));
+        CUDA_TRY(ctx, cudaGetLastError());
+        launches++;
+    }
     if (n_traj > 0) {
         const ModelOps* ops = find_ops(models);
         if (!ops) return fail(ctx, COR_ERR_UNSUPPORTED, "model set not available");
@@ -834,11 +850,607 @@ extern "C" int cor_trace_batch_device_noalloc(cor_ctx* ctx, const cor_scan_job* 
     if (n_jobs > 0) {
         const int threads = 256;
         const int blocks = (int)(((int64_t)n_jobs * 32 + threads - 1) / threads);
-        reduce_kernel<<<blocks, threads, 0, s>>>(jobs_dev, offsets_dev, n_jobs, status, sites_dev);
+        reduce_kernel<<<blocks, threads, 0, s>>>(jobs_dev, offsets_dev, n_jobs, n_traj, status, sites_dev);
         CUDA_TRY(ctx, cudaGetLastError());
         launches++;
     }
     noalloc_launches_kernel<<<1, 1, 0, s>>>(a.counters, launches + 1);
     CUDA_TRY(ctx, cudaGetLastError());
     return COR_OK;
+}
+
+// ---- persistent scan stream (stream.cuh) ------------------------------------
+// One launch of stream_kernel serves every segment the caller publishes until
+// cor_stream_close (or a restart when the launch's parameter pool or segment
+// table is full).  The host writes a segment's inputs and its descriptor with
+// copies on the copy stream, waits for them, and only then moves the
+// published end forward with a release store into mapped pinned memory; the
+// kernel reads that end with an acquire load.  The kernel writes each
+// segment's completion record into mapped pinned memory with a release store.
+// Nothing here launches other kernels or allocates once the stream exists:
+// the stream kernel may hold every SM.
+
+namespace {
+
+struct StreamSlot {
+    // device buffers of cor_stream_submit segments, and per-segment scratch
+    cor_scan_job* jobs = nullptr;
+    JobTrig* trig = nullptr;
+    uint64_t* off = nullptr;
+    cor_site_result* sites = nullptr;
+    uint8_t* status = nullptr;
+    cor_traj_record* records = nullptr;
+    unsigned int* job_done = nullptr;
+    unsigned long long* acc = nullptr;
+    // pinned staging
+    cor_scan_job* h_jobs = nullptr;
+    JobTrig* h_trig = nullptr;
+    uint64_t* h_off = nullptr;
+    cor_site_result* h_sites = nullptr;
+    uint8_t* h_status = nullptr;
+    cor_traj_record* h_records = nullptr;
+    StreamSeg* h_seg = nullptr;
+    unsigned long long* h_end = nullptr;
+    // state
+    int64_t seq = -1;
+    bool busy = false;   // submitted and not yet collected
+    bool own = false;    // outputs in this slot's buffers (cor_stream_submit)
+    bool empty = false;  // a segment without scans: complete at once
+    int32_t n_jobs = 0;
+    uint64_t n_traj = 0;
+};
+
+}  // namespace
+
+struct cor_stream {
+    cor_ctx* ctx = nullptr;
+    const ModelOps* ops = nullptr;
+    cor_stream_config cfg;
+    cudaStream_t ks = nullptr;   // the stream kernel
+    cudaStream_t cs = nullptr;   // copies
+    unsigned blocks = 0;
+    StreamSlot* slots = nullptr;
+    StreamSeg* segs_dev = nullptr;
+    unsigned long long* seg_end_dev = nullptr;
+    DevParams* pool_dev = nullptr;     // [fixed_params blocks | pool_params blocks]
+    DevParams* h_params = nullptr;     // pinned staging
+    int32_t h_params_cap = 0;
+    int32_t n_fixed = 0, pool_used = 0;
+    unsigned long long* queue_dev = nullptr;
+    unsigned long long* h_queue = nullptr;
+    void* mapped = nullptr;            // control block, completion records, error word
+    StreamCtl* ctl_h = nullptr;
+    StreamCtl* ctl_d = nullptr;
+    StreamDone* done_h = nullptr;
+    StreamDone* done_d = nullptr;
+    unsigned int* err_h = nullptr;
+    unsigned int* err_d = nullptr;
+    bool running = false;
+    int64_t next_seq = 0, first_seq = 0;
+    uint64_t published = 0, first_index = 0;
+    unsigned char* last_params = nullptr;  // the previous submit's blocks (host copy) for reuse
+    int32_t last_n = 0, last_base = -1;
+    StreamArgs args;
+    cudaEvent_t ev0 = nullptr, ev1 = nullptr;  // around the current launch, on ks
+    bool timed = false;                        // ev0/ev1 hold a launch not yet drained
+    bool pending_launch = false;               // launch_on_drain: segments wait for cor_stream_drain
+};
+
+extern "C" void cor_stream_config_default(cor_stream_config* c) {
+    if (!c) return;
+    c->slots = 8;
+    c->max_jobs = 16384;
+    c->max_trajectories = 4194304;
+    c->max_params = 64;
+    c->want_records = 0;
+    c->reserve_sms = 0;
+    c->fixed_params = 256;
+    c->pool_params = 4096;
+    c->segments_per_launch = 65536;
+    c->idle_limit_s = 60.;
+    c->launch_on_drain = 0;
+    c->reserved = 0;
+}
+
+static void stream_free(cor_stream* s) {
+    if (!s) return;
+    cudaSetDevice(s->ctx->device);
+    if (s->slots) {
+        for (int k = 0; k < s->cfg.slots; k++) {
+            StreamSlot& sl = s->slots[k];
+            void* dev[] = {sl.jobs, sl.trig, sl.off, sl.sites, sl.status, sl.records, sl.job_done, sl.acc};
+            for (void* p : dev)
+                if (p) cudaFree(p);
+            void* host[] = {sl.h_jobs, sl.h_trig, sl.h_off, sl.h_sites, sl.h_status, sl.h_records, sl.h_seg, sl.h_end};
+            for (void* p : host)
+                if (p) cudaFreeHost(p);
+        }
+        delete[] s->slots;
+    }
+    void* dev[] = {s->segs_dev, s->seg_end_dev, s->pool_dev, s->queue_dev};
+    for (void* p : dev)
+        if (p) cudaFree(p);
+    void* host[] = {s->h_params, s->h_queue, s->mapped};
+    for (void* p : host)
+        if (p) cudaFreeHost(p);
+    free(s->last_params);
+    if (s->ev0) cudaEventDestroy(s->ev0);
+    if (s->ev1) cudaEventDestroy(s->ev1);
+    if (s->ks) cudaStreamDestroy(s->ks);
+    if (s->cs) cudaStreamDestroy(s->cs);
+    delete s;
+}
+
+extern "C" int cor_stream_create(cor_ctx* ctx, cor_model_set models, uint64_t step_limit, double tu_angle,
+                                 double particle_mass, const cor_stream_config* cfg_in, cor_stream** out) {
+    if (!ctx || !out) return COR_ERR_INVALID;
+    *out = nullptr;
+    int rc = check_req(ctx, models, 1, step_limit, tu_angle, particle_mass);
+    if (rc != COR_OK) return rc;
+    cor_stream_config cfg;
+    if (cfg_in) cfg = *cfg_in;
+    else cor_stream_config_default(&cfg);
+    if (cfg.slots < 1 || cfg.slots > 1024 || cfg.max_jobs < 1 || cfg.max_trajectories < 1 || cfg.max_params < 1 ||
+        cfg.fixed_params < 0 || cfg.pool_params < cfg.max_params || cfg.segments_per_launch < 1 ||
+        cfg.reserve_sms < 0 || cfg.reserve_sms >= ctx->sms || !(cfg.idle_limit_s > 0.) ||
+        cfg.idle_limit_s > 86400. || (cfg.want_records != 0 && cfg.want_records != 1) ||
+        (cfg.launch_on_drain != 0 && cfg.launch_on_drain != 1) || cfg.reserved != 0)
+        return fail(ctx, COR_ERR_INVALID, "stream configuration out of range");
+    const ModelOps* ops = find_ops(models);
+    if (!ops) return fail(ctx, COR_ERR_UNSUPPORTED, "model set not available");
+    CUDA_TRY(ctx, cudaSetDevice(ctx->device));
+    int per_sm = 0;
+    CUDA_TRY(ctx, ops->stream_occupancy(&per_sm));
+    if (per_sm < 1) return fail(ctx, COR_ERR_CUDA, "the stream kernel does not fit on an SM");
+    cor_stream* s = new cor_stream();
+    s->ctx = ctx;
+    s->ops = ops;
+    s->cfg = cfg;
+    s->blocks = (unsigned)((ctx->sms - cfg.reserve_sms) * per_sm);
+    rc = COR_OK;
+    do {
+#define SALLOC(call)                                                                                \
+    if ((call) != cudaSuccess) {                                                                    \
+        cudaGetLastError();                                                                         \
+        rc = fail(ctx, COR_ERR_NOMEM, "stream allocation: %s", #call);                              \
+        break;                                                                                      \
+    }
+        SALLOC(cudaStreamCreateWithFlags(&s->ks, cudaStreamNonBlocking));
+        SALLOC(cudaStreamCreateWithFlags(&s->cs, cudaStreamNonBlocking));
+        SALLOC(cudaEventCreate(&s->ev0));
+        SALLOC(cudaEventCreate(&s->ev1));
+        const size_t nj = (size_t)cfg.max_jobs, nt = (size_t)cfg.max_trajectories;
+        SALLOC(cudaMalloc(&s->segs_dev, sizeof(StreamSeg) * (size_t)cfg.slots));
+        SALLOC(cudaMalloc(&s->seg_end_dev, sizeof(unsigned long long) * (size_t)cfg.segments_per_launch));
+        SALLOC(cudaMalloc(&s->pool_dev, sizeof(DevParams) * (size_t)(cfg.fixed_params + cfg.pool_params)));
+        SALLOC(cudaMalloc(&s->queue_dev, 256));
+        s->h_params_cap = cfg.max_params > cfg.fixed_params ? cfg.max_params : cfg.fixed_params;
+        if (s->h_params_cap < 1) s->h_params_cap = 1;
+        SALLOC(cudaHostAlloc(&s->h_params, sizeof(DevParams) * (size_t)s->h_params_cap, cudaHostAllocDefault));
+        SALLOC(cudaHostAlloc(&s->h_queue, sizeof(unsigned long long), cudaHostAllocDefault));
+        const size_t mbytes = sizeof(StreamCtl) + sizeof(StreamDone) * (size_t)cfg.slots + 64;
+        SALLOC(cudaHostAlloc(&s->mapped, mbytes, cudaHostAllocMapped));
+        memset(s->mapped, 0, mbytes);
+        void* dmapped = nullptr;
+        SALLOC(cudaHostGetDevicePointer(&dmapped, s->mapped, 0));
+        s->ctl_h = (StreamCtl*)s->mapped;
+        s->ctl_d = (StreamCtl*)dmapped;
+        s->done_h = (StreamDone*)((char*)s->mapped + sizeof(StreamCtl));
+        s->done_d = (StreamDone*)((char*)dmapped + sizeof(StreamCtl));
+        s->err_h = (unsigned int*)((char*)s->done_h + sizeof(StreamDone) * (size_t)cfg.slots);
+        s->err_d = (unsigned int*)((char*)s->done_d + sizeof(StreamDone) * (size_t)cfg.slots);
+        s->ctl_h->stop_at = ~0ull;
+        s->last_params = (unsigned char*)malloc(sizeof(cor_model_params) * (size_t)cfg.max_params);
+        s->slots = new StreamSlot[cfg.slots];
+        if (!s->last_params) {
+            rc = fail(ctx, COR_ERR_NOMEM, "host allocation");
+            break;
+        }
+        for (int k = 0; k < cfg.slots && rc == COR_OK; k++) {
+            StreamSlot& sl = s->slots[k];
+            SALLOC(cudaMalloc(&sl.jobs, sizeof(cor_scan_job) * nj));
+            SALLOC(cudaMalloc(&sl.trig, sizeof(JobTrig) * nj));
+            SALLOC(cudaMalloc(&sl.off, sizeof(uint64_t) * (nj + 1)));
+            SALLOC(cudaMalloc(&sl.sites, sizeof(cor_site_result) * nj));
+            SALLOC(cudaMalloc(&sl.status, nt));
+            if (cfg.want_records) SALLOC(cudaMalloc(&sl.records, sizeof(cor_traj_record) * nt));
+            SALLOC(cudaMalloc(&sl.job_done, sizeof(unsigned int) * nj));
+            SALLOC(cudaMalloc(&sl.acc, 8 * sizeof(unsigned long long)));
+            SALLOC(cudaMemset(sl.job_done, 0, sizeof(unsigned int) * nj));
+            SALLOC(cudaMemset(sl.acc, 0, 8 * sizeof(unsigned long long)));
+            SALLOC(cudaHostAlloc(&sl.h_jobs, sizeof(cor_scan_job) * nj, cudaHostAllocDefault));
+            SALLOC(cudaHostAlloc(&sl.h_trig, sizeof(JobTrig) * nj, cudaHostAllocDefault));
+            SALLOC(cudaHostAlloc(&sl.h_off, sizeof(uint64_t) * (nj + 1), cudaHostAllocDefault));
+            SALLOC(cudaHostAlloc(&sl.h_sites, sizeof(cor_site_result) * nj, cudaHostAllocDefault));
+            SALLOC(cudaHostAlloc(&sl.h_status, nt, cudaHostAllocDefault));
+            if (cfg.want_records)
+                SALLOC(cudaHostAlloc(&sl.h_records, sizeof(cor_traj_record) * nt, cudaHostAllocDefault));
+            SALLOC(cudaHostAlloc(&sl.h_seg, sizeof(StreamSeg), cudaHostAllocDefault));
+            SALLOC(cudaHostAlloc(&sl.h_end, sizeof(unsigned long long), cudaHostAllocDefault));
+        }
+        if (rc != COR_OK) break;
+        SALLOC(cudaDeviceSynchronize());
+#undef SALLOC
+        StreamArgs& sa = s->args;
+        memset(&sa, 0, sizeof sa);
+        sa.a.params = s->pool_dev;
+        sa.a.step_limit = step_limit;
+        sa.a.tu_angle = tu_angle;
+        sa.a.gc_reject = 0.;
+        sa.a.turn_exact = find_turn_threshold(tu_angle, &sa.a.gc_reject) ? 1 : 0;
+        sa.a.mass = particle_mass;
+        if ((rc = crustal_tables(ctx, models, &sa.a.crust)) != COR_OK) break;
+        sa.ctl = s->ctl_d;
+        sa.done = s->done_d;
+        sa.error = s->err_d;
+        sa.segs = s->segs_dev;
+        sa.n_slots = (uint32_t)cfg.slots;
+        sa.seg_end = s->seg_end_dev;
+        sa.queue = s->queue_dev;
+        sa.idle_limit_ns = (unsigned long long)(cfg.idle_limit_s * 1e9);
+        sa.seg_cap = cfg.segments_per_launch;
+        sa.n_params = cfg.fixed_params + cfg.pool_params;
+    } while (0);
+    if (rc != COR_OK) {
+        stream_free(s);
+        return rc;
+    }
+    *out = s;
+    return COR_OK;
+}
+
+// The stream's failure recorded by its kernel in the mapped error word, if any.
+static int stream_error(cor_stream* s) {
+    const unsigned e = __atomic_load_n(s->err_h, __ATOMIC_ACQUIRE);
+    if (e & kStreamBadChain) return fail(s->ctx, COR_ERR_CUDA, "stream kernel found its segment table out of order");
+    if (e & kStreamBadParam)
+        return fail(s->ctx, COR_ERR_INVALID, "a job's param_index was outside the stream's parameter pool");
+    if (e & kStreamIdle)
+        return fail(s->ctx, COR_ERR_WATCHDOG, "stream kernel gave up waiting for work (idle limit)");
+    return COR_OK;
+}
+
+// Lets the running launch finish every published segment, then waits for it.
+static int stream_stop(cor_stream* s) {
+    if (!s->running) return COR_OK;
+    __atomic_store_n(&s->ctl_h->stop_at, s->published, __ATOMIC_RELEASE);
+    const cudaError_t e = cudaStreamSynchronize(s->ks);
+    s->running = false;
+    if (e != cudaSuccess) return fail(s->ctx, COR_ERR_CUDA, "stream kernel: %s", cudaGetErrorString(e));
+    return stream_error(s);
+}
+
+// Before publishing segment `seq` that brings n_params new parameter blocks:
+// restarts the kernel when this launch's segment table or parameter pool is
+// full, and fixes the new launch's first segment and queue index.
+static int stream_prepare_launch(cor_stream* s, int64_t seq, int32_t n_params_new) {
+    const bool full = (seq - s->first_seq) >= (int64_t)s->cfg.segments_per_launch ||
+                      s->pool_used + n_params_new > s->cfg.pool_params;
+    if (s->pending_launch) {
+        // launch_on_drain: the staged segments belong to the next launch
+        if (full) return fail(s->ctx, COR_ERR_BUSY, "the staged launch is full: drain it first");
+        return COR_OK;
+    }
+    if (s->running && full) {
+        const int rc = stream_stop(s);
+        if (rc != COR_OK) return rc;
+    }
+    if (!s->running) {
+        const int rc = stream_error(s);
+        if (rc != COR_OK) return rc;
+        s->first_seq = seq;
+        s->first_index = s->published;
+        s->pool_used = 0;
+        s->last_base = -1;
+    }
+    return COR_OK;
+}
+
+// Launches the stream kernel from the launch's first segment and queue index,
+// with the stop index given (~0: running until stopped), between two events.
+static int stream_launch(cor_stream* s, unsigned long long stop_at) {
+    cor_ctx* ctx = s->ctx;
+    *s->h_queue = s->first_index;
+    __atomic_store_n(s->err_h, 0u, __ATOMIC_RELAXED);
+    __atomic_store_n(&s->ctl_h->stop_at, stop_at, __ATOMIC_RELEASE);
+    CUDA_TRY(ctx, cudaMemcpyAsync(s->queue_dev, s->h_queue, sizeof(unsigned long long), cudaMemcpyHostToDevice, s->ks));
+    s->args.first_seq = (unsigned long long)s->first_seq;
+    s->args.first_index = s->first_index;
+    CUDA_TRY(ctx, cudaEventRecord(s->ev0, s->ks));
+    CUDA_TRY(ctx, s->ops->launch_stream(s->args, s->blocks, s->ks));
+    CUDA_TRY(ctx, cudaEventRecord(s->ev1, s->ks));
+    s->running = true;
+    s->timed = true;
+    return COR_OK;
+}
+
+// Copies the segment's descriptor and end (and, for cor_stream_submit, its
+// inputs, already queued on cs), waits for the copies, launches the kernel if
+// needed and moves the published end.
+static int stream_publish(cor_stream* s, StreamSlot& sl, int64_t seq, uint64_t n_traj) {
+    cor_ctx* ctx = s->ctx;
+    const unsigned slot = (unsigned)(seq % s->cfg.slots);
+    *sl.h_end = s->published + n_traj;
+    CUDA_TRY(ctx, cudaMemcpyAsync(s->segs_dev + slot, sl.h_seg, sizeof(StreamSeg), cudaMemcpyHostToDevice, s->cs));
+    CUDA_TRY(ctx, cudaMemcpyAsync(s->seg_end_dev + (seq - s->first_seq), sl.h_end, sizeof(unsigned long long),
+                                  cudaMemcpyHostToDevice, s->cs));
+    CUDA_TRY(ctx, cudaStreamSynchronize(s->cs));
+    if (!s->running && !s->cfg.launch_on_drain) {
+        const int rc = stream_launch(s, ~0ull);
+        if (rc != COR_OK) return rc;
+    }
+    s->published += n_traj;
+    __atomic_store_n(&s->ctl_h->published, s->published, __ATOMIC_RELEASE);
+    if (s->cfg.launch_on_drain) s->pending_launch = true;
+    sl.seq = seq;
+    sl.busy = true;
+    sl.n_traj = n_traj;
+    s->next_seq = seq + 1;
+    return COR_OK;
+}
+
+static bool offsets_uniform(const uint64_t* off, int32_t n_jobs) {
+    if (n_jobs < 1) return false;
+    for (int32_t j = 0; j < n_jobs; j++)
+        if (off[j + 1] - off[j] != off[1] - off[0]) return false;
+    return true;
+}
+
+extern "C" int cor_stream_submit(cor_stream* s, const cor_scan_job* jobs, int32_t n_jobs,
+                                 const cor_model_params* params, int32_t n_params, int64_t* ticket) {
+    if (!s || !ticket) return COR_ERR_INVALID;
+    cor_ctx* ctx = s->ctx;
+    NvtxRange nvtx_range("cor_stream_submit");
+    if (n_jobs < 0 || n_jobs > s->cfg.max_jobs || (n_jobs > 0 && (!jobs || !params)) || n_params < 0 ||
+        n_params > s->cfg.max_params || (n_jobs > 0 && n_params < 1))
+        return fail(ctx, COR_ERR_INVALID, "stream submit: %d scans, %d parameter blocks (limits %d, %d)", n_jobs,
+                    n_params, s->cfg.max_jobs, s->cfg.max_params);
+    for (int32_t j = 0; j < n_jobs; j++)
+        if (jobs[j].param_index < 0 || jobs[j].param_index >= n_params)
+            return fail(ctx, COR_ERR_INVALID, "job %d: param_index %d out of range", j, jobs[j].param_index);
+    const int64_t seq = s->next_seq;
+    StreamSlot& sl = s->slots[seq % s->cfg.slots];
+    if (sl.busy) return fail(ctx, COR_ERR_BUSY, "stream slot of segment %lld still holds uncollected segment %lld",
+                             (long long)seq, (long long)sl.seq);
+    uint64_t n_traj = 0;
+    if (cor_batch_count(jobs, n_jobs, &n_traj, sl.h_off) != COR_OK)
+        return fail(ctx, COR_ERR_INVALID, "invalid job: rigidity grid or window, nk1 <= 0, zero charge or non-finite start");
+    if (n_traj > (uint64_t)s->cfg.max_trajectories)
+        return fail(ctx, COR_ERR_RANGE, "%llu trajectories exceed the stream's %lld per segment",
+                    (unsigned long long)n_traj, (long long)s->cfg.max_trajectories);
+    CUDA_TRY(ctx, cudaSetDevice(ctx->device));
+    sl.own = true;
+    sl.n_jobs = n_jobs;
+    if (n_jobs == 0) {
+        // no trajectories: complete at once, but keep the segment chain the
+        // kernel walks whole (its end equals its base)
+        int rc = stream_prepare_launch(s, seq, 0);
+        if (rc != COR_OK) return rc;
+        *sl.h_end = s->published;
+        CUDA_TRY(ctx, cudaMemcpyAsync(s->seg_end_dev + (seq - s->first_seq), sl.h_end, sizeof(unsigned long long),
+                                      cudaMemcpyHostToDevice, s->cs));
+        CUDA_TRY(ctx, cudaStreamSynchronize(s->cs));
+        sl.empty = true;
+        sl.busy = true;
+        sl.seq = seq;
+        sl.n_traj = 0;
+        s->next_seq = seq + 1;
+        *ticket = seq;
+        return COR_OK;
+    }
+    sl.empty = false;
+    const size_t pbytes = sizeof(cor_model_params) * (size_t)n_params;
+    const bool reuse = s->running && s->last_base >= 0 && s->last_n == n_params &&
+                       memcmp(s->last_params, params, pbytes) == 0 &&
+                       (seq - s->first_seq) < (int64_t)s->cfg.segments_per_launch;
+    int rc = stream_prepare_launch(s, seq, reuse ? 0 : n_params);
+    if (rc != COR_OK) return rc;
+    int32_t base;
+    if (reuse && s->last_base >= 0) {
+        base = s->last_base;
+    } else {
+        base = s->cfg.fixed_params + s->pool_used;
+        prepare_params(params, n_params, s->h_params);
+        CUDA_TRY(ctx, cudaMemcpyAsync(s->pool_dev + base, s->h_params, sizeof(DevParams) * (size_t)n_params,
+                                      cudaMemcpyHostToDevice, s->cs));
+        s->pool_used += n_params;
+        memcpy(s->last_params, params, pbytes);
+        s->last_n = n_params;
+        s->last_base = base;
+    }
+    memcpy(sl.h_jobs, jobs, sizeof(cor_scan_job) * (size_t)n_jobs);
+    for (int32_t j = 0; j < n_jobs; j++) sl.h_jobs[j].param_index += base;
+    cor_prepare_trig(jobs, n_jobs, reinterpret_cast<cor_job_trig*>(sl.h_trig));
+    StreamSeg& g = *sl.h_seg;
+    g.jobs = sl.jobs;
+    g.trig = sl.trig;
+    g.offsets = sl.off;
+    g.status = sl.status;
+    g.records = sl.records;
+    g.sites = sl.sites;
+    g.job_done = sl.job_done;
+    g.acc = sl.acc;
+    g.base = s->published;
+    g.n_traj = n_traj;
+    g.seq = (unsigned long long)seq;
+    g.n_jobs = n_jobs;
+    g.n_rig = (offsets_uniform(sl.h_off, n_jobs) && s->ctx->rig_major) ? (uint32_t)(sl.h_off[1] - sl.h_off[0]) : 0u;
+    CUDA_TRY(ctx, cudaMemcpyAsync(sl.jobs, sl.h_jobs, sizeof(cor_scan_job) * (size_t)n_jobs, cudaMemcpyHostToDevice, s->cs));
+    CUDA_TRY(ctx, cudaMemcpyAsync(sl.trig, sl.h_trig, sizeof(JobTrig) * (size_t)n_jobs, cudaMemcpyHostToDevice, s->cs));
+    CUDA_TRY(ctx, cudaMemcpyAsync(sl.off, sl.h_off, sizeof(uint64_t) * ((size_t)n_jobs + 1), cudaMemcpyHostToDevice, s->cs));
+    if ((rc = stream_publish(s, sl, seq, n_traj)) != COR_OK) return rc;
+    *ticket = seq;
+    return COR_OK;
+}
+
+extern "C" int cor_stream_upload_params(cor_stream* s, const cor_model_params* params, int32_t n_params,
+                                        int32_t* first_index) {
+    if (!s || !first_index) return COR_ERR_INVALID;
+    cor_ctx* ctx = s->ctx;
+    if (!params || n_params < 1 || n_params > s->cfg.fixed_params - s->n_fixed)
+        return fail(ctx, COR_ERR_RANGE, "%d parameter blocks do not fit the stream's fixed pool (%d of %d used)",
+                    n_params, s->n_fixed, s->cfg.fixed_params);
+    CUDA_TRY(ctx, cudaSetDevice(ctx->device));
+    prepare_params(params, n_params, s->h_params);
+    CUDA_TRY(ctx, cudaMemcpyAsync(s->pool_dev + s->n_fixed, s->h_params, sizeof(DevParams) * (size_t)n_params,
+                                  cudaMemcpyHostToDevice, s->cs));
+    CUDA_TRY(ctx, cudaStreamSynchronize(s->cs));
+    *first_index = s->n_fixed;
+    s->n_fixed += n_params;
+    return COR_OK;
+}
+
+extern "C" int cor_stream_submit_device(cor_stream* s, const cor_scan_job* jobs_dev, const cor_job_trig* trig_dev,
+                                        const uint64_t* offsets_dev, const uint64_t* offsets_host, int32_t n_jobs,
+                                        cor_site_result* sites_dev, uint8_t* status_dev,
+                                        cor_traj_record* records_dev, int64_t* ticket) {
+    if (!s || !ticket) return COR_ERR_INVALID;
+    cor_ctx* ctx = s->ctx;
+    NvtxRange nvtx_range("cor_stream_submit_device");
+    if (n_jobs < 1 || n_jobs > s->cfg.max_jobs || !jobs_dev || !trig_dev || !offsets_dev || !offsets_host ||
+        !sites_dev || !status_dev)
+        return fail(ctx, COR_ERR_INVALID, "stream device submit: missing buffer or %d scans (limit %d)", n_jobs,
+                    s->cfg.max_jobs);
+    if (s->n_fixed < 1) return fail(ctx, COR_ERR_INVALID, "no parameter blocks: call cor_stream_upload_params first");
+    if (offsets_host[0] != 0) return fail(ctx, COR_ERR_INVALID, "offsets must start at 0");
+    for (int32_t j = 0; j < n_jobs; j++)
+        if (offsets_host[j + 1] <= offsets_host[j])
+            return fail(ctx, COR_ERR_INVALID, "offsets must increase (scan %d has no trajectory)", j);
+    const uint64_t n_traj = offsets_host[n_jobs];
+    const int64_t seq = s->next_seq;
+    StreamSlot& sl = s->slots[seq % s->cfg.slots];
+    if (sl.busy) return fail(ctx, COR_ERR_BUSY, "stream slot of segment %lld still holds uncollected segment %lld",
+                             (long long)seq, (long long)sl.seq);
+    CUDA_TRY(ctx, cudaSetDevice(ctx->device));
+    int rc = stream_prepare_launch(s, seq, 0);
+    if (rc != COR_OK) return rc;
+    sl.own = false;
+    sl.empty = false;
+    sl.n_jobs = n_jobs;
+    StreamSeg& g = *sl.h_seg;
+    g.jobs = jobs_dev;
+    g.trig = reinterpret_cast<const JobTrig*>(trig_dev);
+    g.offsets = offsets_dev;
+    g.status = status_dev;
+    g.records = records_dev;
+    g.sites = sites_dev;
+    g.job_done = sl.job_done;
+    g.acc = sl.acc;
+    g.base = s->published;
+    g.n_traj = n_traj;
+    g.seq = (unsigned long long)seq;
+    g.n_jobs = n_jobs;
+    g.n_rig = (offsets_uniform(offsets_host, n_jobs) && s->ctx->rig_major) ? (uint32_t)offsets_host[1] : 0u;
+    if ((rc = stream_publish(s, sl, seq, n_traj)) != COR_OK) return rc;
+    *ticket = seq;
+    return COR_OK;
+}
+
+extern "C" int cor_stream_wait(cor_stream* s, int64_t ticket, int32_t timeout_ms, cor_batch_result* out,
+                               uint64_t* t_done_ns) {
+    if (!s) return COR_ERR_INVALID;
+    cor_ctx* ctx = s->ctx;
+    if (ticket < 0 || ticket >= s->next_seq) return fail(ctx, COR_ERR_INVALID, "unknown ticket %lld", (long long)ticket);
+    const unsigned slot = (unsigned)(ticket % s->cfg.slots);
+    StreamSlot& sl = s->slots[slot];
+    if (!sl.busy || sl.seq != ticket)
+        return fail(ctx, COR_ERR_INVALID, "ticket %lld is not outstanding", (long long)ticket);
+    if (sl.own && !sl.empty && (!out || !out->sites))
+        return fail(ctx, COR_ERR_INVALID, "a submitted segment's results need out->sites");
+    if (sl.empty) {
+        if (out) memset(&out->counters, 0, sizeof(cor_counters));
+        if (t_done_ns) *t_done_ns = 0;
+        sl.busy = false;
+        return COR_OK;
+    }
+    const auto t0 = std::chrono::steady_clock::now();
+    for (;;) {
+        if (__atomic_load_n(&s->done_h[slot].seq1, __ATOMIC_ACQUIRE) == (unsigned long long)ticket + 1) break;
+        if (__atomic_load_n(s->err_h, __ATOMIC_ACQUIRE)) return stream_error(s);
+        if (s->pending_launch)
+            return fail(ctx, COR_ERR_INVALID, "segment %lld waits for cor_stream_drain (launch_on_drain)",
+                        (long long)ticket);
+        if (s->running) {
+            const cudaError_t e = cudaStreamQuery(s->ks);
+            if (e == cudaSuccess) {
+                s->running = false;
+                if (__atomic_load_n(&s->done_h[slot].seq1, __ATOMIC_ACQUIRE) == (unsigned long long)ticket + 1) break;
+                return fail(ctx, COR_ERR_CUDA, "stream kernel ended before segment %lld completed", (long long)ticket);
+            }
+            if (e != cudaErrorNotReady) return fail(ctx, COR_ERR_CUDA, "stream kernel: %s", cudaGetErrorString(e));
+        } else {
+            return fail(ctx, COR_ERR_CUDA, "stream kernel is not running and segment %lld did not complete",
+                        (long long)ticket);
+        }
+        const double ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+        if (timeout_ms >= 0 && ms >= (double)timeout_ms) return COR_PENDING;
+        timespec ts = {0, 20000};
+        nanosleep(&ts, nullptr);
+    }
+    if (__atomic_load_n(s->err_h, __ATOMIC_ACQUIRE) & kStreamBadParam) {
+        sl.busy = false;
+        return stream_error(s);
+    }
+    const StreamDone& d = s->done_h[slot];
+    if (t_done_ns) *t_done_ns = d.t_ns;
+    if (out) {
+        out->counters.accepted_steps = d.steps;
+        out->counters.trials = d.trials;
+        out->counters.trajectories = d.traj;
+        out->counters.watchdog = d.watchdog;
+        out->counters.kernel_launches = 1;
+        if (sl.own) {
+            CUDA_TRY(ctx, cudaSetDevice(ctx->device));
+            CUDA_TRY(ctx, cudaMemcpyAsync(sl.h_sites, sl.sites, sizeof(cor_site_result) * (size_t)sl.n_jobs,
+                                          cudaMemcpyDeviceToHost, s->cs));
+            if (out->status)
+                CUDA_TRY(ctx, cudaMemcpyAsync(sl.h_status, sl.status, sl.n_traj, cudaMemcpyDeviceToHost, s->cs));
+            if (out->records && sl.h_records)
+                CUDA_TRY(ctx, cudaMemcpyAsync(sl.h_records, sl.records, sizeof(cor_traj_record) * sl.n_traj,
+                                              cudaMemcpyDeviceToHost, s->cs));
+            CUDA_TRY(ctx, cudaStreamSynchronize(s->cs));
+            memcpy(out->sites, sl.h_sites, sizeof(cor_site_result) * (size_t)sl.n_jobs);
+            if (out->status) memcpy(out->status, sl.h_status, sl.n_traj);
+            if (out->records && sl.h_records) memcpy(out->records, sl.h_records, sizeof(cor_traj_record) * sl.n_traj);
+        }
+    }
+    sl.busy = false;
+    return COR_OK;
+}
+
+extern "C" int cor_stream_drain(cor_stream* s, double* launch_ms) {
+    if (!s) return COR_ERR_INVALID;
+    cor_ctx* ctx = s->ctx;
+    CUDA_TRY(ctx, cudaSetDevice(ctx->device));
+    if (launch_ms) *launch_ms = 0.;
+    if (s->pending_launch) {
+        s->pending_launch = false;
+        const int rc = stream_launch(s, s->published);
+        if (rc != COR_OK) return rc;
+    }
+    const int rc = stream_stop(s);
+    if (rc != COR_OK) return rc;
+    if (s->timed) {
+        float ms = 0.f;
+        CUDA_TRY(ctx, cudaEventElapsedTime(&ms, s->ev0, s->ev1));
+        s->timed = false;
+        if (launch_ms) *launch_ms = ms;
+    }
+    return COR_OK;
+}
+
+extern "C" int cor_stream_close(cor_stream* s) {
+    if (!s) return COR_OK;
+    cudaSetDevice(s->ctx->device);
+    int rc = COR_OK;
+    if (s->pending_launch) {
+        // staged segments of a launch_on_drain stream still run, so that the
+        // caller's device buffers are never left half written
+        s->pending_launch = false;
+        rc = stream_launch(s, s->published);
+    }
+    const int rc2 = stream_stop(s);
+    if (rc == COR_OK) rc = rc2;
+    stream_free(s);
+    return rc;
 }

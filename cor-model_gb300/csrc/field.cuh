@@ -25,11 +25,21 @@ struct ModelSet {
 
 // Device copy of one parameter block: the ABI block (ModelsParams) plus the
 // per-condition constants of the external models, derived on the host.
-struct DevParams {
+struct DevParamsBody {
     cor_model_params p;
     T96Cond t96;
     TS05Cond ts05;
 };
+// Padded to a multiple of 256 bytes, so that in an array of blocks no cache
+// line holds parts of two blocks (the scan stream appends blocks while its
+// kernel runs and reads them through the read-only path).
+struct DevParams {
+    cor_model_params p;
+    T96Cond t96;
+    TS05Cond ts05;
+    unsigned char pad[256 - sizeof(DevParamsBody) % 256];
+};
+static_assert(sizeof(DevParams) % 256 == 0, "parameter blocks are whole 256-byte units");
 
 // GSM position in metres -> GEO field in nT, for the lanes with `want` set
 // (the others get zeros and never read dp).  With the crustal model every

@@ -13,6 +13,13 @@
         trace_kernel<MS_##NAME><<<blocks, kTraceThreads, 0, s>>>(a);                                                 \
         return cudaGetLastError();                                                                         \
     }                                                                                                      \
+    static cudaError_t socc_##NAME(int* n) {                                                               \
+        return cudaOccupancyMaxActiveBlocksPerMultiprocessor(n, stream_kernel<MS_##NAME>, kTraceThreads, 0);         \
+    }                                                                                                      \
+    static cudaError_t stream_##NAME(const StreamArgs& a, unsigned blocks, cudaStream_t s) {               \
+        stream_kernel<MS_##NAME><<<blocks, kTraceThreads, 0, s>>>(a);                                               \
+        return cudaGetLastError();                                                                         \
+    }                                                                                                      \
     static cudaError_t field_##NAME(const DevParams* p, int np, const int32_t* idx, const double* pos,     \
                                     int64_t n, double* out, CrustalTables crust, cudaStream_t s) {         \
         const unsigned blocks = (unsigned)((n + 127) / 128);                                               \
@@ -24,5 +31,6 @@
         if (e == cudaSuccess) e = cudaMemcpyToSymbol(c_ts05, ts05, sizeof(TS05Tables));                    \
         return e;                                                                                          \
     }                                                                                                      \
-    const ModelOps ops_##NAME = {I * 100 + E * 10 + C, occ_##NAME, gen_##NAME, field_##NAME, tables_##NAME}; \
+    const ModelOps ops_##NAME = {I * 100 + E * 10 + C, occ_##NAME, gen_##NAME, field_##NAME, tables_##NAME, \
+                                 socc_##NAME, stream_##NAME};                                               \
     }

@@ -6,7 +6,7 @@
 
 #include <cuda_runtime.h>
 
-#include "trace.cuh"
+#include "stream.cuh"
 
 namespace cor {
 
@@ -18,6 +18,9 @@ struct ModelOps {
                                 int64_t n, double* out, CrustalTables crust, cudaStream_t s);
     // copies the host-derived constant blocks into this unit's constant memory
     cudaError_t (*upload_tables)(const T96Tables* t96, const TS05Tables* ts05);
+    // the persistent stream kernel (stream.cuh)
+    cudaError_t (*stream_occupancy)(int* blocks_per_sm);
+    cudaError_t (*launch_stream)(const StreamArgs& a, unsigned blocks, cudaStream_t s);
 };
 
 extern const ModelOps ops_igrf, ops_igrf_t96, ops_t96, ops_igrf_ts05, ops_ts05, ops_crustal;

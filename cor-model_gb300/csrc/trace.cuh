@@ -57,6 +57,11 @@ struct TraceArgs {
     double gc_reject;   // turn test: reject iff gc <= gc_reject (exact host-derived threshold)
     int turn_exact;     // 1: use gc_reject; 0: evaluate atan2 as the reference does
     int rig_major;      // 1: queue index runs over rigidity first (all jobs share n_rig)
+    // device word written by grid_check_kernel before the launch: non-zero iff
+    // offsets[j] == j * n_rig for every j (the rigidity-major mapping is then a
+    // bijection onto 0 .. n_traj-1); rig_major is ignored when it is zero.
+    // Null: rig_major is taken as given (the host checked the grid itself).
+    const unsigned int* grid_ok;
     uint32_t n_rig;
     double mass;
     uint8_t* status;
@@ -148,35 +153,22 @@ __device__ __forceinline__ uint64_t queue_pop(unsigned long long* q, bool want) 
     return want ? base + __popc(mask & ((1u << lane) - 1u)) : ~0ull;
 }
 
-// Start of one trajectory, src/trajectory.c:13-44 (the field is evaluated
-// by the caller in the converged section).
-__device__ __forceinline__ void lane_init(Lane& L, const TraceArgs& a, uint64_t t) {
-    // Queue position -> (scan j, rigidity index i).  In rigidity-major order
-    // the lowest rigidities of every scan, whose trajectories are the
-    // longest, are handed out first (longest-processing-time-first), which
-    // keeps the end of the run from being a tail of lone long trajectories.
-    int j;
-    uint64_t i;
-    if (a.rig_major) {
-        i = t / (uint64_t)a.n_jobs;
-        j = (int)(t - i * (uint64_t)a.n_jobs);
-    } else {
-        j = find_job(a.offsets, a.n_jobs, t);
-        i = t - a.offsets[j];
-    }
-    const cor_scan_job* job = a.jobs + j;
-    const JobTrig tg = a.trig[j];
+// Start of one trajectory, src/trajectory.c:13-44: scan `job` (index j of
+// its batch), grid position i of the traced range, batch-local trajectory
+// index `traj` (the field is evaluated by the caller in the converged section).
+__device__ __forceinline__ void lane_start(Lane& L, const cor_scan_job* job, const JobTrig& tg, const DevParams* par,
+                                           int j, uint64_t i, uint64_t traj, double mass) {
     L.job = job;
     L.job_index = j;
-    L.par = a.params + job->param_index;
-    L.traj = a.offsets[j] + i;
+    L.par = par;
+    L.traj = traj;
     const double rig = job->rig + (int)(i + (uint64_t)job->i_first) * job->del;  // :14, absolute grid index
     L.rig = rig;
     L.nk0 = job->nk1;
     L.time = 0.;
     L.alength = 0.;
     const double zn = job->zn;
-    const double aa = rig * 1.0e+09 * zn * kQ / (a.mass * kC * kC);
+    const double aa = rig * 1.0e+09 * zn * kQ / (mass * kC * kC);
     const double vr0 = kC * sqrt(1. - 1. / (1. + aa * aa));
     {
         const double r = job->r0 * kRe;  // sph_to_car, src/utils.c:28-41
@@ -195,6 +187,25 @@ __device__ __forceinline__ void lane_init(Lane& L, const TraceArgs& a, uint64_t 
     L.step = 0;
     L.trials = 0;
     L.gsm = geo_to_gsm(L.pos, &L.par->p);
+}
+
+// Queue position t -> (scan j, rigidity index i), then lane_start.  In
+// rigidity-major order (rig_major: every scan has n_traj / n_jobs
+// trajectories, checked on the device by grid_check_kernel) the lowest
+// rigidities of every scan, whose trajectories are the longest, are handed
+// out first (longest-processing-time-first), which keeps the end of the run
+// from being a tail of lone long trajectories.
+__device__ __forceinline__ void lane_init(Lane& L, const TraceArgs& a, uint64_t t, bool rig_major) {
+    int j;
+    uint64_t i;
+    if (rig_major) {
+        i = t / (uint64_t)a.n_jobs;
+        j = (int)(t - i * (uint64_t)a.n_jobs);
+    } else {
+        j = find_job(a.offsets, a.n_jobs, t);
+        i = t - a.offsets[j];
+    }
+    lane_start(L, a.jobs + j, a.trig[j], a.params + a.jobs[j].param_index, j, i, a.offsets[j] + i, a.mass);
 }
 
 // Advances one lane to its next accepted step (returns 0) or to its
@@ -270,9 +281,9 @@ __device__ __forceinline__ int lane_advance(Lane& L, const TraceArgs& a) {
     }
 }
 
-__device__ __forceinline__ void lane_finish(Lane& L, const TraceArgs& a, int st) {
-    if (a.status) a.status[L.traj] = (uint8_t)st;
-    if (a.records) {
+__device__ __forceinline__ void lane_record(const Lane& L, int st, uint8_t* status, cor_traj_record* records) {
+    if (status) status[L.traj] = (uint8_t)st;
+    if (records) {
         cor_traj_record r;
         r.pos[0] = L.pos.x; r.pos[1] = L.pos.y; r.pos[2] = L.pos.z;
         r.vel[0] = L.vel.x; r.vel[1] = L.vel.y; r.vel[2] = L.vel.z;
@@ -283,8 +294,15 @@ __device__ __forceinline__ void lane_finish(Lane& L, const TraceArgs& a, int st)
         r.trials = L.trials;
         r.status = st;
         r.reserved = 0;
-        a.records[L.traj] = r;
+        records[L.traj] = r;
     }
+}
+
+// A trajectory's class and final record into the batch's buffers; an index
+// at or beyond n_traj (possible only with offsets that disagree with
+// n_traj) writes nothing.
+__device__ __forceinline__ void lane_finish(Lane& L, const TraceArgs& a, int st) {
+    if (L.traj < a.n_traj) lane_record(L, st, a.status, a.records);
 }
 
 __device__ __forceinline__ void warp_add_u64(unsigned long long* dst, unsigned long long v) {
@@ -316,6 +334,7 @@ __global__ void __launch_bounds__(kTraceThreads, 1) trace_kernel(const TraceArgs
     bool has = false, done = threadIdx.x >= a.active_threads;
     unsigned long long n_steps = 0, n_trials = 0, n_traj = 0, n_wd = 0;
     const int lane = threadIdx.x & 31;
+    const bool rig_major = a.rig_major && (!a.grid_ok || *(volatile const unsigned int*)a.grid_ok != 0u);
     for (;;) {
         bool need_field = false;
         if (has) {
@@ -355,7 +374,7 @@ __global__ void __launch_bounds__(kTraceThreads, 1) trace_kernel(const TraceArgs
         const uint64_t t = queue_pop(a.queue, want);
         if (want) {
             if (t < a.n_traj) {
-                lane_init(L, a, t);
+                lane_init(L, a, t, rig_major);
                 has = true;
                 need_field = true;
             } else {

@@ -285,6 +285,60 @@ def trace_windows(ctx, jobs, params, models, i_lo, i_hi, widen: int = 3, **kw):
     return sites, redone, traced, steps
 
 
+def trace_windows_stream(stream, items, widen: int = 3):
+    """trace_windows for many batches at once through a scan stream
+    (cortrace.Stream): items are (jobs, params, i_lo, i_hi).  Every batch's
+    windows go in as one segment; the jobs of a segment whose window had a
+    boundary on an edge go back in as a new segment over widened windows (the
+    same rule as trace_windows), so first passes and retraces of different
+    batches are in flight together.  Returns, per item, (sites, mask of jobs
+    that needed more than one pass, trajectories traced, accepted steps)."""
+    from collections import deque
+    state = []
+    for jobs, params, i_lo, i_hi in items:
+        n_grid = np.round((jobs["rk"] - jobs["rig"]) / jobs["del"]).astype(np.int64) + 1
+        state.append({"jobs": jobs, "params": params, "n_grid": n_grid,
+                      "lo": np.asarray(i_lo, np.int64).copy(), "hi": np.asarray(i_hi, np.int64).copy(),
+                      "sites": np.zeros(len(jobs), ct.SITE_DTYPE), "redone": np.zeros(len(jobs), bool),
+                      "traced": 0, "steps": 0})
+    todo = deque((k, np.arange(len(it[0])), 0) for k, it in enumerate(items) if len(it[0]))
+    inflight = deque()
+    slots = int(stream.config.slots)
+    while todo or inflight:
+        while todo and len(inflight) < slots:
+            k, idx, attempt = todo.popleft()
+            S = state[k]
+            if attempt == widen + 1:                   # last resort: the whole grid
+                S["lo"][idx] = 0
+                S["hi"][idx] = S["n_grid"][idx] - 1
+            t = stream.submit(window_jobs(S["jobs"][idx], S["lo"][idx], S["hi"][idx]), S["params"])
+            inflight.append((t, k, idx, attempt))
+        t, k, idx, attempt = inflight.popleft()
+        res, _ = stream.wait(t, -1)
+        S = state[k]
+        S["traced"] += int(res.counters["trajectories"])
+        S["steps"] += int(res.counters["accepted_steps"])
+        again = []
+        for m, j in enumerate(idx):
+            st = res.status[res.offsets[m]:res.offsets[m + 1]]
+            allowed = st == ct.TRAJ_ALLOWED
+            low = S["lo"][j] > 0 and allowed[0]
+            high = S["hi"][j] < S["n_grid"][j] - 1 and not allowed[-1]
+            if not (low or high):
+                S["sites"][j] = res.sites[m]
+                continue
+            width = S["hi"][j] - S["lo"][j] + 1
+            if low:
+                S["lo"][j] = max(0, S["lo"][j] - width)
+            if high:
+                S["hi"][j] = min(S["n_grid"][j] - 1, S["hi"][j] + width)
+            again.append(j)
+        if again:
+            S["redone"][again] = True
+            todo.append((k, np.array(again, np.int64), attempt + 1))
+    return [(S["sites"], S["redone"], S["traced"], S["steps"]) for S in state]
+
+
 def trained_external(info: str) -> int | None:
     """The external field model (COR_EXTERNAL_*) a window network was trained
     with, from the provenance train_window.py stores ("igrf14+t96" ...); None

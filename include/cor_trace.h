@@ -42,6 +42,8 @@ extern "C" {
 #define COR_ERR_NODEV       -5  /* no CUDA device / library built without it */
 #define COR_ERR_UNSUPPORTED -6  /* combination of models not available       */
 #define COR_ERR_RANGE       -7  /* epoch outside the coefficient table       */
+#define COR_ERR_BUSY        -8  /* no free stream slot: collect a ticket first */
+#define COR_PENDING          1  /* cor_stream_wait: the segment is not done yet */
 
 /* ---- field models ----------------------------------------------------- */
 /* main() builds models[] in the order internal, external, crustal
@@ -142,7 +144,10 @@ typedef struct {
     uint64_t trials;          /* RK trials (accepted + rejected)           */
     uint64_t trajectories;
     uint64_t watchdog;        /* trajectories that ended COR_TRAJ_WATCHDOG */
-    uint64_t kernel_launches; /* kernels this call launched (generations + reduction) */
+    uint64_t kernel_launches; /* kernels the call launched: the scan's generations, the uniform-grid
+                                 check (when the rigidity-major order was asked for) and the reduction;
+                                 cor_trace_batch_device_noalloc also counts the kernel that writes
+                                 this block; a stream segment counts its stream launch (1) */
 } cor_counters;
 
 typedef struct {
@@ -205,7 +210,11 @@ int cor_trace_batch(cor_ctx *ctx, const cor_batch_req *req, cor_batch_result *ou
 /* cor_trace_batch_device flags */
 #define COR_FLAG_UNIFORM_GRID 1u  /* every job has the same number of rigidities:
                                      the work queue then hands out the lowest
-                                     rigidities of all jobs first */
+                                     rigidities of all jobs first.  The device
+                                     checks the offsets before the scan and
+                                     keeps the scan-by-scan order when they are
+                                     not uniform: a wrong flag costs the order,
+                                     never a result or a write out of bounds */
 
 /* Uploads n_params parameter blocks to the device, where they stay for the
  * following cor_trace_batch_device calls (cor_trace_batch uploads its own).
@@ -254,7 +263,9 @@ int cor_upload_crustal(cor_ctx *ctx, const double *g, const double *h, int32_t n
  * with every buffer already in device memory (jobs, trig from
  * cor_prepare_trig, offsets from cor_batch_count, sites, status, records),
  * using the parameter blocks of the last cor_upload_params.  The jobs are not
- * checked again here: they must be ones that cor_batch_count accepted.
+ * checked again here: they must be ones that cor_batch_count accepted, and
+ * offsets_dev[n_jobs] must equal n_trajectories (writes and reads stay below
+ * n_trajectories either way).
  * `stream` is a cudaStream_t (NULL = the legacy default stream).  The scan runs in
  * generations: between two of them the host reads how many trajectories the
  * kernel parked for regrouping, so the call synchronises `stream` a few
@@ -286,7 +297,11 @@ int cor_trace_batch_device(cor_ctx *ctx,
  * (sites, records, counters) are identical to cor_trace_batch_device's.
  * Preconditions: the parameter blocks are resident (cor_upload_params) and,
  * for a model set with the crustal model, so is its table (cor_upload_crustal)
- * -- otherwise COR_ERR_INVALID.
+ * -- otherwise COR_ERR_INVALID; offsets_dev[n_jobs] equals n_trajectories
+ * (the kernels never touch the array at or beyond n_trajectories in any case).
+ * counters_dev->kernel_launches counts every kernel of the call: the
+ * uniform-grid check (with COR_FLAG_UNIFORM_GRID), the scan, the reduction
+ * and the kernel that writes the count (4 for a uniform batch).
  * The first call on a device looks up the array's device address there
  * (cudaGetSymbolAddress, which may load this library's device code onto that
  * device); make that first call before any stream capture on the device.
@@ -301,6 +316,104 @@ int cor_trace_batch_device_noalloc(cor_ctx *ctx,
                                    double tu_angle, double particle_mass,
                                    cor_site_result *sites_dev, cor_traj_record *records_dev,
                                    cor_counters *counters_dev, uint32_t flags, void *stream);
+
+/* ---- persistent scan stream -------------------------------------------- */
+/* No counterpart in the reference, which runs one INFILE per process and
+ * waits for its whole scan (trajectory_simulation_cutoff, src/trajectory.c:6-161,
+ * called once from cutoff(), src/main.c:86).  A stream keeps ONE launch of the
+ * scan kernel resident on the device and feeds it batches of scans
+ * ("segments") as the caller submits them: every trajectory is traced and
+ * every scan reduced exactly as cor_trace_batch does (same flags, cutoffs and
+ * records, bit for bit), but a lane whose trajectory ends takes the next
+ * trajectory of any published segment, so the device never waits for one
+ * batch's last long trajectories before starting the next batch.
+ *
+ * Each segment's inputs are copied to the device (or already there, for
+ * cor_stream_submit_device), published through a control block in mapped
+ * pinned host memory, and reduced on the device by the warp that finishes a
+ * scan's last trajectory; the segment's completion is written back to mapped
+ * host memory, where cor_stream_wait reads it.  While a stream runs, its
+ * kernel occupies every SM but cfg.reserve_sms: other kernels on the device
+ * (the caller's, or libraries') run only on the reserved SMs, so a caller
+ * that launches device work between submits must reserve some.
+ * A stream is used from one host thread at a time. */
+typedef struct cor_stream cor_stream;
+
+typedef struct {
+    int32_t slots;             /* segments submitted and not yet collected, at most (ring size; default 8)  */
+    int32_t max_jobs;          /* scans per segment (default 16384)                                          */
+    int64_t max_trajectories;  /* trajectories per segment (default 4194304)                                 */
+    int32_t max_params;        /* parameter blocks per cor_stream_submit (default 64)                        */
+    int32_t want_records;      /* 1: cor_stream_submit segments keep per-trajectory final records (default 0) */
+    int32_t reserve_sms;       /* SMs the stream kernel leaves free for other kernels (default 0)            */
+    int32_t fixed_params;      /* capacity of cor_stream_upload_params (default 256)                         */
+    int32_t pool_params;       /* parameter blocks of cor_stream_submit per launch (default 4096)            */
+    int32_t segments_per_launch; /* segments per launch (default 65536)                                      */
+    double idle_limit_s;       /* a block of the kernel with nothing to trace for this long gives up and the
+                                  stream fails with COR_ERR_WATCHDOG (default 60 s); cor_stream_drain and
+                                  cor_stream_close are the normal ways to end a launch                      */
+    int32_t launch_on_drain;   /* 1: submits only stage and publish; cor_stream_drain launches the kernel
+                                  with everything published and the stop index already set, so the launch
+                                  never waits on the host (at most `slots` segments per launch; default 0) */
+    int32_t reserved;
+} cor_stream_config;
+
+void cor_stream_config_default(cor_stream_config *cfg);
+
+/* A stream on ctx's device for one model set and one step control
+ * (step_limit, tu_angle, particle_mass as in cor_batch_req).  Allocates every
+ * buffer it will use (device ring slots, pinned staging, mapped control
+ * block); no call on the stream allocates afterwards.  The kernel is launched
+ * by the first submit and relaunched when a launch's parameter pool or
+ * segment capacity is used up (after its published segments finish). */
+int cor_stream_create(cor_ctx *ctx, cor_model_set models, uint64_t step_limit, double tu_angle,
+                      double particle_mass, const cor_stream_config *cfg, cor_stream **out);
+
+/* Publishes a batch of scans from host buffers: jobs (checked as by
+ * cor_batch_count; param_index into params[0 .. n_params-1]) and their
+ * parameter blocks.  Returns at once with a ticket (the segment's sequence
+ * number); cor_stream_wait collects the results.  COR_ERR_BUSY when the ring
+ * slot the segment needs still holds an uncollected segment. */
+int cor_stream_submit(cor_stream *s, const cor_scan_job *jobs, int32_t n_jobs, const cor_model_params *params,
+                      int32_t n_params, int64_t *ticket);
+
+/* Parameter blocks for cor_stream_submit_device: appended to the stream's
+ * fixed pool, where they stay for the stream's lifetime; *first_index is the
+ * pool index of params[0] (device jobs use first_index + k as param_index). */
+int cor_stream_upload_params(cor_stream *s, const cor_model_params *params, int32_t n_params, int32_t *first_index);
+
+/* Publishes a batch whose buffers are already in device memory: jobs_dev
+ * (param_index into the fixed pool), trig_dev (cor_prepare_trig),
+ * offsets_dev (cor_batch_count), and the outputs sites_dev, status_dev
+ * (required) and records_dev (optional).  offsets_host is the host copy of
+ * the same offsets: the trajectory count and the queue order are taken from
+ * it (rigidity-major when every scan has the same count); offsets_dev must
+ * hold the same values.  The buffers must stay valid until the ticket is
+ * collected. */
+int cor_stream_submit_device(cor_stream *s, const cor_scan_job *jobs_dev, const cor_job_trig *trig_dev,
+                             const uint64_t *offsets_dev, const uint64_t *offsets_host, int32_t n_jobs,
+                             cor_site_result *sites_dev, uint8_t *status_dev, cor_traj_record *records_dev,
+                             int64_t *ticket);
+
+/* Waits up to timeout_ms (0: just look; negative: no limit) for a ticket.
+ * COR_PENDING if it is not done yet; COR_OK once done, with out->counters
+ * filled and, for a cor_stream_submit segment, out->sites (required),
+ * out->status and out->records (optional, NULL = not copied) filled from
+ * the device; the ticket is then collected and its slot free.  t_done_ns,
+ * if not NULL, gets the device's %globaltimer at the segment's completion.
+ * COR_ERR_WATCHDOG if the kernel gave up waiting for work (idle_limit_s),
+ * COR_ERR_CUDA if it failed. */
+int cor_stream_wait(cor_stream *s, int64_t ticket, int32_t timeout_ms, cor_batch_result *out, uint64_t *t_done_ns);
+
+/* Ends the current launch once every published segment has finished (their
+ * results stay collectable) and writes the launch's duration in ms, measured
+ * with CUDA events recorded on the kernel's stream around it, to *launch_ms
+ * (if not NULL; 0 when nothing ran).  The next submit starts a new launch. */
+int cor_stream_drain(cor_stream *s, double *launch_ms);
+
+/* Stops the kernel after every published segment has finished (uncollected
+ * results are dropped) and frees the stream. */
+int cor_stream_close(cor_stream *s);
 
 /* ---- trajectory dump (`cor -m trajectory`) ----------------------------- */
 /* One accepted step of a traced trajectory: what trajectory_simulation

@@ -383,21 +383,16 @@ static int o_trace_one(const cor_scan_job *job, const cor_model_params *p, cor_m
     return status;
 }
 
-int orc_scan_job(const cor_scan_job *job, const cor_model_params *params, cor_model_set models,
-                 uint64_t step_limit, double tu_angle, double particle_mass,
-                 cor_site_result *site, uint8_t *status, cor_traj_record *records,
-                 cor_counters *counters) {
-    if (!(job->del > 0.)) return COR_ERR_INVALID;
-    const int64_t n = o_n_traced(job);
-    if (n < 0) return COR_ERR_INVALID;
+/* The reduction of src/trajectory.c:156-160 over the classes of one scan's
+ * traced trajectories (status[0..n-1] = grid indices i_first..), in ascending
+ * rigidity, i.e. the reference's serial result (its OpenMP fmin/fmax). */
+static void o_reduce_job(const cor_scan_job *job, const uint8_t *status, int64_t n, cor_site_result *site) {
     int nza = job->i_first;  /* a window's untraced lower indices count as forbidden */
     double rmx1 = 0., rmx2 = 0., rmi = job->rk;                        /* :8-9 */
-    uint64_t steps = 0, trials = 0, wd = 0;
     for (int64_t k = 0; k < n; k++) {
         const int64_t i = job->i_first + k;
         const double rig = job->rig + i * job->del;                    /* :14 */
-        cor_traj_record r;
-        const int st = o_trace_one(job, params, models, step_limit, tu_angle, particle_mass, rig, &r, NULL, 0);
+        const int st = status[k];
         if (st == COR_TRAJ_ALLOWED) {
             rmi = fmin(rmi, rig);                                      /* :115 */
         } else if (st == COR_TRAJ_REENTRY || st == COR_TRAJ_SUPERLUM) {
@@ -406,24 +401,41 @@ int orc_scan_job(const cor_scan_job *job, const cor_model_params *params, cor_mo
         } else {
             nza += 1;
             rmx2 = fmax(rmx2, rig);                                    /* :143 */
-            if (st == COR_TRAJ_WATCHDOG) wd++;
         }
-        steps += r.steps;
-        trials += r.trials;
-        if (status) status[k] = (uint8_t)st;
-        if (records) records[k] = r;
     }
     double rmx = fmax(rmx1, rmx2);                                     /* :156-159 */
     const double zan = nza - (rmi - job->rig) / job->del;
     const double rms = rmi + zan * job->del;
     rmx = rmx + job->del;
-    if (site) {
-        site->r_lower = rmi;
-        site->r_upper = rmx;
-        site->r_cutoff = rms;
-        site->n_forbidden = nza;
-        site->n_traj = (int32_t)n;
+    site->r_lower = rmi;
+    site->r_upper = rmx;
+    site->r_cutoff = rms;
+    site->n_forbidden = nza;
+    site->n_traj = (int32_t)n;
+}
+
+int orc_scan_job(const cor_scan_job *job, const cor_model_params *params, cor_model_set models,
+                 uint64_t step_limit, double tu_angle, double particle_mass,
+                 cor_site_result *site, uint8_t *status, cor_traj_record *records,
+                 cor_counters *counters) {
+    if (!(job->del > 0.)) return COR_ERR_INVALID;
+    const int64_t n = o_n_traced(job);
+    if (n < 0) return COR_ERR_INVALID;
+    uint8_t *st_buf = status ? status : (uint8_t *)malloc(n > 0 ? (size_t)n : 1);
+    if (!st_buf) return COR_ERR_NOMEM;
+    uint64_t steps = 0, trials = 0, wd = 0;
+    for (int64_t k = 0; k < n; k++) {
+        const double rig = job->rig + (job->i_first + k) * job->del;  /* :14 */
+        cor_traj_record r;
+        const int st = o_trace_one(job, params, models, step_limit, tu_angle, particle_mass, rig, &r, NULL, 0);
+        wd += st == COR_TRAJ_WATCHDOG;
+        steps += r.steps;
+        trials += r.trials;
+        st_buf[k] = (uint8_t)st;
+        if (records) records[k] = r;
     }
+    if (site) o_reduce_job(job, st_buf, n, site);
+    if (st_buf != status) free(st_buf);
     if (counters) {
         counters->accepted_steps += steps;
         counters->trials += trials;
@@ -434,13 +446,20 @@ int orc_scan_job(const cor_scan_job *job, const cor_model_params *params, cor_mo
 }
 
 /* ---- batch over host threads ------------------------------------------ */
+/* Work items are chunks of ORC_CHUNK consecutive rigidities of one scan,
+ * handed out from a shared counter in scan order: every host thread stays
+ * busy until the batch's last chunk, as the reference's schedule(dynamic,1)
+ * over the rigidities of a scan keeps its team busy (src/trajectory.c:11).
+ * The per-scan reductions run after every chunk has finished. */
+#define ORC_CHUNK 4
+
 typedef struct {
     const cor_batch_req *req;
     const uint64_t *offsets;
-    cor_site_result *sites;
+    const uint64_t *chunk_off;   /* n_jobs + 1 prefix of chunks per scan */
     uint8_t *status;
     cor_traj_record *records;
-    int next;
+    uint64_t next;
     pthread_mutex_t lock;
     cor_counters total;
     int err;
@@ -448,21 +467,30 @@ typedef struct {
 
 static void *o_worker(void *arg) {
     o_pool *pl = (o_pool *)arg;
+    const int32_t nj = pl->req->n_jobs;
     cor_counters local = { 0, 0, 0, 0, 0 };
+    int j = 0;
     for (;;) {
-        pthread_mutex_lock(&pl->lock);
-        const int j = pl->next++;
-        pthread_mutex_unlock(&pl->lock);
-        if (j >= pl->req->n_jobs) break;
+        const uint64_t c = __atomic_fetch_add(&pl->next, 1, __ATOMIC_RELAXED);
+        if (c >= pl->chunk_off[nj]) break;
+        while (pl->chunk_off[j + 1] <= c) j++;   /* a thread's claims only ever move forward */
         const cor_scan_job *job = &pl->req->jobs[j];
-        if (job->param_index < 0 || job->param_index >= pl->req->n_params) { pl->err = COR_ERR_INVALID; continue; }
-        const uint64_t off = pl->offsets[j];
-        const int rc = orc_scan_job(job, &pl->req->params[job->param_index], pl->req->models,
-                                    pl->req->step_limit, pl->req->tu_angle, pl->req->particle_mass,
-                                    pl->sites ? &pl->sites[j] : NULL,
-                                    pl->status ? pl->status + off : NULL,
-                                    pl->records ? pl->records + off : NULL, &local);
-        if (rc != COR_OK) pl->err = rc;
+        const uint64_t n = pl->offsets[j + 1] - pl->offsets[j];
+        const uint64_t k0 = (c - pl->chunk_off[j]) * ORC_CHUNK;
+        const uint64_t k1 = k0 + ORC_CHUNK < n ? k0 + ORC_CHUNK : n;
+        const cor_model_params *par = &pl->req->params[job->param_index];
+        for (uint64_t k = k0; k < k1; k++) {
+            const double rig = job->rig + (int64_t)(job->i_first + (int64_t)k) * job->del;  /* :14 */
+            cor_traj_record r;
+            const int st = o_trace_one(job, par, pl->req->models, pl->req->step_limit, pl->req->tu_angle,
+                                       pl->req->particle_mass, rig, &r, NULL, 0);
+            pl->status[pl->offsets[j] + k] = (uint8_t)st;
+            if (pl->records) pl->records[pl->offsets[j] + k] = r;
+            local.accepted_steps += r.steps;
+            local.trials += r.trials;
+            local.trajectories += 1;
+            local.watchdog += st == COR_TRAJ_WATCHDOG;
+        }
     }
     pthread_mutex_lock(&pl->lock);
     pl->total.accepted_steps += local.accepted_steps;
@@ -478,9 +506,26 @@ int orc_scan_batch(const cor_batch_req *req, const uint64_t *offsets, int thread
                    cor_counters *counters) {
     if (threads < 1) threads = 1;
     if (threads > 1024) threads = 1024;
+    const int32_t nj = req->n_jobs;
+    for (int32_t j = 0; j < nj; j++) {
+        const cor_scan_job *job = &req->jobs[j];
+        if (job->param_index < 0 || job->param_index >= req->n_params || !(job->del > 0.) ||
+            o_n_traced(job) != (int64_t)(offsets[j + 1] - offsets[j]))
+            return COR_ERR_INVALID;
+    }
+    uint64_t *chunk_off = (uint64_t *)malloc(sizeof(uint64_t) * ((size_t)nj + 1));
+    uint8_t *st_buf = status ? status : (uint8_t *)malloc(offsets[nj] > 0 ? (size_t)offsets[nj] : 1);
+    if (!chunk_off || !st_buf) {
+        free(chunk_off);
+        if (st_buf != status) free(st_buf);
+        return COR_ERR_NOMEM;
+    }
+    chunk_off[0] = 0;
+    for (int32_t j = 0; j < nj; j++)
+        chunk_off[j + 1] = chunk_off[j] + (offsets[j + 1] - offsets[j] + ORC_CHUNK - 1) / ORC_CHUNK;
     o_pool pl;
     memset(&pl, 0, sizeof pl);
-    pl.req = req; pl.offsets = offsets; pl.sites = sites; pl.status = status; pl.records = records;
+    pl.req = req; pl.offsets = offsets; pl.chunk_off = chunk_off; pl.status = st_buf; pl.records = records;
     pthread_mutex_init(&pl.lock, NULL);
     pthread_t tid[1024];
     int started = 0;
@@ -489,6 +534,11 @@ int orc_scan_batch(const cor_batch_req *req, const uint64_t *offsets, int thread
     o_worker(&pl);
     for (int t = 0; t < started; t++) pthread_join(tid[t], NULL);
     pthread_mutex_destroy(&pl.lock);
+    if (sites)
+        for (int32_t j = 0; j < nj; j++)
+            o_reduce_job(&req->jobs[j], st_buf + offsets[j], (int64_t)(offsets[j + 1] - offsets[j]), &sites[j]);
+    free(chunk_off);
+    if (st_buf != status) free(st_buf);
     if (counters) *counters = pl.total;
     return pl.err;
 }

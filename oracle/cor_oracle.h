@@ -57,8 +57,10 @@ int orc_scan_job(const cor_scan_job *job, const cor_model_params *params, cor_mo
                  cor_site_result *site, uint8_t *status, cor_traj_record *records,
                  cor_counters *counters);
 
-/* A batch of scans over `threads` host threads (jobs are handed out one at a
- * time from a shared counter).  offsets as from cor_batch_count. */
+/* A batch of scans over `threads` host threads: chunks of 4 consecutive
+ * rigidities are handed out from a shared counter (the reference balances its
+ * OpenMP team per rigidity, src/trajectory.c:11), and each scan is reduced
+ * once all of its chunks are done.  offsets as from cor_batch_count. */
 int orc_scan_batch(const cor_batch_req *req, const uint64_t *offsets, int threads,
                    cor_site_result *sites, uint8_t *status, cor_traj_record *records,
                    cor_counters *counters);

@@ -74,7 +74,7 @@ def scan_batch_nudged(jobs, params, models, seed: int, threads=8, step_limit=250
     lib = load_nudge()
     jobs = np.ascontiguousarray(jobs, ct.JOB_DTYPE)
     params = np.ascontiguousarray(params, ct.PARAMS_DTYPE)
-    n, off = ct.batch_offsets(jobs)
+    n, off = batch_offsets(jobs)
     sites = np.zeros(len(jobs), ct.SITE_DTYPE)
     status = np.zeros(n, np.uint8)
     req = ct.BatchReq(_p(jobs), len(jobs), len(params), _p(params), models, step_limit, 0.01, ct.DEF_HM0_P)
@@ -136,13 +136,26 @@ def calculate_field(gsm_m: np.ndarray, params: np.ndarray, models=None, lib=None
     return out
 
 
+def batch_offsets(jobs: np.ndarray) -> tuple[int, np.ndarray]:
+    """Trajectories per scan, as src/trajectory.c:7,12 counts them
+    ((int)round((rk-rig)/del) + 1, C's round: half away from zero), or a
+    window's i_count; the exclusive prefix.  Computed here so that the oracle
+    needs nothing from the product library."""
+    x = (jobs["rk"] - jobs["rig"]) / jobs["del"]
+    n_grid = (np.sign(x) * np.floor(np.abs(x) + 0.5)).astype(np.int64) + 1
+    n = np.where(jobs["i_count"] > 0, jobs["i_count"], n_grid - jobs["i_first"]).astype(np.uint64)
+    off = np.zeros(len(jobs) + 1, np.uint64)
+    off[1:] = np.cumsum(n)
+    return int(off[-1]), off
+
+
 def scan_batch(jobs: np.ndarray, params: np.ndarray, models=None, step_limit=25000, tu_angle=0.01,
                particle_mass=ct.DEF_HM0_P, threads=1, want_records=False):
     """orc_scan_batch over `threads` host threads -> ScanResult like the product's."""
     lib = load()
     jobs = np.ascontiguousarray(jobs, ct.JOB_DTYPE)
     params = np.ascontiguousarray(params, ct.PARAMS_DTYPE)
-    n, off = ct.batch_offsets(jobs)
+    n, off = batch_offsets(jobs)
     sites = np.zeros(len(jobs), ct.SITE_DTYPE)
     status = np.zeros(n, np.uint8)
     records = np.zeros(n, ct.RECORD_DTYPE) if want_records else None

@@ -24,7 +24,7 @@ void trace_all(const TraceArgs& a) {
     const CrustalTables none{};
     for (uint64_t t = 0; t < a.n_traj; t++) {
         Lane L;
-        lane_init(L, a, t);
+        lane_init(L, a, t, false);
         for (;;) {
             L.field = calculate_field<ModelSet<I, E, 0>>(true, L.gsm, L.par, none);
             L.b = 1.E-09 * sqrt(L.field.x * L.field.x + L.field.y * L.field.y + L.field.z * L.field.z);

@@ -9,7 +9,7 @@ and driven two ways:
     giving the printed rows and the CUTOFF line of whole rigidity scans.
 
 Run here (where the reference tree exists):  python tests/golden/make_golden.py [section ...]
-Sections: setup field field_storm scan0 scan_t96 scan_ts05 scan_chaos scan_storm field_cli trajectory_cli cli_errors nudge nudge_extra nudge_storm.  The fixtures are small JSON
+Sections: setup field field_storm scan0 scan_t96 scan_ts05 scan_chaos scan_storm field_cli trajectory_cli cli_errors nudge nudge_extra nudge_storm scan_large nudge_large.  The fixtures are small JSON
 files; nothing on the GPU side reads the reference.
 """
 from __future__ import annotations
@@ -330,6 +330,97 @@ def make_scan_chaos(n_sites: int = 12) -> dict:
             "step_limit": 2000, "sites": recs}
 
 
+# ---- enlarged scan sets: enough site-directions to resolve a 99.5% bar ------
+# The nine arrival directions of the storm configuration: vertical, and 30 deg
+# zenith at azimuths 0..315 deg in 45 deg steps.
+NINE_DIRS = [(0.0, 0.0)] + [(30.0, float(a)) for a in range(0, 360, 45)]
+
+
+def _allowed_hex(idx, n: int) -> str:
+    bits = np.zeros(n, bool)
+    bits[idx] = True
+    return np.packbits(bits, bitorder="little").tobytes().hex()
+
+
+def _large_set(name, sites, rig, dele, conditions, args_for, workers):
+    """conditions: [(time7, parmod, ext_lines, [site indices])]; every site
+    record keeps its allowed flags as a little-endian bitmap in hex."""
+    n = int(round((20.0 - rig) / dele)) + 1
+    out = []
+    for time7, pm, ext, which in conditions:
+        recs = run_scan_set([sites[k] for k in which], rig, 20.0, dele, time7, args_for, ext_lines=ext,
+                            workers=workers)
+        for r in recs:
+            r["allowed_hex"] = _allowed_hex(r.pop("allowed"), n)
+        out.append({"time": time7, "parmod": pm, "sites": recs})
+        print(name, "condition done:", len(recs), "site-directions", flush=True)
+    return out
+
+
+def make_scan_large(workers: int = 6) -> dict:
+    """Scans large enough that one site-direction is at most 0.5% of a set:
+    * t96: 1,000 vertical sites of the 5-degree grid, IGRF-14 + T96 at the bench
+      condition, 20 -> 0.05 GV by 0.05;
+    * ts05: 800 site-directions of the 5-degree grid, each with one of the nine
+      storm-configuration directions, IGRF-14 + TS05 (W1..W6 = 1), same grid;
+    * storm: 4 seeded storm conditions x 60 site-directions (TS05, nine
+      directions), same grid;
+    * config1: 64 sites spread over the 5-degree grid at the bench condition on
+      the bench's own 0.01 GV grid (2,000 rigidities)."""
+    import window
+    grid = [(float(a), float(o)) for a in range(-90, 91, 5) for o in range(0, 360, 5)]
+    t7 = [2020, 6, 21, 173, 12, 0, 0]
+    out = {}
+    rng = np.random.default_rng(31)
+    pick = rng.choice(len(grid), 1000, replace=False)
+    sites = [(grid[k][0], grid[k][1], grid[k][0], grid[k][1]) for k in pick]
+    out["t96"] = {"config": "IGRF-14 + T96 at 2020-06-21 12 UT, vertical, 20 km, 20 -> 0.05 GV by 0.05",
+                  "rig": 0.05, "rk": 20.0, "del": 0.05, "model": "igrf14", "external": "t96",
+                  "conditions": _large_set("t96", sites, 0.05, 0.05,
+                                           [(t7, [2.0, -20.0, 0.0, -1.0], ["-20 2 0 -1"], range(len(sites)))],
+                                           ["-i", "igrf14", "-e", "t96"], workers)}
+    rng = np.random.default_rng(37)
+    pick = rng.choice(len(grid), 800, replace=False)
+    sites = []
+    for k, g in enumerate(pick):
+        lat, lon = grid[g]
+        the1, fi1 = window.arrival_direction(lat, lon, *NINE_DIRS[k % 9])
+        sites.append((lat, lon, float(the1), float(fi1)))
+    out["ts05"] = {"config": "IGRF-14 + TS05 (W1..W6 = 1) at 2020-06-21 12 UT, 20 km, nine directions, "
+                             "20 -> 0.05 GV by 0.05",
+                   "rig": 0.05, "rk": 20.0, "del": 0.05, "model": "igrf14", "external": "ts05",
+                   "conditions": _large_set("ts05", sites, 0.05, 0.05,
+                                            [(t7, TS05_PARMOD, ["-20 2 0 -1", "1 1 1 1 1 1"], range(len(sites)))],
+                                            ["-i", "igrf14", "-e", "ts05"], workers)}
+    rng = np.random.default_rng(41)
+    conds = []
+    sites = []
+    for ci, c in enumerate(window.sample_conditions(rng, 4, "ts05")):
+        pm = [float(v) for v in c["parmod"]]
+        ext = [f"{pm[1]!r} {pm[0]!r} {pm[2]!r} {pm[3]!r}", " ".join(repr(w) for w in pm[4:10])]  # src/io.c:98-113
+        first = len(sites)
+        for k in range(60):
+            lat = float(np.degrees(np.arcsin(rng.uniform(-1, 1))))
+            lon = float(rng.uniform(0, 360))
+            the1, fi1 = window.arrival_direction(lat, lon, *NINE_DIRS[k % 9])
+            sites.append((lat, lon, float(the1), float(fi1)))
+        conds.append((c["time7"], pm, ext, range(first, len(sites))))
+    out["storm"] = {"config": "IGRF-14 + TS05 at 4 seeded storm conditions, 20 km, nine directions, "
+                              "20 -> 0.05 GV by 0.05",
+                    "rig": 0.05, "rk": 20.0, "del": 0.05, "model": "igrf14", "external": "ts05",
+                    "conditions": _large_set("storm", sites, 0.05, 0.05, conds, ["-i", "igrf14", "-e", "ts05"],
+                                             workers)}
+    pick = [int(round(i * len(grid) / 64)) for i in range(64)]
+    sites = [(grid[k][0], grid[k][1], grid[k][0], grid[k][1]) for k in pick]
+    out["config1"] = {"config": "IGRF-14 + T96 at 2020-06-21 12 UT, vertical, 20 km, 20 -> 0.01 GV by 0.01 "
+                                "(the bench's grid and condition)",
+                      "rig": 0.01, "rk": 20.0, "del": 0.01, "model": "igrf14", "external": "t96",
+                      "conditions": _large_set("config1", sites, 0.01, 0.01,
+                                               [(t7, [2.0, -20.0, 0.0, -1.0], ["-20 2 0 -1"], range(len(sites)))],
+                                               ["-i", "igrf14", "-e", "t96"], workers)}
+    return out
+
+
 def make_field_cli() -> dict:
     """`cor -m field` of the reference on three grids (src/field.c:6-53): its
     text output, header included, for the drop-in CLI to reproduce."""
@@ -584,6 +675,49 @@ def make_nudge_extra() -> dict:
     return out
 
 
+def large_set_sites(g: dict) -> list[dict]:
+    """The site records of one scan_large.json set, with their condition."""
+    return [dict(s, time=c["time"], parmod=c["parmod"]) for c in g["conditions"] for s in c["sites"]]
+
+
+def allowed_from_hex(h: str, n: int) -> np.ndarray:
+    return np.unpackbits(np.frombuffer(bytes.fromhex(h), np.uint8), bitorder="little")[:n].astype(bool)
+
+
+def make_nudge_large() -> dict:
+    """The reference's one-ulp self-agreement on every scan_large.json set
+    (three seeds): flags that differ and site-directions off by more than one
+    rigidity step, the same two figures the GPU tests report."""
+    with open(os.path.join(HERE, "nudge_sensitivity.json")) as f:
+        out = json.load(f)
+    with open(os.path.join(HERE, "scan_large.json")) as f:
+        large = json.load(f)
+    out["scans_large"] = {}
+    for name, g in large.items():
+        ext = ct.EXTERNAL_T96 if g["external"] == "t96" else ct.EXTERNAL_TS05
+        n = int(round((g["rk"] - g["rig"]) / g["del"])) + 1
+        stats = []
+        for seed in (1, 2, 3):
+            n_diff = n_traj = ok = n_sites = 0
+            for c in g["conditions"]:
+                p = ct.internal_setup(g["model"], c["time"], parmod=c["parmod"])
+                jobs = np.concatenate([ct.make_job(s["lat"], s["lon"], rig=g["rig"], rk=g["rk"], dele=g["del"],
+                                                   the1=s["the1"], fi1=s["fi1"]) for s in c["sites"]])
+                res = pyoracle.scan_batch_nudged(jobs, p, ct.model_set(ct.INTERNAL_SH, ext), seed, threads=6)
+                for j, s in enumerate(c["sites"]):
+                    st = res.status[res.offsets[j]:res.offsets[j + 1]]
+                    n_diff += int(np.sum((st == ct.TRAJ_ALLOWED) != allowed_from_hex(s["allowed_hex"], n)))
+                    n_traj += n
+                    mine3 = [res.sites[j]["r_lower"], res.sites[j]["r_upper"], res.sites[j]["r_cutoff"]]
+                    ok += all(abs(a - float(b)) <= g["del"] * 1.0000001 for a, b in zip(mine3, s["cutoff"]))
+                    n_sites += 1
+            stats.append({"flags_differing": n_diff, "trajectories": n_traj, "sites_off": n_sites - ok,
+                          "sites": n_sites})
+            print(name, seed, stats[-1], flush=True)
+        out["scans_large"][name] = {"seeds": [1, 2, 3], "runs": stats}
+    return out
+
+
 def main(sections):
     lib = ref_lib()
     todo = {
@@ -601,6 +735,8 @@ def main(sections):
         "nudge": ("nudge_sensitivity.json", make_nudge),
         "nudge_extra": ("nudge_sensitivity.json", make_nudge_extra),
         "nudge_storm": ("nudge_sensitivity.json", make_nudge_storm),
+        "scan_large": ("scan_large.json", make_scan_large),
+        "nudge_large": ("nudge_sensitivity.json", make_nudge_large),
     }
     for s in sections or list(todo):
         fn, mk = todo[s]
