@@ -12,6 +12,9 @@
 #include <string.h>
 #include <time.h>
 
+#include <algorithm>
+#include <vector>
+
 #include "model_ops.h"
 #include "reduce_kernels.cuh"
 #include "model_prep.h"
@@ -880,6 +883,7 @@ struct StreamSlot {
     cor_site_result* sites = nullptr;
     uint8_t* status = nullptr;
     cor_traj_record* records = nullptr;
+    uint32_t* order = nullptr;
     unsigned int* job_done = nullptr;
     unsigned long long* acc = nullptr;
     // pinned staging
@@ -889,6 +893,7 @@ struct StreamSlot {
     cor_site_result* h_sites = nullptr;
     uint8_t* h_status = nullptr;
     cor_traj_record* h_records = nullptr;
+    uint32_t* h_order = nullptr;
     StreamSeg* h_seg = nullptr;
     unsigned long long* h_end = nullptr;
     // state
@@ -940,7 +945,7 @@ extern "C" void cor_stream_config_default(cor_stream_config* c) {
     if (!c) return;
     c->slots = 8;
     c->max_jobs = 16384;
-    c->max_trajectories = 4194304;
+    c->max_trajectories = 2097152;
     c->max_params = 64;
     c->want_records = 0;
     c->reserve_sms = 0;
@@ -958,10 +963,11 @@ static void stream_free(cor_stream* s) {
     if (s->slots) {
         for (int k = 0; k < s->cfg.slots; k++) {
             StreamSlot& sl = s->slots[k];
-            void* dev[] = {sl.jobs, sl.trig, sl.off, sl.sites, sl.status, sl.records, sl.job_done, sl.acc};
+            void* dev[] = {sl.jobs, sl.trig, sl.off, sl.sites, sl.status, sl.records, sl.order, sl.job_done, sl.acc};
             for (void* p : dev)
                 if (p) cudaFree(p);
-            void* host[] = {sl.h_jobs, sl.h_trig, sl.h_off, sl.h_sites, sl.h_status, sl.h_records, sl.h_seg, sl.h_end};
+            void* host[] = {sl.h_jobs,    sl.h_trig,  sl.h_off, sl.h_sites, sl.h_status,
+                            sl.h_records, sl.h_order, sl.h_seg, sl.h_end};
             for (void* p : host)
                 if (p) cudaFreeHost(p);
         }
@@ -990,7 +996,8 @@ extern "C" int cor_stream_create(cor_ctx* ctx, cor_model_set models, uint64_t st
     cor_stream_config cfg;
     if (cfg_in) cfg = *cfg_in;
     else cor_stream_config_default(&cfg);
-    if (cfg.slots < 1 || cfg.slots > 1024 || cfg.max_jobs < 1 || cfg.max_trajectories < 1 || cfg.max_params < 1 ||
+    if (cfg.slots < 1 || cfg.slots > 1024 || cfg.max_jobs < 1 || cfg.max_trajectories < 1 ||
+        cfg.max_trajectories > 0xffffffffll || cfg.max_params < 1 ||
         cfg.fixed_params < 0 || cfg.pool_params < cfg.max_params || cfg.segments_per_launch < 1 ||
         cfg.reserve_sms < 0 || cfg.reserve_sms >= ctx->sms || !(cfg.idle_limit_s > 0.) ||
         cfg.idle_limit_s > 86400. || (cfg.want_records != 0 && cfg.want_records != 1) ||
@@ -1054,6 +1061,7 @@ extern "C" int cor_stream_create(cor_ctx* ctx, cor_model_set models, uint64_t st
             SALLOC(cudaMalloc(&sl.sites, sizeof(cor_site_result) * nj));
             SALLOC(cudaMalloc(&sl.status, nt));
             if (cfg.want_records) SALLOC(cudaMalloc(&sl.records, sizeof(cor_traj_record) * nt));
+            SALLOC(cudaMalloc(&sl.order, sizeof(uint32_t) * nt));
             SALLOC(cudaMalloc(&sl.job_done, sizeof(unsigned int) * nj));
             SALLOC(cudaMalloc(&sl.acc, 8 * sizeof(unsigned long long)));
             SALLOC(cudaMemset(sl.job_done, 0, sizeof(unsigned int) * nj));
@@ -1065,6 +1073,7 @@ extern "C" int cor_stream_create(cor_ctx* ctx, cor_model_set models, uint64_t st
             SALLOC(cudaHostAlloc(&sl.h_status, nt, cudaHostAllocDefault));
             if (cfg.want_records)
                 SALLOC(cudaHostAlloc(&sl.h_records, sizeof(cor_traj_record) * nt, cudaHostAllocDefault));
+            SALLOC(cudaHostAlloc(&sl.h_order, sizeof(uint32_t) * nt, cudaHostAllocDefault));
             SALLOC(cudaHostAlloc(&sl.h_seg, sizeof(StreamSeg), cudaHostAllocDefault));
             SALLOC(cudaHostAlloc(&sl.h_end, sizeof(unsigned long long), cudaHostAllocDefault));
         }
@@ -1189,6 +1198,18 @@ static int stream_publish(cor_stream* s, StreamSlot& sl, int64_t seq, uint64_t n
     return COR_OK;
 }
 
+// The batch's trajectories (offsets space) sorted by rigidity, lowest first;
+// ties keep the batch order.
+static void rigidity_order(const cor_scan_job* jobs, int32_t n_jobs, const uint64_t* off, uint32_t* order) {
+    const uint64_t n = off[n_jobs];
+    std::vector<double> rig(n);
+    for (int32_t j = 0; j < n_jobs; j++)
+        for (uint64_t k = 0; k < off[j + 1] - off[j]; k++)
+            rig[off[j] + k] = jobs[j].rig + (int)(k + (uint64_t)jobs[j].i_first) * jobs[j].del;
+    for (uint64_t t = 0; t < n; t++) order[t] = (uint32_t)t;
+    std::stable_sort(order, order + n, [&](uint32_t a, uint32_t b) { return rig[a] < rig[b]; });
+}
+
 static bool offsets_uniform(const uint64_t* off, int32_t n_jobs) {
     if (n_jobs < 1) return false;
     for (int32_t j = 0; j < n_jobs; j++)
@@ -1275,6 +1296,15 @@ extern "C" int cor_stream_submit(cor_stream* s, const cor_scan_job* jobs, int32_
     g.seq = (unsigned long long)seq;
     g.n_jobs = n_jobs;
     g.n_rig = (offsets_uniform(sl.h_off, n_jobs) && s->ctx->rig_major) ? (uint32_t)(sl.h_off[1] - sl.h_off[0]) : 0u;
+    g.order = nullptr;
+    if (!g.n_rig && s->ctx->rig_major && n_jobs > 1) {
+        // scans of different lengths: hand out all their trajectories in
+        // ascending rigidity, as the rigidity-major order does for a uniform
+        // grid (the lowest rigidities are the longest trajectories)
+        rigidity_order(jobs, n_jobs, sl.h_off, sl.h_order);
+        CUDA_TRY(ctx, cudaMemcpyAsync(sl.order, sl.h_order, sizeof(uint32_t) * n_traj, cudaMemcpyHostToDevice, s->cs));
+        g.order = sl.order;
+    }
     CUDA_TRY(ctx, cudaMemcpyAsync(sl.jobs, sl.h_jobs, sizeof(cor_scan_job) * (size_t)n_jobs, cudaMemcpyHostToDevice, s->cs));
     CUDA_TRY(ctx, cudaMemcpyAsync(sl.trig, sl.h_trig, sizeof(JobTrig) * (size_t)n_jobs, cudaMemcpyHostToDevice, s->cs));
     CUDA_TRY(ctx, cudaMemcpyAsync(sl.off, sl.h_off, sizeof(uint64_t) * ((size_t)n_jobs + 1), cudaMemcpyHostToDevice, s->cs));
@@ -1341,6 +1371,7 @@ extern "C" int cor_stream_submit_device(cor_stream* s, const cor_scan_job* jobs_
     g.seq = (unsigned long long)seq;
     g.n_jobs = n_jobs;
     g.n_rig = (offsets_uniform(offsets_host, n_jobs) && s->ctx->rig_major) ? (uint32_t)offsets_host[1] : 0u;
+    g.order = nullptr;
     if ((rc = stream_publish(s, sl, seq, n_traj)) != COR_OK) return rc;
     *ticket = seq;
     return COR_OK;

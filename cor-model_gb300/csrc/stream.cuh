@@ -46,6 +46,7 @@ struct StreamSeg {
     unsigned long long seq;
     int32_t n_jobs;
     uint32_t n_rig;                // > 0: rigidity-major order (the host checked that every scan has n_rig)
+    const uint32_t* order;         // queue position -> trajectory (offsets space), or null; overrides n_rig
 };
 
 // Host-written control block (mapped pinned memory).
@@ -288,10 +289,15 @@ __global__ void __launch_bounds__(kTraceThreads, 1) stream_kernel(const StreamAr
                 const int n_jobs = __ldcg(&sg->n_jobs);
                 const unsigned n_rig = __ldcg(&sg->n_rig);
                 const uint64_t* off = ldcg_ptr(&sg->offsets);
-                const uint64_t tl = pend - lo;
+                const uint32_t* order = ldcg_ptr(&sg->order);
+                uint64_t tl = pend - lo;
                 int j;
                 uint64_t i;
-                if (n_rig) {
+                if (order) {
+                    tl = __ldcg(order + tl);
+                    j = find_job_cg(off, n_jobs, tl);
+                    i = tl - __ldcg(reinterpret_cast<const unsigned long long*>(off) + j);
+                } else if (n_rig) {
                     i = tl / (uint64_t)n_jobs;
                     j = (int)(tl - i * (uint64_t)n_jobs);
                 } else {

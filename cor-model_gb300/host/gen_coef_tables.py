@@ -9,7 +9,7 @@ CHAOS table packed as the lower triangle (m <= n) that chaos_geo reads.
 Each value is written as the shortest decimal that round-trips, so the
 compiled doubles equal the reference's.
 
-Usage: python gen_coef_tables.py [reference_root]
+Usage: python gen_coef_tables.py REFERENCE_ROOT   (or COR_REFERENCE_ROOT set)
 """
 from __future__ import annotations
 
@@ -153,7 +153,9 @@ def generate(root: str) -> str:
 
 
 if __name__ == "__main__":
-    root = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
+    root = sys.argv[1] if len(sys.argv) > 1 else os.environ.get("COR_REFERENCE_ROOT")
+    if not root:
+        sys.exit("usage: gen_coef_tables.py REFERENCE_ROOT (or set COR_REFERENCE_ROOT)")
     out = os.path.join(HERE, "coef_tables.c")
     with open(out, "w") as f:
         f.write(generate(root))

@@ -342,7 +342,7 @@ typedef struct cor_stream cor_stream;
 typedef struct {
     int32_t slots;             /* segments submitted and not yet collected, at most (ring size; default 8)  */
     int32_t max_jobs;          /* scans per segment (default 16384)                                          */
-    int64_t max_trajectories;  /* trajectories per segment (default 4194304)                                 */
+    int64_t max_trajectories;  /* trajectories per segment (default 2097152, at most 2^32-1)                 */
     int32_t max_params;        /* parameter blocks per cor_stream_submit (default 64)                        */
     int32_t want_records;      /* 1: cor_stream_submit segments keep per-trajectory final records (default 0) */
     int32_t reserve_sms;       /* SMs the stream kernel leaves free for other kernels (default 0)            */
@@ -373,7 +373,11 @@ int cor_stream_create(cor_ctx *ctx, cor_model_set models, uint64_t step_limit, d
  * cor_batch_count; param_index into params[0 .. n_params-1]) and their
  * parameter blocks.  Returns at once with a ticket (the segment's sequence
  * number); cor_stream_wait collects the results.  COR_ERR_BUSY when the ring
- * slot the segment needs still holds an uncollected segment. */
+ * slot the segment needs still holds an uncollected segment.  With the
+ * context's rigidity-major queue order (the default), a batch of equal scans
+ * is handed out lowest rigidity first across its scans, and a batch of
+ * unequal scans (windows) in ascending rigidity over all its trajectories:
+ * the longest trajectories start first. */
 int cor_stream_submit(cor_stream *s, const cor_scan_job *jobs, int32_t n_jobs, const cor_model_params *params,
                       int32_t n_params, int64_t *ticket);
 

@@ -4,7 +4,8 @@
   ``oracle/liboracle.so`` (always; it is the checker on any machine).
 * ``build_ref()`` compiles the reference itself, from its sources where they lie
   under ``/root/reference`` (never copied), into ``oracle/_ref/``:
-  ``libcorref.so`` (everything but the CLI) and the ``cor`` binary.  It is used
+  ``libcorref.so`` (everything but the CLI) and the ``cor`` binary.  The
+  environment variable COR_REFERENCE_ROOT names another location of the tree.  It is used
   only to pin the restatement and to make the golden fixtures in
   ``tests/golden/``.  It is skipped when the reference tree is absent.
 
@@ -20,7 +21,8 @@ import sys
 from concurrent.futures import ThreadPoolExecutor
 
 HERE = os.path.dirname(os.path.abspath(__file__))
-REF_ROOT = "/root/reference"
+# where the reference tree lies (read only); COR_REFERENCE_ROOT overrides it
+REF_ROOT = os.environ.get("COR_REFERENCE_ROOT", "/root/reference")
 REF_OUT = os.path.join(HERE, "_ref")
 
 FP_FLAGS = ["-O3", "-fno-math-errno", "-fno-trapping-math", "-ffp-contract=off", "-finline-limit=300"]

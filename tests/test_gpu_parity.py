@@ -195,13 +195,19 @@ def _scan_vs_reference(name, res, label):
     n_sites = len(g["sites"])
     ref_diff = max(1.0 - a for a in nudge["flag_agreement"]) * n_traj
     ref_off = max(1.0 - a for a in nudge["sites_within_one_step"]) * n_sites
-    print(f"{label}: flags differing {n_diff}/{n_traj} (reference vs itself, one-ulp libm: up to "
-          f"{ref_diff:.0f}), sites off by more than one step {sites_off}/{n_sites} (reference vs itself: "
-          f"up to {ref_off:.0f})")
+    # the fixed bars: flags on >= 99.9% of trajectories, cutoffs within one
+    # step on >= 99.5% of site-directions (on 200 sites one site is 0.5%: the
+    # enlarged sets of test_gpu_parity_large.py resolve that bar)
+    print(f"{label}: flags agree {1 - n_diff / n_traj:.6f} ({n_diff}/{n_traj} differ; the reference vs itself, "
+          f"one-ulp libm: up to {ref_diff:.0f}), sites within one step {1 - sites_off / n_sites:.4f} "
+          f"({sites_off}/{n_sites} off; the reference vs itself: up to {ref_off:.0f})")
     for o in off:
         print("  site off by more than one step (lat, lon, gpu, reference):", o)
     assert not outside, outside[:10]
+    assert 1 - n_diff / n_traj >= 0.999
     assert n_diff <= NUDGE_FACTOR * ref_diff + 1
+    if 1 - ref_off / n_sites >= 0.995:
+        assert 1 - sites_off / n_sites >= 0.995
     assert sites_off <= NUDGE_FACTOR * ref_off + 1
 
 
