@@ -209,3 +209,16 @@ def test_stream_launch_on_drain(ctx):
     assert ms > 0
     for b, g in zip(batches, got):
         _same(g[0], ctx.trace_batch(b, p), records=False)
+
+
+def test_stream_labels_equal_batch_labels(ctx):
+    """train_window.label_stream (the training labels, streamed in segments
+    with one parameter block per sample) equals train_window.label through
+    cor_trace_batch, sample for sample (IGRF-14 only: bit for bit)."""
+    import train_window as tw
+    s = tw.build_samples(np.random.default_rng(5), 7, "t96")
+    models = ct.model_set(ct.INTERNAL_SH)
+    ru, rl, traced = tw.label(ctx, s, models, chunk=3)
+    ru2, rl2, rc2, traced2, _ = tw.label_stream(ctx, s, models, chunk=3)
+    assert np.array_equal(ru, ru2) and np.array_equal(rl, rl2) and traced == traced2
+    assert np.all(np.isfinite(rc2))
