@@ -107,6 +107,24 @@ def work_model() -> dict:
             "flops_per_rejected_trial": 244 + 20, "source": "hand count"}
 
 
+FN_INDEX = {"exp": 1, "log": 2, "sin": 3, "cos": 4, "atan": 5, "asin": 6, "atan2": 7, "pow": 8}
+
+
+def step_flops(wm: dict, fn_flops) -> dict:
+    """FP64 work per accepted step three ways: + - * / sqrt count 1 each and a
+    transcendental counts (a) its cost measured on this GPU in FMA-pipe flops
+    (cor_probe_fp64_functions), (b) the work model's fixed weight, (c) 0."""
+    cls = wm.get("per_step_by_class")
+    if not cls:
+        return {"measured": wm["flops_per_step"], "fixed": wm["flops_per_step"], "excluded": wm["flops_per_step"]}
+    base = sum(cls[k] for k in ("add", "mul", "div", "sqrt"))
+    trans = {k: v for k, v in cls.items() if k not in ("add", "mul", "div", "sqrt") and v}
+    measured = base + sum(v * fn_flops[FN_INDEX[k]] for k, v in trans.items())
+    fixed = base + sum(trans.values()) * wm.get("transcendental_weight", 20)
+    return {"measured": measured, "fixed": fixed, "excluded": base,
+            "weights_measured": {k: round(float(fn_flops[FN_INDEX[k]]), 1) for k in trans}}
+
+
 # ---- measurement helpers -----------------------------------------------------
 class ClockSampler:
     """nvidia-smi clocks and throttle reasons sampled during the timed region."""
@@ -362,6 +380,8 @@ def run_ours(args, rank: int, world: int, dist) -> dict | None:
     ctx.set_queue_order(bool(tune["rigidity_major"]))
     peak = C.c_double(0.0)
     ctx.lib.cor_probe_fp64_peak(ctx.h, C.byref(peak))
+    fn_flops = np.zeros(11)
+    ctx._check(ctx.lib.cor_probe_fp64_functions(ctx.h, fn_flops.ctypes.data), "cor_probe_fp64_functions")
     max_jobs = max(len(j) for j, _ in steps)
     s = ct.Stream(ctx, models(), **stream_settings(max_jobs, max_jobs * N_RIG))
     base = s.upload_params(p)
@@ -412,9 +432,9 @@ def run_ours(args, rank: int, world: int, dist) -> dict | None:
     if rank != 0:
         return None
     wm = work_model()
-    rejected = trials_acc - steps_acc
-    flops = steps_acc * wm["flops_per_step"] + rejected * wm["flops_per_rejected_trial"]
-    achieved = flops / dev_s / 1e12
+    per_step = step_flops(wm, fn_flops)
+    achieved = steps_acc * per_step["measured"] / dev_s / 1e12
+    pk = peak.value / 1e12
     out = {
         "metric": METRIC, "value": sites_done / dev_s, "unit": UNIT, "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": dev_s * 1e3 / args.steps,
@@ -431,13 +451,19 @@ def run_ours(args, rank: int, world: int, dist) -> dict | None:
         "trajectories_per_s": traj_done / dev_s, "steps_per_s": steps_acc / dev_s,
         "timing": {"launch_ms_cuda_events": launch_ms, "host_wall_s": host_s,
                    "segment_done_s": [round((t - done_ns[0]) / 1e9, 3) for t in done_ns]},
-        "roofline": {"bound": "fp64", "achieved": achieved, "peak": peak.value / 1e12, "unit": "TFLOP/s",
-                     "frac": achieved / (peak.value / 1e12) if peak.value else None,
+        "roofline": {"bound": "fp64", "achieved": achieved, "peak": pk, "unit": "TFLOP/s",
+                     "frac": achieved / pk if pk else None,
+                     "frac_transcendentals_at_fixed_weight": steps_acc * per_step["fixed"] / dev_s / 1e12 / pk,
+                     "frac_transcendentals_excluded": steps_acc * per_step["excluded"] / dev_s / 1e12 / pk,
+                     "flops_per_step_measured_weights": per_step["measured"],
+                     "transcendental_weights_measured": per_step.get("weights_measured"),
+                     "division_sqrt_cost_measured": [round(float(fn_flops[9]), 1), round(float(fn_flops[10]), 1)],
                      "traffic": DRAM_BYTES_PER_TRAJ * traj_done / max(1, args.steps * world),
                      "traffic_unit": "bytes per step (one batch), scaled by trajectories from the ncu capture of "
                                      "the profiling case",
-                     "work_model": wm.get("source"),
-                     "flops_per_step": wm["flops_per_step"],
+                     "work_model": wm.get("source") + "; + - * / sqrt = 1 op, each transcendental at its cost "
+                                   "measured on this GPU (cor_probe_fp64_functions, FMA-pipe flops per call)",
+                     "flops_per_step_fixed_weight": wm["flops_per_step"],
                      "peak_source": "DFMA microbenchmark in libcortrace (cor_probe_fp64_peak), FMA = 2 flops"},
         "e2e": {"value": sites_done / e2e_s, "unit": UNIT,
                 "h2d_bytes_per_step": h2d // args.steps, "d2h_bytes_per_step": d2h // args.steps,

@@ -94,7 +94,8 @@ class BatchResult(C.Structure):
 EXPORTS = [
     "cor_ctx_create", "cor_ctx_destroy", "cor_last_error_string", "cor_abi_version", "cor_batch_count",
     "cor_prepare_trig", "cor_trace_batch", "cor_trace_batch_device", "cor_upload_params", "cor_field_batch",
-    "cor_internal_setup", "cor_gsm_setup", "cor_probe_fp64_peak", "cor_upload_crustal",
+    "cor_internal_setup", "cor_gsm_setup", "cor_probe_fp64_peak", "cor_probe_fp64_functions",
+    "cor_upload_crustal",
     "cor_trace_batch_device_noalloc", "cor_ctx_set_regroup", "cor_trace_steps", "cor_ctx_set_queue_order",
     "cor_ctx_generation_log", "cor_stream_config_default", "cor_stream_create", "cor_stream_submit",
     "cor_stream_upload_params", "cor_stream_submit_device", "cor_stream_wait", "cor_stream_drain",
@@ -134,6 +135,7 @@ def load(path: str = LIB_PATH) -> C.CDLL:
     lib.cor_trace_batch_device_noalloc.argtypes = [vp, vp, vp, i32, vp, u64, ModelSet, u64, dbl, dbl,
                                                    vp, vp, vp, C.c_uint32, vp]
     lib.cor_probe_fp64_peak.argtypes = [vp, C.POINTER(C.c_double)]
+    lib.cor_probe_fp64_functions.argtypes = [vp, vp]
     lib.cor_field_batch.argtypes = [vp, ModelSet, vp, i32, vp, vp, i64, vp]
     lib.cor_internal_setup.argtypes = [C.c_char_p, vp, vp]
     lib.cor_gsm_setup.argtypes = [vp, vp]

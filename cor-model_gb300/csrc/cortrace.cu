@@ -729,6 +729,120 @@ extern "C" int cor_probe_fp64_peak(cor_ctx* ctx, double* flops_per_s) {
     return COR_OK;
 }
 
+// ---- cost of CUDA's FP64 functions in FMA units ------------------------------
+// Each thread evaluates one function on COR_FN_CHAINS independent argument
+// streams (seeded host values, stepped by a tiny increment each call) and sums
+// the results, so the kernel is throughput-bound like the scan.  Function 0
+// is the identity: its time is the loop's own cost (the two adds per call),
+// subtracted from every other.
+constexpr int kFnChains = 4;
+constexpr int kFnArgs = 4096;
+constexpr int kFnCount = 11;   // identity, exp, log, sin, cos, atan, asin, atan2, pow, div, sqrt
+
+template <int F>
+__device__ __forceinline__ double probe_fn(double x, double y) {
+    if constexpr (F == 0) return x;
+    else if constexpr (F == 1) return exp(x);
+    else if constexpr (F == 2) return log(x);
+    else if constexpr (F == 3) return sin(x);
+    else if constexpr (F == 4) return cos(x);
+    else if constexpr (F == 5) return atan(x);
+    else if constexpr (F == 6) return asin(x);
+    else if constexpr (F == 7) return atan2(x, y);
+    else if constexpr (F == 8) return pow(x, y);
+    else if constexpr (F == 9) return x / y;
+    else return sqrt(x);
+}
+
+template <int F>
+__global__ void fp64_fn_kernel(const double* __restrict__ xs, const double* __restrict__ ys, int iters,
+                               double* __restrict__ out) {
+    const int tid = blockIdx.x * blockDim.x + threadIdx.x;
+    double x[kFnChains], y[kFnChains], acc[kFnChains];
+#pragma unroll
+    for (int c = 0; c < kFnChains; ++c) {
+        x[c] = xs[(tid * kFnChains + c) % kFnArgs];
+        y[c] = ys[(tid * kFnChains + c) % kFnArgs];
+        acc[c] = 0.;
+    }
+    for (int i = 0; i < iters; ++i) {
+#pragma unroll
+        for (int c = 0; c < kFnChains; ++c) {
+            acc[c] += probe_fn<F>(x[c], y[c]);
+            x[c] += 1e-12;
+        }
+    }
+    double t = 0.;
+#pragma unroll
+    for (int c = 0; c < kFnChains; ++c) t += acc[c];
+    out[tid] = t;
+}
+
+using FnKernel = void (*)(const double*, const double*, int, double*);
+static const FnKernel kFnKernels[kFnCount] = {fp64_fn_kernel<0>, fp64_fn_kernel<1>, fp64_fn_kernel<2>,
+                                              fp64_fn_kernel<3>, fp64_fn_kernel<4>, fp64_fn_kernel<5>,
+                                              fp64_fn_kernel<6>, fp64_fn_kernel<7>, fp64_fn_kernel<8>,
+                                              fp64_fn_kernel<9>, fp64_fn_kernel<10>};
+
+extern "C" int cor_probe_fp64_functions(cor_ctx* ctx, double* flops_per_call) {
+    if (!ctx || !flops_per_call) return COR_ERR_INVALID;
+    CUDA_TRY(ctx, cudaSetDevice(ctx->device));
+    // arguments in the ranges the field models use them (seeded LCG)
+    static const double lo[kFnCount] = {-1., -10., 0.05, -12., -12., -10., -0.99, -5., 0.1, -50., 0.};
+    static const double hi[kFnCount] = {1., 2., 200., 12., 12., 10., 0.99, 5., 10., 50., 1000.};
+    static const double ylo[kFnCount] = {0., 0., 0., 0., 0., 0., 0., -5., -2., 0.5, 0.};
+    static const double yhi[kFnCount] = {0., 0., 0., 0., 0., 0., 0., 5., 2., 20., 0.};
+    const int blocks = ctx->sms * 8, threads = 256, iters = 256;
+    const size_t n_out = (size_t)blocks * threads;
+    double *d = nullptr, *hx = nullptr;
+    CUDA_TRY(ctx, cudaMalloc(&d, sizeof(double) * (2 * kFnArgs + n_out)));
+    hx = (double*)malloc(sizeof(double) * 2 * kFnArgs);
+    if (!hx) {
+        cudaFree(d);
+        return fail(ctx, COR_ERR_NOMEM, "host allocation");
+    }
+    cudaEvent_t e0, e1;
+    cudaEventCreate(&e0);
+    cudaEventCreate(&e1);
+    float ms[kFnCount];
+    cudaError_t e = cudaSuccess;
+    uint64_t state = 0x9E3779B97F4A7C15ull;
+    for (int f = 0; f < kFnCount && e == cudaSuccess; ++f) {
+        for (int k = 0; k < 2 * kFnArgs; ++k) {
+            state = state * 6364136223846793005ull + 1442695040888963407ull;
+            const double u = (double)(state >> 11) * (1.0 / 9007199254740992.0);
+            hx[k] = k < kFnArgs ? lo[f] + u * (hi[f] - lo[f]) : ylo[f] + u * (yhi[f] - ylo[f]);
+        }
+        e = cudaMemcpy(d, hx, sizeof(double) * 2 * kFnArgs, cudaMemcpyHostToDevice);
+        if (e != cudaSuccess) break;
+        kFnKernels[f]<<<blocks, threads, 0, ctx->stream>>>(d, d + kFnArgs, 16, d + 2 * kFnArgs);  // warm-up
+        float best = 1e30f;
+        for (int r = 0; r < 3; r++) {
+            cudaEventRecord(e0, ctx->stream);
+            kFnKernels[f]<<<blocks, threads, 0, ctx->stream>>>(d, d + kFnArgs, iters, d + 2 * kFnArgs);
+            cudaEventRecord(e1, ctx->stream);
+            cudaEventSynchronize(e1);
+            float t = 0.f;
+            cudaEventElapsedTime(&t, e0, e1);
+            if (t < best) best = t;
+        }
+        ms[f] = best;
+        e = cudaGetLastError();
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    free(hx);
+    cudaFree(d);
+    if (e != cudaSuccess) return fail(ctx, COR_ERR_CUDA, "fp64 function probe: %s", cudaGetErrorString(e));
+    double peak = 0.;
+    const int rc = cor_probe_fp64_peak(ctx, &peak);
+    if (rc != COR_OK) return rc;
+    const double calls = (double)n_out * kFnChains * iters;
+    flops_per_call[0] = 0.;
+    for (int f = 1; f < kFnCount; ++f) flops_per_call[f] = (ms[f] - ms[0]) * 1e-3 * peak / calls;
+    return COR_OK;
+}
+
 // ---- scan without allocation ------------------------------------------------
 // cor_trace_batch_device_noalloc keeps its scratch in one file-scope device
 // array instead of context buffers: the work-queue counter, the generation

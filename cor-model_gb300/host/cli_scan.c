@@ -11,6 +11,7 @@
 #include <string.h>
 
 #include "cli.h"
+#include "scan_text.h"
 
 static cor_ctx *g_ctx = NULL;
 
@@ -42,53 +43,10 @@ static void job_from_header(const InfileHeader *h, cor_scan_job *j) {
     j->i_count = 0;
 }
 
-/* car_to_sph, src/utils.c:43-73 */
-static void car_to_sph(const double car[3], double sph[3]) {
-    const double x = car[0], y = car[1], z = car[2];
-    const double sq = x * x + y * y;
-    const double r = sqrt(sq + z * z);
-    if (sq != 0.) {
-        double phi = atan2(y, x);
-        const double theta = atan2(sqrt(sq), z);
-        if (phi < 0.) phi += DEF_2PI;
-        sph[0] = r; sph[1] = theta; sph[2] = phi;
-        return;
-    }
-    sph[0] = r;
-    sph[1] = z < 0. ? DEF_PI : 0.;
-    sph[2] = 0.;
-}
-
-/* One allowed row, src/trajectory.c:81-122. */
-static void write_row(FILE *out, double rig, const cor_traj_record *r) {
-    double sph[3];
-    car_to_sph(r->pos, sph);
-    const double rr = sph[0] / DEF_RE;
-    const double td = 90. - (sph[1] / DEF_TO_RAD);
-    const double fei = sph[2] / DEF_TO_RAD;
-    const double s = sin(sph[1]), c = cos(sph[1]), sf = sin(sph[2]), cf = cos(sph[2]);
-    const double be = r->vel[0] * cf + r->vel[1] * sf;
-    const double vr = be * s + r->vel[2] * c;
-    const double vt = be * c - r->vel[2] * s;
-    const double vp = -r->vel[0] * sf + r->vel[1] * cf;
-    const double va = vt * c + vr * s;
-    const double dm = sqrt(vt * vt + va * va);
-    const double ast = atan2(-vt * s + vr * c, dm) / DEF_TO_RAD;
-    double asf = (sph[2] + atan2(vp, va)) / DEF_TO_RAD;
-    if (asf > 360.) asf -= 360.;
-    fprintf(out, "%10.6f%15.10f%12.6f%10.3f%10.3f%10.3f%10.3f%12.6f%16.2f\n", rig, r->v / DEF_C, rr, td, fei, ast, asf,
-            r->time, r->length / 1000.);
-}
-
 int cli_write_scan(FILE *out, const InfileHeader *h, const cor_site_result *site, const uint8_t *status,
                    const cor_traj_record *records) {
     const int n = (int)round((h->rk - h->rig) / h->del);
-    for (int i = 0; i <= n; i++)
-        if (status[i] == COR_TRAJ_ALLOWED) write_row(out, h->rig + i * h->del, &records[i]);
-    return fprintf(out, "  CUTOFF with rigidities P(S),P(C),P(M) are:\n%12.5f%12.5f%12.5f\n\n", site->r_lower,
-                   site->r_upper, site->r_cutoff) < 0
-               ? -1
-               : 0;
+    return cor_txt_scan(out, h->rig, h->del, (int64_t)n + 1, site, status, records);
 }
 
 void trajectory_simulation_cutoff(InfileHeader *header, const Model **models, ModelsParams *models_params,
@@ -184,7 +142,7 @@ int trajectory_simulation(InfileHeader *header, const Model **models, ModelsPara
         const cor_step_record *s = steps + t * cap;
         for (uint32_t k = 0; k < cap && s[k].step == k + 1; k++) {
             double sph[3];
-            car_to_sph(s[k].pos, sph);
+            cor_txt_car_to_sph(s[k].pos, sph);
             const double r = sph[0] / DEF_RE;
             const double td = 90. - (sph[1] / DEF_TO_RAD);
             const double fei = sph[2] / DEF_TO_RAD;

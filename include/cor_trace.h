@@ -472,6 +472,16 @@ int cor_gsm_setup(const int32_t time[7], cor_model_params *out);
  * denominator of the scan's FP64 roofline; no counterpart in the reference. */
 int cor_probe_fp64_peak(cor_ctx *ctx, double *flops_per_s);
 
+/* The throughput cost of the device's FP64 functions in units of the peak
+ * above: flops_per_call[k] = (time per call, the probe loop's own cost taken
+ * out) x (cor_probe_fp64_peak flops/s), for k = 1 exp, 2 log, 3 sin, 4 cos,
+ * 5 atan, 6 asin, 7 atan2, 8 pow, 9 division, 10 sqrt ([0] = 0, the loop).
+ * Arguments are seeded values in the ranges the field models use.  These are
+ * the measured weights of the transcendentals in the scan's roofline
+ * numerator (the reference's C library functions it calls per step); no
+ * counterpart in the reference. */
+int cor_probe_fp64_functions(cor_ctx *ctx, double *flops_per_call);
+
 #ifdef __cplusplus
 }
 #endif

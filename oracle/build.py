@@ -117,6 +117,54 @@ def build_ref(force: bool = False) -> str | None:
     return REF_OUT
 
 
+def build_shim(force: bool = False) -> str | None:
+    """The reference's own `cor` program with its trajectory_simulation_cutoff
+    replaced by cor-model_gb300/host/trajectory_shim.c and linked against
+    libcortrace.so, into oracle/_ref/cor_shim: the link-in drop-in a
+    maintainer would build.  The reference's definition in src/trajectory.c is
+    renamed away at compile time; everything else of the reference (main,
+    argument parsing, INFILE reader, model registry and set-up, output
+    header) is its own code.  Needs the reference tree and the built library;
+    returns None without them."""
+    pkg = os.path.join(HERE, "..", "cor-model_gb300")
+    lib_so = os.path.join(pkg, "libcortrace.so")
+    if not ref_available() or not os.path.exists(lib_so):
+        return None
+    os.makedirs(REF_OUT, exist_ok=True)
+    src = os.path.join(REF_ROOT, "src")
+    lib = os.path.join(REF_ROOT, "lib")
+    lib_srcs = [os.path.join(lib, d, f) for d in ("internal", "t96", "ts05", "chaos")
+                for f in sorted(os.listdir(os.path.join(lib, d))) if f.endswith(".c")]
+    ref_srcs = lib_srcs + [os.path.join(src, f) for f in ("models.c", "utils.c", "io.c", "field.c", "trajectory.c",
+                                                         "main.c", "args.c")]
+    shim = os.path.join(pkg, "host", "trajectory_shim.c")
+    exe = os.path.join(REF_OUT, "cor_shim")
+    deps = ref_srcs + [shim, os.path.join(pkg, "host", "scan_text.h"), lib_so]
+    if not force and not _stale(exe, deps):
+        return exe
+    cflags = ["-std=gnu17", "-fopenmp", *FP_FLAGS, f"-I{lib}", f"-I{src}"]
+    objs = []
+    with ThreadPoolExecutor(max_workers=min(8, os.cpu_count() or 1)) as ex:
+        futs = []
+        for s in ref_srcs:
+            o = os.path.join(REF_OUT, "shim_" + os.path.relpath(s, REF_ROOT).replace(os.sep, "_")[:-2] + ".o")
+            extra = ["-Dtrajectory_simulation_cutoff=reference_trajectory_simulation_cutoff_replaced"] \
+                if s.endswith("trajectory.c") else []
+            objs.append(o)
+            futs.append(ex.submit(_run, ["gcc", *cflags, *extra, "-c", s, "-o", o]))
+        o = os.path.join(REF_OUT, "shim_trajectory_shim.o")
+        objs.append(o)
+        futs.append(ex.submit(_run, ["gcc", *cflags, f"-I{os.path.join(HERE, '..', 'include')}",
+                                     f"-I{os.path.join(pkg, 'host')}", "-c", shim, "-o", o]))
+        for f in futs:
+            f.result()
+    _run(["gcc", "-fopenmp", "-o", exe, *objs, f"-L{pkg}", "-lcortrace", f"-Wl,-rpath,{os.path.abspath(pkg)}",
+          "-lm"])
+    for o in objs:
+        os.remove(o)
+    return exe
+
+
 if __name__ == "__main__":
     print(build_port(force="--force" in sys.argv))
     print(build_ref(force="--force" in sys.argv))
