@@ -3,13 +3,18 @@
 A request is one site or a latitude/longitude grid box, one geomagnetic
 condition, vertical incidence or 9 directions (vertical plus 30 deg zenith at
 8 azimuths), scanned on the 0.01 GV grid.  Requests arrive as a seeded
-Poisson stream.  The server keeps several slots in flight, each a context
-with its own CUDA stream (continuous batching): whenever a slot is free it
-takes every admitted request that is waiting, up to a per-batch trajectory
-cap, and traces them in one call while the other slots' batches run on the
-GPU.  A request is admitted when its device memory (jobs, start vectors,
-offsets, classes, results, parameter block) fits in what the HBM budget has
-left after the requests in flight.  With a window model, each site-direction
+Poisson stream.  Two servers share one interface:
+* StreamServer (the default): persistent scan streams (cor_stream_*), one per
+  field model; every admitted request goes into its model's stream at once as
+  a segment, so requests that arrive while others run share the lanes of the
+  one resident kernel at trajectory granularity (continuous batching);
+* Server: several slots, each a context with its own CUDA stream; whenever a
+  slot is free it takes every admitted request that is waiting, up to a
+  per-batch trajectory cap, and traces them in one call while the other
+  slots' batches run.
+A request is admitted when its device memory (jobs, start vectors, offsets,
+classes, results, parameter block) fits in what the HBM budget has left after
+the requests in flight, and in the device's free memory less a reserve.  With a window model, each site-direction
 of a request with the field model the network was trained with is first
 scanned over its predicted window and falls back to the full scan on an edge
 hit; requests with another field model get the full scan.  Each request's latency runs from its arrival to the end of
@@ -225,8 +230,10 @@ class Server:
     """Continuous batching over `slots` contexts under an HBM budget."""
 
     def __init__(self, device: int = 0, slots: int = 3, hbm_budget: float = 40e9, max_batch_traj: int = 2_000_000,
-                 window_model=None, executor=None, log: RequestLog | None = None):
+                 window_model=None, executor=None, log: RequestLog | None = None, free_memory=None,
+                 reserve_bytes: float = 2e9):
         self.budget = int(hbm_budget)
+        self.admission = Admission(self.budget, free_memory, reserve_bytes)
         self.log = log
         self.in_flight = 0
         self.max_batch_traj = max_batch_traj
@@ -302,7 +309,7 @@ class Server:
                 for r in list(self.waiting):
                     b = r.device_bytes()
                     n = r.n_scans * r.n_rig
-                    if self.in_flight + mem + b > self.budget:
+                    if not self.admission.fits(self.in_flight + mem, b):
                         break                      # admission: wait for memory to free up
                     if batch and traj + n > self.max_batch_traj:
                         break
@@ -347,6 +354,247 @@ class Server:
                 self.in_flight -= sum(r.device_bytes() for r in batch)
                 self.batches += 1
                 self.lock.notify_all()
+
+
+def device_free_bytes(device: int = 0):
+    """The device's free memory now (cudaMemGetInfo through torch)."""
+    import torch
+    return lambda: torch.cuda.mem_get_info(device)[0]
+
+
+class Admission:
+    """Admits a request of b bytes when the bytes of the requests in flight
+    plus b stay within the HBM budget AND b fits in the device's free memory
+    less a reserve (free_memory: a callable giving the free bytes now, or
+    None to skip that check)."""
+
+    def __init__(self, budget: int, free_memory=None, reserve_bytes: float = 2e9):
+        self.budget = int(budget)
+        self.free_memory = free_memory
+        self.reserve = int(reserve_bytes)
+        self.waits = 0           # times a request was held back
+
+    def fits(self, in_flight: int, b: int) -> bool:
+        ok = in_flight + b <= self.budget and (self.free_memory is None or b <= self.free_memory() - self.reserve)
+        self.waits += not ok
+        return ok
+
+
+class _WindowState:
+    """One request's learned-window scan (the rule of window.trace_windows):
+    windows first, edge hits widened and traced again, then the whole grid."""
+
+    def __init__(self, jobs, i_lo, i_hi, widen: int = 3):
+        self.jobs = jobs
+        self.n_grid = np.round((jobs["rk"] - jobs["rig"]) / jobs["del"]).astype(np.int64) + 1
+        self.lo = np.asarray(i_lo, np.int64).copy()
+        self.hi = np.asarray(i_hi, np.int64).copy()
+        self.sites = np.zeros(len(jobs), ct.SITE_DTYPE)
+        self.redone = np.zeros(len(jobs), bool)
+        self.todo = np.arange(len(jobs))
+        self.attempt = 0
+        self.widen = widen
+
+    def next_jobs(self):
+        if self.attempt == self.widen + 1:
+            self.lo[self.todo] = 0
+            self.hi[self.todo] = self.n_grid[self.todo] - 1
+        return window.window_jobs(self.jobs[self.todo], self.lo[self.todo], self.hi[self.todo])
+
+    def absorb(self, res) -> bool:
+        """Takes a pass's result; returns whether another pass is needed."""
+        again = []
+        for m, j in enumerate(self.todo):
+            st = res.status[res.offsets[m]:res.offsets[m + 1]]
+            allowed = st == ct.TRAJ_ALLOWED
+            low = self.lo[j] > 0 and allowed[0]
+            high = self.hi[j] < self.n_grid[j] - 1 and not allowed[-1]
+            if not (low or high):
+                self.sites[j] = res.sites[m]
+                continue
+            width = self.hi[j] - self.lo[j] + 1
+            if low:
+                self.lo[j] = max(0, self.lo[j] - width)
+            if high:
+                self.hi[j] = min(self.n_grid[j] - 1, self.hi[j] + width)
+            again.append(j)
+        self.redone[again] = True
+        self.todo = np.array(again, np.int64)
+        self.attempt += 1
+        return len(again) > 0
+
+
+class StreamServer:
+    """Serving on persistent scan streams (cor_stream_*): one stream per field
+    model, the SMs split between them with `reserve_sms` left for the window
+    network.  Every admitted request goes in at once as a segment of its
+    model's stream (window passes as further segments), so requests that
+    arrive while others are on the GPU share the device's lanes with them at
+    trajectory granularity: a lane that finishes a trajectory of one request
+    takes the next trajectory of whichever request is next in the queue.
+    Admission: the HBM budget over the requests in flight and the device's
+    free memory (Admission).  Same interface as Server."""
+
+    def __init__(self, device: int = 0, hbm_budget: float = 40e9, window_model=None, log: RequestLog | None = None,
+                 externals=(ct.EXTERNAL_TS05,), free_memory="device", reserve_bytes: float = 2e9,
+                 stream_slots: int = 32, max_segment_traj: int = 1_200_000, reserve_sms: int = 2,
+                 idle_drain_s: float = 1.0):
+        import torch
+        self.budget = int(hbm_budget)
+        if free_memory == "device":
+            free_memory = device_free_bytes(device)
+        self.admission = Admission(self.budget, free_memory, reserve_bytes)
+        self.log = log
+        models = window_model if isinstance(window_model, (list, tuple)) else [window_model]
+        self.window_models = {getattr(m, "external", None): m for m in models if m is not None}
+        self.lock = threading.Condition()
+        self.waiting: list[Request] = []
+        self.rejected: list[Request] = []
+        self.closed = False
+        self.in_flight = 0
+        self.batches = 0
+        self.t0 = None
+        self.idle_drain_s = idle_drain_s
+        self.ctx = ct.Context(device)
+        sms = torch.cuda.get_device_properties(device).multi_processor_count
+        share = max(1, (sms - reserve_sms) // max(1, len(externals)))
+        self.streams = {ext: ct.Stream(self.ctx, ct.model_set(ct.INTERNAL_SH, ext), slots=stream_slots,
+                                       max_jobs=max_segment_traj // 100, max_trajectories=max_segment_traj,
+                                       max_params=1, pool_params=4096, reserve_sms=sms - share, idle_limit_s=600.0)
+                        for ext in externals}
+        self.max_segment_traj = max_segment_traj
+        self.thread = threading.Thread(target=self._loop, daemon=True)
+        self.error = None
+
+    def start(self):
+        self.t0 = time.perf_counter()
+        self.thread.start()
+
+    def now(self) -> float:
+        return time.perf_counter() - self.t0
+
+    def submit(self, req: Request):
+        if req.device_bytes() > self.budget or req.external not in self.streams:
+            req.done_at = self.now()
+            if self.log:
+                self.log.rejected(req)
+            with self.lock:
+                self.rejected.append(req)
+            return
+        if self.log:
+            self.log.submitted(req)
+        with self.lock:
+            self.waiting.append(req)
+            self.lock.notify_all()
+
+    def close(self):
+        with self.lock:
+            self.closed = True
+            self.lock.notify_all()
+        self.thread.join()
+        for st in self.streams.values():
+            st.close()
+        self.ctx.close()
+        if self.error:
+            raise self.error
+
+    # -- the dispatcher: admit, submit segments, collect finished ones
+    def _start(self, r: Request, pending: list):
+        params = ct.internal_setup("igrf14", r.time7, parmod=r.parmod)
+        jobs = request_jobs(r, 0)
+        wm = self.window_models.get(r.external)
+        state = None
+        if wm is not None:
+            i_lo, i_hi = wm.windows(request_features(r, params))   # on the SMs the streams leave free
+            state = _WindowState(jobs, i_lo, i_hi)
+            pending.append((r, params, state, state.next_jobs()))
+        else:
+            # whole scans, split so that no segment exceeds the stream's size
+            per = max(1, self.max_segment_traj // r.n_rig)
+            r._parts = [None] * ((len(jobs) + per - 1) // per)
+            for k in range(0, len(jobs), per):
+                pending.append((r, params, ("part", k // per), jobs[k:k + per]))
+        r._state = state
+
+    def _loop(self):
+        from collections import deque
+        pending = deque()        # (request, params, state or ("part", k), jobs) waiting for a ring slot
+        inflight = {ext: deque() for ext in self.streams}   # (ticket, request, params, state)
+        last_busy = time.perf_counter()
+        try:
+            while True:
+                admitted = []
+                with self.lock:
+                    for r in list(self.waiting):
+                        b = r.device_bytes()
+                        if not self.admission.fits(self.in_flight, b):
+                            break
+                        self.waiting.remove(r)
+                        self.in_flight += b
+                        admitted.append(r)
+                    done_all = self.closed and not self.waiting and not pending and \
+                        not any(inflight.values())
+                if done_all:
+                    return
+                for r in admitted:
+                    r._open = 0
+                    self._start(r, pending)
+                progressed = bool(admitted)
+                for _ in range(len(pending)):
+                    r, params, state, jobs = pending[0]
+                    st = self.streams[r.external]
+                    if len(inflight[r.external]) >= st.config.slots:
+                        pending.rotate(-1)
+                        continue
+                    t = st.submit(jobs, params)
+                    pending.popleft()
+                    inflight[r.external].append((t, r, params, state))
+                    r._open += 1
+                    progressed = True
+                for ext, q in inflight.items():
+                    st = self.streams[ext]
+                    for _ in range(len(q)):
+                        t, r, params, state = q[0]
+                        got = st.wait(t, 0)
+                        if got is None:
+                            q.rotate(-1)
+                            continue
+                        q.popleft()
+                        progressed = True
+                        r._open -= 1
+                        res = got[0]
+                        if isinstance(state, _WindowState):
+                            if state.absorb(res):
+                                pending.append((r, params, state, state.next_jobs()))
+                                continue
+                            r.result, r.fallback = state.sites, int(state.redone.sum())
+                        else:
+                            r._parts[state[1]] = res.sites
+                            if r._open or any(p is None for p in r._parts):
+                                continue
+                            r.result, r.fallback = np.concatenate(r._parts), 0
+                        if r._open:
+                            continue
+                        r.done_at = self.now()
+                        if self.log:
+                            self.log.completed([r])
+                        with self.lock:
+                            self.in_flight -= r.device_bytes()
+                            self.batches += 1
+                            self.lock.notify_all()
+                if progressed:
+                    last_busy = time.perf_counter()
+                elif not pending and not any(inflight.values()):
+                    if time.perf_counter() - last_busy > self.idle_drain_s:
+                        for st in self.streams.values():
+                            st.drain()                    # nothing in flight: let the kernels end
+                        last_busy = time.perf_counter()
+                    with self.lock:
+                        self.lock.wait(0.005)
+                else:
+                    time.sleep(0.0005)
+        except Exception as e:  # noqa: BLE001
+            self.error = e
 
 
 def run_stream(server: Server, reqs: list[Request]) -> dict:
@@ -397,6 +645,9 @@ def main():
     ap.add_argument("--rate", type=float, default=1.0, help="requests per second")
     ap.add_argument("--requests", type=int, default=20)
     ap.add_argument("--seed", type=int, default=7)
+    ap.add_argument("--server", default="stream", choices=["stream", "slots"],
+                    help="stream: every request a segment of a persistent scan stream; slots: per-call batches "
+                         "over --slots contexts")
     ap.add_argument("--slots", type=int, default=3)
     ap.add_argument("--budget-gb", type=float, default=40.0)
     ap.add_argument("--external", default="ts05", choices=["t96", "ts05"])
@@ -416,10 +667,17 @@ def main():
         restored, reqs = resume(args.log, reqs)
     wms = [window.WindowModel(f) for f in args.window]
     log = RequestLog(args.log) if args.log else None
-    srv = Server(0, args.slots, args.budget_gb * 1e9, window_model=wms, log=log)
+    if args.server == "stream":
+        srv = StreamServer(0, args.budget_gb * 1e9, window_model=wms, log=log, externals=(ext,))
+    else:
+        srv = Server(0, args.slots, args.budget_gb * 1e9, window_model=wms, log=log,
+                     free_memory=device_free_bytes(0))
     out = run_stream(srv, reqs)
-    out.update({"rate": args.rate, "seed": args.seed, "slots": args.slots, "external": args.external,
-                "window": [os.path.basename(f) for f in args.window], "restored_from_log": len(restored)})
+    out.update({"rate": args.rate, "seed": args.seed, "server": args.server, "external": args.external,
+                "window": [os.path.basename(f) for f in args.window], "restored_from_log": len(restored),
+                "admission_waits": srv.admission.waits})
+    if args.server == "slots":
+        out["slots"] = args.slots
     print(json.dumps(out), flush=True)
     if log:
         log.close()

@@ -23,9 +23,16 @@ import cortrace as ct  # noqa: E402  (dtype and struct layouts of include/cor_tr
 import build as obuild  # noqa: E402
 
 _lib = None
+_load_lock = __import__("threading").Lock()
 
 
 def load() -> C.CDLL:
+    global _lib
+    with _load_lock:          # one build at a time when several threads load it first
+        return _load()
+
+
+def _load() -> C.CDLL:
     global _lib
     if _lib is None:
         path = obuild.build_port()

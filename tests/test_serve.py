@@ -193,3 +193,55 @@ def test_one_window_network_per_field_model():
     srv = serve.Server(slots=1, executor=executor, window_model=[_M(ct.EXTERNAL_T96), _M(ct.EXTERNAL_TS05)])
     assert serve.run_stream(srv, reqs)["completed"] == 4
     assert {ext for ext, _ in seen} == {ct.EXTERNAL_T96, ct.EXTERNAL_TS05} and all(used for _, used in seen)
+
+
+def test_admission_waits_for_free_device_memory():
+    """The device reports too little free memory for the first polls: no
+    request is admitted (the executor is not called) until it reports
+    enough; then every request completes."""
+    reqs = _small(serve.poisson_stream(23, 1000.0, 4, max_box_sites=4))
+    polls = {"n": 0}
+
+    def free():
+        polls["n"] += 1
+        return 0 if polls["n"] < 40 else 10 ** 12
+
+    calls = []
+
+    def executor(ctx, jobs, params, models, feats):
+        calls.append(polls["n"])
+        res = pyoracle.scan_batch(jobs, params, models=models, threads=2)
+        return res.sites, np.zeros(len(jobs), bool)
+    srv = serve.Server(slots=2, executor=executor, free_memory=free, reserve_bytes=1e9)
+    out = serve.run_stream(srv, reqs)
+    assert out["completed"] == 4
+    assert srv.admission.waits > 0
+    assert calls and min(calls) >= 40
+
+
+def test_admission_rule():
+    adm = serve.Admission(1000, free_memory=lambda: 700, reserve_bytes=200)
+    assert adm.fits(0, 500) and not adm.fits(0, 501)          # free less the reserve
+    assert not adm.fits(600, 500) and adm.fits(500, 500)      # the budget over the requests in flight
+    assert serve.Admission(1000).fits(999, 1) and not serve.Admission(1000).fits(999, 2)
+
+
+def test_window_state_widens_then_takes_the_whole_grid():
+    """The per-request window state of the stream server follows
+    window.trace_windows: an edge hit widens that side, and after the
+    widenings the whole grid is scanned."""
+    import window
+    jobs = ct.make_job(10.0, 20.0, rig=0.01, rk=20.0, dele=0.01)
+    st = serve._WindowState(jobs, [100], [120], widen=1)
+    j1 = st.next_jobs()
+    assert int(j1["i_first"][0]) == 100 and int(j1["i_count"][0]) == 21
+    n = 21
+    res = ct.ScanResult(np.zeros(1, ct.SITE_DTYPE), np.full(n, ct.TRAJ_ALLOWED, np.uint8), None,
+                        np.array([0, n], np.uint64), {})
+    assert st.absorb(res)                                   # first allowed: widen downwards
+    j2 = st.next_jobs()
+    assert int(j2["i_first"][0]) == 79
+    assert st.absorb(ct.ScanResult(np.zeros(1, ct.SITE_DTYPE), np.full(42, ct.TRAJ_ALLOWED, np.uint8), None,
+                                   np.array([0, 42], np.uint64), {}))
+    j3 = st.next_jobs()                                     # after `widen` widenings: the whole grid
+    assert int(j3["i_first"][0]) == 0 and int(j3["i_count"][0]) == window.GRID_N
