@@ -309,7 +309,7 @@ def measure_window(args, ctx, bufs, plain, p, plain_e2e: float) -> dict:
     timed = list(range(args.warmup, args.warmup + args.steps))
     jobs = np.concatenate([bufs[i]["host_jobs"] for i in timed])
     feats = np.concatenate([site_features(bufs[i]["latlon"]) for i in timed])
-    s = ct.Stream(ctx, models(), **stream_settings(len(jobs), len(jobs) * N_RIG))
+    s = ct.Stream(ctx, models(), scan_events=1, **stream_settings(len(jobs), len(jobs) * N_RIG))
     wm.windows(feats[:8])                            # load the network's kernels before timing
     t0 = time.perf_counter()
     i_lo, i_hi = wm.windows(feats)                   # no stream kernel runs now: the network has the SMs
@@ -330,7 +330,8 @@ def measure_window(args, ctx, bufs, plain, p, plain_e2e: float) -> dict:
             "model": json.loads(wm.info) if wm.info.startswith("{") else wm.info,
             "how": "predicted window +-3 sigma on the 0.01 GV grid, widened on the hit side on an edge hit (full scan "
                    "after 3 widenings); the timed steps' windows as one segment of a scan stream (ascending "
-                   "rigidity), host buffers, network inference on the tensor cores inside the timed region"}
+                   "rigidity), each scan's result taken as soon as it is reduced so that a retrace starts at once; "
+                   "host buffers, network inference on the tensor cores inside the timed region"}
 
 
 def reduce_over_ranks(dist, seconds: float, counts: list, device: str) -> list:

@@ -51,12 +51,14 @@ RECORD_DTYPE = np.dtype([
 SITE_DTYPE = np.dtype([
     ("r_lower", "f8"), ("r_upper", "f8"), ("r_cutoff", "f8"),
     ("n_forbidden", "i4"), ("n_traj", "i4")], align=True)
+SCAN_EVENT_DTYPE = np.dtype([("site", SITE_DTYPE), ("first_class", "u1"), ("last_class", "u1"),
+                             ("reserved", "u2"), ("reserved2", "u4"), ("seq1", "u8")], align=True)
 TRIG_DTYPE = np.dtype([(k, "f8") for k in ("st0", "ct0", "sp0", "cp0", "st1", "ct1", "sp1", "cp1")], align=True)
 
 STEP_DTYPE = np.dtype([("gsm", "f8", 3), ("pos", "f8", 3), ("v", "f8"), ("time", "f8"), ("length", "f8"),
                        ("step", "u4"), ("reserved", "u4")], align=True)
 assert JOB_DTYPE.itemsize == 88 and PARAMS_DTYPE.itemsize == 2672 and STEP_DTYPE.itemsize == 80
-assert RECORD_DTYPE.itemsize == 88 and SITE_DTYPE.itemsize == 32
+assert RECORD_DTYPE.itemsize == 88 and SITE_DTYPE.itemsize == 32 and SCAN_EVENT_DTYPE.itemsize == 48
 
 
 class ModelSet(C.Structure):
@@ -83,7 +85,7 @@ class StreamConfig(C.Structure):
     _fields_ = [("slots", C.c_int32), ("max_jobs", C.c_int32), ("max_trajectories", C.c_int64),
                 ("max_params", C.c_int32), ("want_records", C.c_int32), ("reserve_sms", C.c_int32),
                 ("fixed_params", C.c_int32), ("pool_params", C.c_int32), ("segments_per_launch", C.c_int32),
-                ("idle_limit_s", C.c_double), ("launch_on_drain", C.c_int32), ("reserved", C.c_int32)]
+                ("idle_limit_s", C.c_double), ("launch_on_drain", C.c_int32), ("scan_events", C.c_int32)]
 
 
 class BatchResult(C.Structure):
@@ -99,6 +101,7 @@ EXPORTS = [
     "cor_trace_batch_device_noalloc", "cor_ctx_set_regroup", "cor_trace_steps", "cor_ctx_set_queue_order",
     "cor_ctx_generation_log", "cor_stream_config_default", "cor_stream_create", "cor_stream_submit",
     "cor_stream_upload_params", "cor_stream_submit_device", "cor_stream_wait", "cor_stream_drain",
+    "cor_stream_poll_scans",
     "cor_stream_close",
 ]
 NOALLOC_MAX_TRAJ = 1048576  # COR_NOALLOC_MAX_TRAJ
@@ -147,6 +150,7 @@ def load(path: str = LIB_PATH) -> C.CDLL:
     lib.cor_stream_submit_device.argtypes = [vp, vp, vp, vp, vp, i32, vp, vp, vp, C.POINTER(i64)]
     lib.cor_stream_wait.argtypes = [vp, i64, i32, C.POINTER(BatchResult), C.POINTER(u64)]
     lib.cor_stream_drain.argtypes = [vp, C.POINTER(C.c_double)]
+    lib.cor_stream_poll_scans.argtypes = [vp, i64, i32, i32, vp, vp]
     lib.cor_stream_close.argtypes = [vp]
     _lib = lib
     return lib
@@ -395,6 +399,18 @@ class Stream:
         if meta:
             return ScanResult(sites, status, records, off, res.counters.as_dict()), int(t_ns.value)
         return res.counters.as_dict(), int(t_ns.value)
+
+    def poll_scans(self, ticket: int, first: int = 0, count: int | None = None):
+        """cor_stream_poll_scans: (done flags, SCAN_EVENT_DTYPE records) of
+        scans first .. first+count-1 of an outstanding segment."""
+        if count is None:
+            count = self._pending[ticket][0] - first
+        done = np.zeros(count, np.uint8)
+        ev = np.zeros(count, SCAN_EVENT_DTYPE)
+        rc = self.lib.cor_stream_poll_scans(self.h, ticket, first, count, _ptr(done), _ptr(ev))
+        if rc < 0:
+            self.ctx._check(rc, "cor_stream_poll_scans")
+        return done.astype(bool), ev
 
     def drain(self) -> float:
         """cor_stream_drain: ends the current launch once everything published

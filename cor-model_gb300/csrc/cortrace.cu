@@ -1050,6 +1050,8 @@ struct cor_stream {
     unsigned char* last_params = nullptr;  // the previous submit's blocks (host copy) for reuse
     int32_t last_n = 0, last_base = -1;
     StreamArgs args;
+    cor_scan_event* events_h = nullptr;        // mapped: slots x max_jobs per-scan results (scan_events)
+    cor_scan_event* events_d = nullptr;
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;  // around the current launch, on ks
     bool timed = false;                        // ev0/ev1 hold a launch not yet drained
     bool pending_launch = false;               // launch_on_drain: segments wait for cor_stream_drain
@@ -1068,7 +1070,7 @@ extern "C" void cor_stream_config_default(cor_stream_config* c) {
     c->segments_per_launch = 65536;
     c->idle_limit_s = 60.;
     c->launch_on_drain = 0;
-    c->reserved = 0;
+    c->scan_events = 0;
 }
 
 static void stream_free(cor_stream* s) {
@@ -1090,7 +1092,7 @@ static void stream_free(cor_stream* s) {
     void* dev[] = {s->segs_dev, s->seg_end_dev, s->pool_dev, s->queue_dev};
     for (void* p : dev)
         if (p) cudaFree(p);
-    void* host[] = {s->h_params, s->h_queue, s->mapped};
+    void* host[] = {s->h_params, s->h_queue, s->mapped, s->events_h};
     for (void* p : host)
         if (p) cudaFreeHost(p);
     free(s->last_params);
@@ -1115,7 +1117,7 @@ extern "C" int cor_stream_create(cor_ctx* ctx, cor_model_set models, uint64_t st
         cfg.fixed_params < 0 || cfg.pool_params < cfg.max_params || cfg.segments_per_launch < 1 ||
         cfg.reserve_sms < 0 || cfg.reserve_sms >= ctx->sms || !(cfg.idle_limit_s > 0.) ||
         cfg.idle_limit_s > 86400. || (cfg.want_records != 0 && cfg.want_records != 1) ||
-        (cfg.launch_on_drain != 0 && cfg.launch_on_drain != 1) || cfg.reserved != 0)
+        (cfg.launch_on_drain != 0 && cfg.launch_on_drain != 1) || (cfg.scan_events != 0 && cfg.scan_events != 1))
         return fail(ctx, COR_ERR_INVALID, "stream configuration out of range");
     const ModelOps* ops = find_ops(models);
     if (!ops) return fail(ctx, COR_ERR_UNSUPPORTED, "model set not available");
@@ -1161,6 +1163,14 @@ extern "C" int cor_stream_create(cor_ctx* ctx, cor_model_set models, uint64_t st
         s->err_h = (unsigned int*)((char*)s->done_h + sizeof(StreamDone) * (size_t)cfg.slots);
         s->err_d = (unsigned int*)((char*)s->done_d + sizeof(StreamDone) * (size_t)cfg.slots);
         s->ctl_h->stop_at = ~0ull;
+        if (cfg.scan_events) {
+            const size_t eb = sizeof(cor_scan_event) * (size_t)cfg.slots * nj;
+            SALLOC(cudaHostAlloc(&s->events_h, eb, cudaHostAllocMapped));
+            memset(s->events_h, 0, eb);
+            void* ed = nullptr;
+            SALLOC(cudaHostGetDevicePointer(&ed, s->events_h, 0));
+            s->events_d = (cor_scan_event*)ed;
+        }
         s->last_params = (unsigned char*)malloc(sizeof(cor_model_params) * (size_t)cfg.max_params);
         s->slots = new StreamSlot[cfg.slots];
         if (!s->last_params) {
@@ -1411,6 +1421,7 @@ extern "C" int cor_stream_submit(cor_stream* s, const cor_scan_job* jobs, int32_
     g.n_jobs = n_jobs;
     g.n_rig = (offsets_uniform(sl.h_off, n_jobs) && s->ctx->rig_major) ? (uint32_t)(sl.h_off[1] - sl.h_off[0]) : 0u;
     g.order = nullptr;
+    g.events = s->events_d ? s->events_d + (size_t)(seq % s->cfg.slots) * (size_t)s->cfg.max_jobs : nullptr;
     if (!g.n_rig && s->ctx->rig_major && n_jobs > 1) {
         // scans of different lengths: hand out all their trajectories in
         // ascending rigidity, as the rigidity-major order does for a uniform
@@ -1486,6 +1497,7 @@ extern "C" int cor_stream_submit_device(cor_stream* s, const cor_scan_job* jobs_
     g.n_jobs = n_jobs;
     g.n_rig = (offsets_uniform(offsets_host, n_jobs) && s->ctx->rig_major) ? (uint32_t)offsets_host[1] : 0u;
     g.order = nullptr;
+    g.events = nullptr;
     if ((rc = stream_publish(s, sl, seq, n_traj)) != COR_OK) return rc;
     *ticket = seq;
     return COR_OK;
@@ -1561,6 +1573,35 @@ extern "C" int cor_stream_wait(cor_stream* s, int64_t ticket, int32_t timeout_ms
     }
     sl.busy = false;
     return COR_OK;
+}
+
+extern "C" int cor_stream_poll_scans(cor_stream* s, int64_t ticket, int32_t first, int32_t count, uint8_t* done,
+                                     cor_scan_event* events) {
+    if (!s) return COR_ERR_INVALID;
+    cor_ctx* ctx = s->ctx;
+    if (!s->events_h) return fail(ctx, COR_ERR_INVALID, "the stream was created without scan_events");
+    if (ticket < 0 || ticket >= s->next_seq) return fail(ctx, COR_ERR_INVALID, "unknown ticket %lld", (long long)ticket);
+    const unsigned slot = (unsigned)(ticket % s->cfg.slots);
+    const StreamSlot& sl = s->slots[slot];
+    if (!sl.busy || sl.seq != ticket || !sl.own)
+        return fail(ctx, COR_ERR_INVALID, "ticket %lld is not an outstanding cor_stream_submit segment",
+                    (long long)ticket);
+    if (first < 0 || count < 0 || (int64_t)first + count > sl.n_jobs)
+        return fail(ctx, COR_ERR_INVALID, "scans %d .. %d outside the segment's %d", first, first + count - 1,
+                    sl.n_jobs);
+    const cor_scan_event* base = s->events_h + (size_t)slot * (size_t)s->cfg.max_jobs;
+    int n = 0;
+    for (int32_t k = 0; k < count; k++) {
+        const cor_scan_event* e = base + first + k;
+        const bool d = sl.empty ? false
+                                : __atomic_load_n(&e->seq1, __ATOMIC_ACQUIRE) == (unsigned long long)ticket + 1;
+        if (done) done[k] = d ? 1 : 0;
+        if (d) {
+            n++;
+            if (events) memcpy(&events[k], e, sizeof(cor_scan_event));
+        }
+    }
+    return n;
 }
 
 extern "C" int cor_stream_drain(cor_stream* s, double* launch_ms) {

@@ -47,6 +47,7 @@ struct StreamSeg {
     int32_t n_jobs;
     uint32_t n_rig;                // > 0: rigidity-major order (the host checked that every scan has n_rig)
     const uint32_t* order;         // queue position -> trajectory (offsets space), or null; overrides n_rig
+    cor_scan_event* events;        // device address of mapped host records, one per scan, or null
 };
 
 // Host-written control block (mapped pinned memory).
@@ -230,6 +231,16 @@ __global__ void __launch_bounds__(kTraceThreads, 1) stream_kernel(const StreamAr
             const cor_site_result r = reduce_scan_warp(job, ldcg_ptr(&sg->status), b, e);
             if (lane == 0) {
                 ldcg_ptr(&sg->sites)[j] = r;
+                cor_scan_event* ev = ldcg_ptr(&sg->events);
+                if (ev) {
+                    // this scan's result straight to the host, before its segment completes
+                    ev[j].site = r;
+                    ev[j].first_class = __ldcg(ldcg_ptr(&sg->status) + b);
+                    ev[j].last_class = __ldcg(ldcg_ptr(&sg->status) + (e - 1));
+                    ev[j].reserved = 0;
+                    __threadfence_system();
+                    st_release_sys(reinterpret_cast<unsigned long long*>(&ev[j].seq1), sq + 1);
+                }
                 atomicExch(ldcg_ptr(&sg->job_done) + j, 0u);
                 __threadfence();
                 unsigned long long* acc = ldcg_ptr(&sg->acc);

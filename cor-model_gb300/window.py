@@ -285,15 +285,19 @@ def trace_windows(ctx, jobs, params, models, i_lo, i_hi, widen: int = 3, **kw):
     return sites, redone, traced, steps
 
 
-def trace_windows_stream(stream, items, widen: int = 3):
+def trace_windows_stream(stream, items, widen: int = 3, poll_s: float = 0.002):
     """trace_windows for many batches at once through a scan stream
     (cortrace.Stream): items are (jobs, params, i_lo, i_hi).  Every batch's
-    windows go in as one segment; the jobs of a segment whose window had a
-    boundary on an edge go back in as a new segment over widened windows (the
-    same rule as trace_windows), so first passes and retraces of different
-    batches are in flight together.  Returns, per item, (sites, mask of jobs
-    that needed more than one pass, trajectories traced, accepted steps)."""
+    windows go in as one segment; a scan whose window had a boundary on an
+    edge goes back in over a widened window (the same rule as trace_windows),
+    so first passes and retraces are in flight together.  With a stream made
+    with scan_events=1, each scan's result is taken the moment the scan is
+    reduced (cor_stream_poll_scans) and its retrace goes in at once, without
+    waiting for the rest of its segment.  Returns, per item, (sites, mask of
+    jobs that needed more than one pass, trajectories traced, accepted steps)."""
     from collections import deque
+    import time
+    events = bool(stream.config.scan_events)
     state = []
     for jobs, params, i_lo, i_hi in items:
         n_grid = np.round((jobs["rk"] - jobs["rig"]) / jobs["del"]).astype(np.int64) + 1
@@ -302,8 +306,24 @@ def trace_windows_stream(stream, items, widen: int = 3):
                       "sites": np.zeros(len(jobs), ct.SITE_DTYPE), "redone": np.zeros(len(jobs), bool),
                       "traced": 0, "steps": 0})
     todo = deque((k, np.arange(len(it[0])), 0) for k, it in enumerate(items) if len(it[0]))
-    inflight = deque()
+    inflight = []
     slots = int(stream.config.slots)
+
+    def judge(S, j, first_allowed: bool, last_allowed: bool, site) -> bool:
+        """Takes scan j's pass; returns whether it must be traced again."""
+        low = S["lo"][j] > 0 and first_allowed
+        high = S["hi"][j] < S["n_grid"][j] - 1 and not last_allowed
+        if not (low or high):
+            S["sites"][j] = site
+            return False
+        width = S["hi"][j] - S["lo"][j] + 1
+        if low:
+            S["lo"][j] = max(0, S["lo"][j] - width)
+        if high:
+            S["hi"][j] = min(S["n_grid"][j] - 1, S["hi"][j] + width)
+        S["redone"][j] = True
+        return True
+
     while todo or inflight:
         while todo and len(inflight) < slots:
             k, idx, attempt = todo.popleft()
@@ -311,31 +331,44 @@ def trace_windows_stream(stream, items, widen: int = 3):
             if attempt == widen + 1:                   # last resort: the whole grid
                 S["lo"][idx] = 0
                 S["hi"][idx] = S["n_grid"][idx] - 1
-            t = stream.submit(window_jobs(S["jobs"][idx], S["lo"][idx], S["hi"][idx]), S["params"])
-            inflight.append((t, k, idx, attempt))
-        t, k, idx, attempt = inflight.popleft()
-        res, _ = stream.wait(t, -1)
-        S = state[k]
-        S["traced"] += int(res.counters["trajectories"])
-        S["steps"] += int(res.counters["accepted_steps"])
-        again = []
-        for m, j in enumerate(idx):
-            st = res.status[res.offsets[m]:res.offsets[m + 1]]
-            allowed = st == ct.TRAJ_ALLOWED
-            low = S["lo"][j] > 0 and allowed[0]
-            high = S["hi"][j] < S["n_grid"][j] - 1 and not allowed[-1]
-            if not (low or high):
-                S["sites"][j] = res.sites[m]
-                continue
-            width = S["hi"][j] - S["lo"][j] + 1
-            if low:
-                S["lo"][j] = max(0, S["lo"][j] - width)
-            if high:
-                S["hi"][j] = min(S["n_grid"][j] - 1, S["hi"][j] + width)
-            again.append(j)
-        if again:
-            S["redone"][again] = True
-            todo.append((k, np.array(again, np.int64), attempt + 1))
+            t = stream.submit(window_jobs(S["jobs"][idx], S["lo"][idx], S["hi"][idx]), S["params"],
+                              want_status=not events)
+            inflight.append({"t": t, "k": k, "idx": idx, "attempt": attempt, "seen": np.zeros(len(idx), bool)})
+        progressed = False
+        again = {}
+        for seg in list(inflight):
+            S = state[seg["k"]]
+            key = (seg["k"], seg["attempt"] + 1)
+            if events:
+                done, ev = stream.poll_scans(seg["t"])
+                new = np.nonzero(done & ~seg["seen"])[0]
+                for m in new:
+                    j = seg["idx"][m]
+                    if judge(S, j, ev[m]["first_class"] == ct.TRAJ_ALLOWED, ev[m]["last_class"] == ct.TRAJ_ALLOWED,
+                             ev[m]["site"]):
+                        again.setdefault(key, []).append(j)
+                seg["seen"][new] = True
+                progressed |= len(new) > 0
+                if not seg["seen"].all():
+                    continue
+                res, _ = stream.wait(seg["t"], -1)
+            else:
+                got = stream.wait(seg["t"], 0)
+                if got is None:
+                    continue
+                res = got[0]
+                for m, j in enumerate(seg["idx"]):
+                    st = res.status[res.offsets[m]:res.offsets[m + 1]]
+                    if judge(S, j, st[0] == ct.TRAJ_ALLOWED, st[-1] == ct.TRAJ_ALLOWED, res.sites[m]):
+                        again.setdefault(key, []).append(j)
+            inflight.remove(seg)
+            progressed = True
+            S["traced"] += int(res.counters["trajectories"])
+            S["steps"] += int(res.counters["accepted_steps"])
+        for (k, attempt), js in again.items():
+            todo.append((k, np.array(js, np.int64), attempt))
+        if not progressed and not todo:
+            time.sleep(poll_s)
     return [(S["sites"], S["redone"], S["traced"], S["steps"]) for S in state]
 
 

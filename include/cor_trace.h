@@ -355,7 +355,8 @@ typedef struct {
     int32_t launch_on_drain;   /* 1: submits only stage and publish; cor_stream_drain launches the kernel
                                   with everything published and the stop index already set, so the launch
                                   never waits on the host (at most `slots` segments per launch; default 0) */
-    int32_t reserved;
+    int32_t scan_events;       /* 1: each cor_stream_submit scan's result is also written to mapped host
+                                  memory as soon as it is reduced (cor_stream_poll_scans; default 0)     */
 } cor_stream_config;
 
 void cor_stream_config_default(cor_stream_config *cfg);
@@ -380,6 +381,29 @@ int cor_stream_create(cor_ctx *ctx, cor_model_set models, uint64_t step_limit, d
  * the longest trajectories start first. */
 int cor_stream_submit(cor_stream *s, const cor_scan_job *jobs, int32_t n_jobs, const cor_model_params *params,
                       int32_t n_params, int64_t *ticket);
+
+/* The result of one scan of a segment as the stream kernel reports it the
+ * moment the scan's last trajectory is reduced, before the rest of its
+ * segment has finished (cor_stream_poll_scans). */
+typedef struct {
+    cor_site_result site;   /* P(S), P(C), P(M) as cor_trace_batch gives them              */
+    uint8_t first_class;    /* COR_TRAJ_* of the scan's first traced rigidity              */
+    uint8_t last_class;     /* COR_TRAJ_* of its last                                      */
+    uint16_t reserved;
+    uint32_t reserved2;
+    uint64_t seq1;          /* the segment's ticket + 1 once this record is the scan's     */
+} cor_scan_event;
+
+/* Which scans of an outstanding cor_stream_submit segment have finished so
+ * far (the stream must have been created with scan_events = 1): for scans
+ * first .. first+count-1 of the segment, done[k] is set to 1 when scan
+ * first+k has finished, and then events[k] holds its result (either array may
+ * be NULL to skip it).  Returns the number of finished scans in the range.
+ * No counterpart in the reference: it lets a caller act on a scan (a window
+ * edge hit, a small request inside a big segment) without waiting for the
+ * whole segment. */
+int cor_stream_poll_scans(cor_stream *s, int64_t ticket, int32_t first, int32_t count, uint8_t *done,
+                          cor_scan_event *events);
 
 /* Parameter blocks for cor_stream_submit_device: appended to the stream's
  * fixed pool, where they stay for the stream's lifetime; *first_index is the

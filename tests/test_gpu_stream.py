@@ -222,3 +222,31 @@ def test_stream_labels_equal_batch_labels(ctx):
     ru2, rl2, rc2, traced2, _ = tw.label_stream(ctx, s, models, chunk=3)
     assert np.array_equal(ru, ru2) and np.array_equal(rl, rl2) and traced == traced2
     assert np.all(np.isfinite(rc2))
+
+
+def test_window_scan_reacts_to_scan_events(ctx):
+    """window.trace_windows_stream on a stream with per-scan events (each
+    scan's result read the moment it is reduced, retraces submitted at once)
+    gives the sites and widenings of window.trace_windows over
+    cor_trace_batch, including windows placed wrong on purpose (edge hits)."""
+    import window
+    p = ct.internal_setup("igrf14", [2020, 1, 1, 1, 0, 0, 0])
+    jobs = _jobs([(a, o) for a in (-70.0, -30.0, 0.0, 30.0, 70.0) for o in (0.0, 180.0)], rig=0.01, rk=20.0,
+                 dele=0.01)
+    full = ctx.trace_batch(jobs, p)
+    n = full.offsets[1] - full.offsets[0]
+    i_lo, i_hi = np.zeros(len(jobs), np.int64), np.zeros(len(jobs), np.int64)
+    for j in range(len(jobs)):
+        st = full.status[full.offsets[j]:full.offsets[j + 1]]
+        a = np.nonzero(st == ct.TRAJ_ALLOWED)[0]
+        f = np.nonzero(st != ct.TRAJ_ALLOWED)[0]
+        i_lo[j] = max(0, (a.min() if len(a) else 0) - 5)
+        i_hi[j] = min(n - 1, (f.max() if len(f) else n - 1) + 5)
+    i_lo[0], i_hi[0] = i_hi[0] + 10, min(n - 1, i_hi[0] + 40)     # above the penumbra: first rigidity allowed
+    i_lo[1], i_hi[1] = max(0, i_lo[1] - 60), max(0, i_lo[1] - 20)  # below it: last rigidity forbidden
+    want_sites, want_redone, _, _ = window.trace_windows(ctx, jobs, p, ct.model_set(ct.INTERNAL_SH), i_lo, i_hi)
+    with ct.Stream(ctx, ct.model_set(ct.INTERNAL_SH), slots=4, scan_events=1, idle_limit_s=30.0) as s:
+        (sites, redone, traced, _), = window.trace_windows_stream(s, [(jobs, p, i_lo, i_hi)])
+    assert np.array_equal(sites.view(np.uint8), want_sites.view(np.uint8))
+    assert np.array_equal(redone, want_redone) and redone[0] and redone[1]
+    assert np.array_equal(sites.view(np.uint8), full.sites.view(np.uint8))
