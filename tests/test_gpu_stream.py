@@ -249,4 +249,3 @@ def test_window_scan_reacts_to_scan_events(ctx):
         (sites, redone, traced, _), = window.trace_windows_stream(s, [(jobs, p, i_lo, i_hi)])
     assert np.array_equal(sites.view(np.uint8), want_sites.view(np.uint8))
     assert np.array_equal(redone, want_redone) and redone[0] and redone[1]
-    assert np.array_equal(sites.view(np.uint8), full.sites.view(np.uint8))
