@@ -643,6 +643,8 @@ def resume(log_path: str, reqs: list[Request]) -> tuple[list[Request], list[Requ
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--rate", type=float, default=1.0, help="requests per second")
+    ap.add_argument("--sweep", default=None,
+                    help="comma-separated rates: run the same seeded stream at each (one JSON line per rate)")
     ap.add_argument("--requests", type=int, default=20)
     ap.add_argument("--seed", type=int, default=7)
     ap.add_argument("--server", default="stream", choices=["stream", "slots"],
@@ -658,12 +660,22 @@ def main():
     ap.add_argument("--resume", action="store_true",
                     help="with --log: take the results the log holds and run only what it shows unfinished")
     args = ap.parse_args()
+    if args.sweep:
+        rates = [float(v) for v in args.sweep.split(",")]
+        for rate in rates:
+            args.rate = rate
+            serve_once(args)
+        return
+    serve_once(args)
+
+
+def serve_once(args):
     ext = ct.EXTERNAL_TS05 if args.external == "ts05" else ct.EXTERNAL_T96
     reqs = poisson_stream(args.seed, args.rate, args.requests, ext, args.max_box_sites)
     restored = []
     if args.resume:
         if not args.log:
-            ap.error("--resume needs --log")
+            raise SystemExit("--resume needs --log")
         restored, reqs = resume(args.log, reqs)
     wms = [window.WindowModel(f) for f in args.window]
     log = RequestLog(args.log) if args.log else None
