@@ -1,6 +1,7 @@
 """Autotuner of the scan's launch settings (no counterpart in the reference).
 
     python cor-model_gb300/autotune.py [--stride K] [--batches B] [--out FILE]
+    python cor-model_gb300/autotune.py --stream [--stride K] [--out FILE]
 
 Times a sample of the IGRF-14 + T96 5-degree-grid workload (every k-th site,
 the full 2,000-rigidity scans, cut into interleaved batches that stream
@@ -15,8 +16,16 @@ fastest to FILE (JSON), which bench.py and serve.py read:
     batch's bulk;
   * the work-queue order (cor_ctx_set_queue_order): lowest rigidities of all
     scans first, or consecutive rigidities of one scan to neighbouring lanes.
+With --stream it tunes the persistent scan stream instead (cor_stream_*, the
+path bench.py and serve.py run): the same sample cut into more or fewer
+segments, published together to one launch, with the rigidity-major queue
+order on or off; the time is the launch's (CUDA events on its stream), and
+the choice goes to the "stream" entry of FILE.
 Results do not depend on any setting (checked: every candidate's P(S), P(C),
-P(M) must equal the first's, bit for bit); only the time does.
+P(M) must equal the first's, bit for bit); only the time does.  The block
+size is not a knob: the external-field kernels use 255 registers a thread,
+so one 256-thread block fills an SM's register file (128-thread blocks would
+give the same 8 warps per SM), and each lane carries one trajectory.
 """
 from __future__ import annotations
 
@@ -122,14 +131,82 @@ def tune(ctxs, batches, p, models, cands, log=None):
     return {k: best[k] for k in KNOBS}, results
 
 
+STREAM_KNOBS = ("segments", "rigidity_major")
+
+
+def stream_candidates():
+    """Segments per launch (the sample cut into 4, 16 or 64 interleaved
+    segments) x rigidity-major order on or off."""
+    return [{"segments": n, "rigidity_major": o} for n in (4, 16, 64) for o in (1, 0)]
+
+
+def tune_stream(run_launch, cands, log=None):
+    """run_launch(candidate) -> (launch ms, sites in sample order).  Returns
+    (the fastest candidate whose results equal the first's bit for bit, every
+    measurement)."""
+    ref = None
+    results = []
+    for c in cands:
+        ms, sites = run_launch(c)
+        if ref is None:
+            ref = sites
+        same = bool(np.array_equal(sites.view(np.uint8), ref.view(np.uint8)))
+        results.append({**c, "launch_ms": ms, "site_cutoffs_per_s": len(sites) / (ms / 1e3), "same_results": same})
+        if log:
+            log(results[-1])
+    best = min((r for r in results if r["same_results"]), key=lambda r: r["launch_ms"])
+    return {k: best[k] for k in STREAM_KNOBS}, results
+
+
+def stream_launcher(ctx, grid_jobs, p, models):
+    """A run_launch for tune_stream on the GPU: the sample's jobs cut into the
+    candidate's interleaved segments, all submitted, one launch drained."""
+    def run_launch(c):
+        ctx.set_queue_order(bool(c["rigidity_major"]))
+        parts = [grid_jobs[k::c["segments"]] for k in range(c["segments"])]
+        st = ct.Stream(ctx, models, slots=max(8, c["segments"]), max_jobs=max(len(x) for x in parts),
+                       max_trajectories=max(len(x) for x in parts) * 2000, max_params=1, idle_limit_s=300.0)
+        try:
+            tickets = [st.submit(x, p, want_status=False) for x in parts]
+            got = [st.wait(t, -1)[0] for t in tickets]
+            ms = st.drain()
+        finally:
+            st.close()
+        sites = np.zeros(len(grid_jobs), ct.SITE_DTYPE)
+        for k, g in enumerate(got):
+            sites[k::c["segments"]] = g.sites
+        return ms, sites
+    return run_launch
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--stride", type=int, default=24, help="every stride-th site of the grid (default: 111 sites)")
     ap.add_argument("--batches", type=int, default=8)
     ap.add_argument("--out", default=DEFAULT_OUT)
+    ap.add_argument("--stream", action="store_true", help="tune the persistent scan stream's settings")
     args = ap.parse_args()
     p = ct.internal_setup("igrf14", TIME7, parmod=PARMOD)
     models = ct.model_set(ct.INTERNAL_SH, ct.EXTERNAL_T96)
+    if args.stream:
+        grid = [(float(la), float(lo)) for la in range(-90, 91, 5) for lo in range(0, 360, 5)][::args.stride]
+        jobs = np.concatenate([ct.make_job(la, lo, rig=0.01, rk=20.0, dele=0.01) for la, lo in grid])
+        ctx = ct.Context(0)
+        run_launch = stream_launcher(ctx, jobs, p, models)
+        run_launch({"segments": 4, "rigidity_major": 1})            # load the kernels, warm the clocks
+        best, results = tune_stream(run_launch, stream_candidates(), log=lambda r: print(json.dumps(r), flush=True))
+        ctx.close()
+        prev = {}
+        if os.path.exists(args.out):
+            with open(args.out) as f:
+                prev = json.load(f)
+        prev["stream"] = {**best, "sample": f"{len(jobs)} sites of the 5-deg grid (every {args.stride}th) x 2000 "
+                                            f"rigidities, IGRF-14 + T96, one stream launch per candidate",
+                          "measurements": results}
+        with open(args.out, "w") as f:
+            json.dump(prev, f, indent=1)
+        print(json.dumps(best))
+        return
     batches = sample_batches(args.batches, args.stride)
     n_sites = sum(len(b) for b in batches)
     ctxs = [ct.Context(0) for _ in range(4)]

@@ -81,3 +81,21 @@ def test_committed_tuning_loads():
     t = autotune.load_tuning()
     assert t is not None and set(t) == set(autotune.KNOBS)
     assert t["inflight"] >= 1 and 0 <= t["park_below"] <= 32 and t["max_generations"] >= 1
+
+
+def test_tune_stream_picks_the_fastest_with_the_same_results():
+    """The stream autotuner's choice: the fastest candidate whose sites equal
+    the first candidate's; a faster one with different results is never
+    chosen."""
+    sites = np.zeros(6, ct.SITE_DTYPE)
+    sites["r_cutoff"] = np.arange(6) * 0.5
+    times = {(4, 1): 30.0, (4, 0): 31.0, (16, 1): 20.0, (16, 0): 25.0, (64, 1): 10.0, (64, 0): 40.0}
+
+    def run_launch(c):
+        out = sites.copy()
+        if (c["segments"], c["rigidity_major"]) == (64, 1):
+            out["r_cutoff"][2] += 0.01                   # fastest, but wrong
+        return times[(c["segments"], c["rigidity_major"])], out
+    best, results = autotune.tune_stream(run_launch, autotune.stream_candidates())
+    assert best == {"segments": 16, "rigidity_major": 1}
+    assert len(results) == 6 and sum(not r["same_results"] for r in results) == 1
