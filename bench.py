@@ -312,7 +312,7 @@ def measure_window(args, ctx, bufs, plain, p, plain_e2e: float) -> dict:
     s = ct.Stream(ctx, models(), scan_events=1, **stream_settings(len(jobs), len(jobs) * N_RIG))
     wm.windows(feats[:8])                            # load the network's kernels before timing
     t0 = time.perf_counter()
-    i_lo, i_hi = wm.windows(feats)                   # no stream kernel runs now: the network has the SMs
+    i_lo, i_hi = wm.windows(feats, k=args.window_k)  # no stream kernel runs now: the network has the SMs
     (sites, fb, traced, _), = window.trace_windows_stream(s, [(jobs, p, i_lo, i_hi)])
     launch_ms = s.drain()
     wall = time.perf_counter() - t0
@@ -327,8 +327,8 @@ def measure_window(args, ctx, bufs, plain, p, plain_e2e: float) -> dict:
             "sites": n_sites, "agree_frac_dRc_le_0.01GV": int(np.sum(d <= 0.01 + 1e-9)) / n_sites,
             "max_abs_dRc_GV": float(d.max()), "widened_frac": int(fb.sum()) / n_sites,
             "trajectories_frac_of_full_scan": traced / full_traj, "stream_launch_ms": launch_ms,
-            "model": json.loads(wm.info) if wm.info.startswith("{") else wm.info,
-            "how": "predicted window +-3 sigma on the 0.01 GV grid, widened on the hit side on an edge hit (full scan "
+            "model": json.loads(wm.info) if wm.info.startswith("{") else wm.info, "k_sigma": args.window_k,
+            "how": f"predicted window +-{args.window_k:g} sigma on the 0.01 GV grid, widened on the hit side on an edge hit (full scan "
                    "after 3 widenings); the timed steps' windows as one segment of a scan stream (ascending "
                    "rigidity), each scan's result taken as soon as it is reduced so that a retrace starts at once; "
                    "host buffers, network inference on the tensor cores inside the timed region"}
@@ -583,6 +583,8 @@ def main():
                     help="the grid is split into this many interleaved batches; one step scans one batch")
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--window-k", type=float, default=3.0,
+                    help="half-width of the learned window in held-out sigmas of the network's band")
     ap.add_argument("--window", default=WINDOW_FILE, help="trained window model for the learned-window line "
                     "(train_window.py output); skipped when the file is absent")
     ap.add_argument("--profile-case", action="store_true",
