@@ -59,6 +59,8 @@ def tuning() -> dict:
         with open(TUNING_FILE) as f:
             t = json.load(f)
         out = {k: t[k] for k in ("inflight", "park_below", "max_generations", "min_park")}
+        if "stream" in t:
+            out["stream_queue_order"] = t["stream"]["queue_order"]
         return out | {"rigidity_major": t.get("rigidity_major", 1), "source": "autotune"}
     return {"inflight": 3, "park_below": 16, "max_generations": 48, "min_park": 256, "rigidity_major": 1,
             "source": "defaults"}
@@ -378,7 +380,7 @@ def run_ours(args, rank: int, world: int, dist) -> dict | None:
                                                                                    args.batches))
              for k in range(n_steps)]
     ctx = ct.Context(dev)
-    ctx.set_queue_order(bool(tune["rigidity_major"]))
+    ctx.set_queue_order(int(tune.get("stream_queue_order", tune["rigidity_major"])))
     peak = C.c_double(0.0)
     ctx.lib.cor_probe_fp64_peak(ctx.h, C.byref(peak))
     fn_flops = np.zeros(11)

@@ -18,8 +18,8 @@ fastest to FILE (JSON), which bench.py and serve.py read:
     scans first, or consecutive rigidities of one scan to neighbouring lanes.
 With --stream it tunes the persistent scan stream instead (cor_stream_*, the
 path bench.py and serve.py run): the same sample cut into more or fewer
-segments, published together to one launch, with the rigidity-major queue
-order on or off; the time is the launch's (CUDA events on its stream), and
+segments, published together to one launch, under each queue order
+(cor_ctx_set_queue_order); the time is the launch's (CUDA events on its stream), and
 the choice goes to the "stream" entry of FILE.
 Results do not depend on any setting (checked: every candidate's P(S), P(C),
 P(M) must equal the first's, bit for bit); only the time does.  The block
@@ -131,13 +131,14 @@ def tune(ctxs, batches, p, models, cands, log=None):
     return {k: best[k] for k in KNOBS}, results
 
 
-STREAM_KNOBS = ("segments", "rigidity_major")
+STREAM_KNOBS = ("segments", "queue_order")
 
 
 def stream_candidates():
-    """Segments per launch (the sample cut into 4, 16 or 64 interleaved
-    segments) x rigidity-major order on or off."""
-    return [{"segments": n, "rigidity_major": o} for n in (4, 16, 64) for o in (1, 0)]
+    """The sample as 16 interleaved segments under each queue order (0 scan
+    by scan, 1 rigidity-major, 2 warp-wide chunks of one scan in ascending
+    rigidity), and as 4 and 64 segments under the chunked order."""
+    return [{"segments": n, "queue_order": o} for n, o in ((16, 0), (16, 1), (16, 2), (4, 2), (64, 2))]
 
 
 def tune_stream(run_launch, cands, log=None):
@@ -162,7 +163,7 @@ def stream_launcher(ctx, grid_jobs, p, models):
     """A run_launch for tune_stream on the GPU: the sample's jobs cut into the
     candidate's interleaved segments, all submitted, one launch drained."""
     def run_launch(c):
-        ctx.set_queue_order(bool(c["rigidity_major"]))
+        ctx.set_queue_order(int(c["queue_order"]))
         parts = [grid_jobs[k::c["segments"]] for k in range(c["segments"])]
         st = ct.Stream(ctx, models, slots=max(8, c["segments"]), max_jobs=max(len(x) for x in parts),
                        max_trajectories=max(len(x) for x in parts) * 2000, max_params=1, idle_limit_s=300.0)
@@ -193,7 +194,7 @@ def main():
         jobs = np.concatenate([ct.make_job(la, lo, rig=0.01, rk=20.0, dele=0.01) for la, lo in grid])
         ctx = ct.Context(0)
         run_launch = stream_launcher(ctx, jobs, p, models)
-        run_launch({"segments": 4, "rigidity_major": 1})            # load the kernels, warm the clocks
+        run_launch({"segments": 4, "queue_order": 1})               # load the kernels, warm the clocks
         best, results = tune_stream(run_launch, stream_candidates(), log=lambda r: print(json.dumps(r), flush=True))
         ctx.close()
         prev = {}

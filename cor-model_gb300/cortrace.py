@@ -20,6 +20,7 @@ COR_OK = 0
 ERRORS = {-1: "invalid", -2: "nomem", -3: "cuda", -4: "watchdog", -5: "nodev", -6: "unsupported", -7: "range",
           -8: "busy"}
 COR_PENDING = 1
+ERR_BUSY = -8
 
 INTERNAL_NONE, INTERNAL_SH = 0, 1
 EXTERNAL_NONE, EXTERNAL_T96, EXTERNAL_TS05 = 0, 1, 2
@@ -298,9 +299,12 @@ class Context:
         n = self.lib.cor_ctx_generation_log(self.h, 1024, live.ctypes.data, ms.ctypes.data)
         return [(int(live[k]), float(ms[k])) for k in range(max(0, n))]
 
-    def set_queue_order(self, rigidity_major: bool = True) -> None:
-        """cor_ctx_set_queue_order: lowest rigidities first (True) or scan by scan."""
-        self._check(self.lib.cor_ctx_set_queue_order(self.h, 1 if rigidity_major else 0), "cor_ctx_set_queue_order")
+    def set_queue_order(self, rigidity_major=True) -> None:
+        """cor_ctx_set_queue_order: lowest rigidities first (True or 1), scan
+        by scan (False or 0), or warp-wide chunks of one scan in ascending
+        rigidity (2, streams)."""
+        mode = int(rigidity_major) if not isinstance(rigidity_major, bool) else (1 if rigidity_major else 0)
+        self._check(self.lib.cor_ctx_set_queue_order(self.h, mode), "cor_ctx_set_queue_order")
 
     def upload_crustal(self, g: np.ndarray, h: np.ndarray, nmax: int) -> None:
         """cor_upload_crustal: packed lower-triangle G, H (index n(n+1)/2 + m)."""

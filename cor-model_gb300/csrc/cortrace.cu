@@ -444,7 +444,7 @@ extern "C" int32_t cor_ctx_generation_log(const cor_ctx* ctx, int32_t cap, uint6
 
 extern "C" int cor_ctx_set_queue_order(cor_ctx* ctx, int32_t rigidity_major) {
     if (!ctx) return COR_ERR_INVALID;
-    if (rigidity_major != 0 && rigidity_major != 1) return fail(ctx, COR_ERR_INVALID, "queue order must be 0 or 1");
+    if (rigidity_major < 0 || rigidity_major > 2) return fail(ctx, COR_ERR_INVALID, "queue order must be 0, 1 or 2");
     ctx->rig_major = rigidity_major;
     return COR_OK;
 }
@@ -1322,16 +1322,30 @@ static int stream_publish(cor_stream* s, StreamSlot& sl, int64_t seq, uint64_t n
     return COR_OK;
 }
 
-// The batch's trajectories (offsets space) sorted by rigidity, lowest first;
+// Warp-wide chunk of the queue orders that keep neighbouring rigidities of a
+// scan together (cor_ctx_set_queue_order mode 2).
+constexpr uint32_t kQueueChunk = 32;
+
+// The batch's trajectories (offsets space) in ascending rigidity, lowest
+// first, in chunks of `chunk` consecutive trajectories of one scan (the
+// chunk's key is its first rigidity; chunk 1 = trajectory by trajectory);
 // ties keep the batch order.
-static void rigidity_order(const cor_scan_job* jobs, int32_t n_jobs, const uint64_t* off, uint32_t* order) {
-    const uint64_t n = off[n_jobs];
-    std::vector<double> rig(n);
+static void rigidity_order(const cor_scan_job* jobs, int32_t n_jobs, const uint64_t* off, uint32_t chunk,
+                           uint32_t* order) {
+    std::vector<std::pair<double, uint64_t>> keys;   // (first rigidity, first trajectory) per chunk
     for (int32_t j = 0; j < n_jobs; j++)
-        for (uint64_t k = 0; k < off[j + 1] - off[j]; k++)
-            rig[off[j] + k] = jobs[j].rig + (int)(k + (uint64_t)jobs[j].i_first) * jobs[j].del;
-    for (uint64_t t = 0; t < n; t++) order[t] = (uint32_t)t;
-    std::stable_sort(order, order + n, [&](uint32_t a, uint32_t b) { return rig[a] < rig[b]; });
+        for (uint64_t k = 0; k < off[j + 1] - off[j]; k += chunk)
+            keys.emplace_back(jobs[j].rig + (int)(k + (uint64_t)jobs[j].i_first) * jobs[j].del, off[j] + k);
+    std::stable_sort(keys.begin(), keys.end(),
+                     [](const std::pair<double, uint64_t>& a, const std::pair<double, uint64_t>& b) {
+                         return a.first < b.first;
+                     });
+    uint64_t o = 0;
+    for (const auto& kv : keys) {
+        const int32_t j = (int32_t)(std::upper_bound(off, off + n_jobs + 1, kv.second) - off) - 1;
+        const uint64_t end = std::min<uint64_t>(kv.second + chunk, off[j + 1]);
+        for (uint64_t t = kv.second; t < end; t++) order[o++] = (uint32_t)t;
+    }
 }
 
 static bool offsets_uniform(const uint64_t* off, int32_t n_jobs) {
@@ -1420,13 +1434,14 @@ extern "C" int cor_stream_submit(cor_stream* s, const cor_scan_job* jobs, int32_
     g.seq = (unsigned long long)seq;
     g.n_jobs = n_jobs;
     g.n_rig = (offsets_uniform(sl.h_off, n_jobs) && s->ctx->rig_major) ? (uint32_t)(sl.h_off[1] - sl.h_off[0]) : 0u;
+    g.chunk = (g.n_rig && s->ctx->rig_major == 2) ? kQueueChunk : 0u;
     g.order = nullptr;
     g.events = s->events_d ? s->events_d + (size_t)(seq % s->cfg.slots) * (size_t)s->cfg.max_jobs : nullptr;
     if (!g.n_rig && s->ctx->rig_major && n_jobs > 1) {
         // scans of different lengths: hand out all their trajectories in
         // ascending rigidity, as the rigidity-major order does for a uniform
         // grid (the lowest rigidities are the longest trajectories)
-        rigidity_order(jobs, n_jobs, sl.h_off, sl.h_order);
+        rigidity_order(jobs, n_jobs, sl.h_off, s->ctx->rig_major == 2 ? kQueueChunk : 1u, sl.h_order);
         CUDA_TRY(ctx, cudaMemcpyAsync(sl.order, sl.h_order, sizeof(uint32_t) * n_traj, cudaMemcpyHostToDevice, s->cs));
         g.order = sl.order;
     }
@@ -1496,6 +1511,7 @@ extern "C" int cor_stream_submit_device(cor_stream* s, const cor_scan_job* jobs_
     g.seq = (unsigned long long)seq;
     g.n_jobs = n_jobs;
     g.n_rig = (offsets_uniform(offsets_host, n_jobs) && s->ctx->rig_major) ? (uint32_t)offsets_host[1] : 0u;
+    g.chunk = (g.n_rig && s->ctx->rig_major == 2) ? kQueueChunk : 0u;
     g.order = nullptr;
     g.events = nullptr;
     if ((rc = stream_publish(s, sl, seq, n_traj)) != COR_OK) return rc;

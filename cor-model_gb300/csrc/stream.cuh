@@ -45,7 +45,10 @@ struct StreamSeg {
     unsigned long long n_traj;
     unsigned long long seq;
     int32_t n_jobs;
-    uint32_t n_rig;                // > 0: rigidity-major order (the host checked that every scan has n_rig)
+    uint32_t n_rig;                // > 0: every scan has n_rig trajectories (checked by the host): rigidity-major
+                                   // order, or with chunk > 0 chunks of `chunk` consecutive rigidities of one
+                                   // scan, the chunks in ascending rigidity
+    uint32_t chunk;
     const uint32_t* order;         // queue position -> trajectory (offsets space), or null; overrides n_rig
     cor_scan_event* events;        // device address of mapped host records, one per scan, or null
 };
@@ -308,6 +311,20 @@ __global__ void __launch_bounds__(kTraceThreads, 1) stream_kernel(const StreamAr
                     tl = __ldcg(order + tl);
                     j = find_job_cg(off, n_jobs, tl);
                     i = tl - __ldcg(reinterpret_cast<const unsigned long long*>(off) + j);
+                } else if (n_rig && __ldcg(&sg->chunk)) {
+                    // warp-wide chunks: the lanes that take consecutive queue
+                    // positions trace neighbouring rigidities of one scan
+                    const uint64_t W = __ldcg(&sg->chunk), J = (uint64_t)n_jobs, R = n_rig;
+                    const uint64_t full = R / W, tf = full * W * J;
+                    if (tl < tf) {
+                        const uint64_t c = tl / (W * J), rem = tl - c * W * J;
+                        j = (int)(rem / W);
+                        i = c * W + rem % W;
+                    } else {
+                        const uint64_t wl = R - full * W, rem = tl - tf;
+                        j = (int)(rem / wl);
+                        i = full * W + rem % wl;
+                    }
                 } else if (n_rig) {
                     i = tl / (uint64_t)n_jobs;
                     j = (int)(tl - i * (uint64_t)n_jobs);

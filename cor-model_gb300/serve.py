@@ -532,7 +532,7 @@ class StreamServer:
                         self.waiting.remove(r)
                         self.in_flight += b
                         admitted.append(r)
-                    done_all = self.closed and not self.waiting and not pending and \
+                    done_all = self.closed and not self.waiting and not admitted and not pending and \
                         not any(inflight.values())
                 if done_all:
                     return
@@ -546,7 +546,13 @@ class StreamServer:
                     if len(inflight[r.external]) >= st.config.slots:
                         pending.rotate(-1)
                         continue
-                    t = st.submit(jobs, params)
+                    try:
+                        t = st.submit(jobs, params)
+                    except ct.CorError as e:
+                        if e.code != ct.ERR_BUSY:
+                            raise
+                        pending.rotate(-1)       # the ring slot it needs is still held: later
+                        continue
                     pending.popleft()
                     inflight[r.external].append((t, r, params, state))
                     r._open += 1

@@ -331,8 +331,16 @@ def trace_windows_stream(stream, items, widen: int = 3, poll_s: float = 0.002):
             if attempt == widen + 1:                   # last resort: the whole grid
                 S["lo"][idx] = 0
                 S["hi"][idx] = S["n_grid"][idx] - 1
-            t = stream.submit(window_jobs(S["jobs"][idx], S["lo"][idx], S["hi"][idx]), S["params"],
-                              want_status=not events)
+            try:
+                t = stream.submit(window_jobs(S["jobs"][idx], S["lo"][idx], S["hi"][idx]), S["params"],
+                                  want_status=not events)
+            except ct.CorError as e:
+                if e.code != ct.ERR_BUSY:
+                    raise
+                # the ring slot this segment needs still holds an older,
+                # unfinished one: submit after it is collected
+                todo.appendleft((k, idx, attempt))
+                break
             inflight.append({"t": t, "k": k, "idx": idx, "attempt": attempt, "seen": np.zeros(len(idx), bool)})
         progressed = False
         again = {}
@@ -367,7 +375,7 @@ def trace_windows_stream(stream, items, widen: int = 3, poll_s: float = 0.002):
             S["steps"] += int(res.counters["accepted_steps"])
         for (k, attempt), js in again.items():
             todo.append((k, np.array(js, np.int64), attempt))
-        if not progressed and not todo:
+        if not progressed:
             time.sleep(poll_s)
     return [(S["sites"], S["redone"], S["traced"], S["steps"]) for S in state]
 

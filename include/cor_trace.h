@@ -241,13 +241,17 @@ int cor_ctx_set_regroup(cor_ctx *ctx, int32_t park_below, int32_t max_generation
  * number of generations (negative COR_ERR_* for a null context). */
 int32_t cor_ctx_generation_log(const cor_ctx *ctx, int32_t cap, uint64_t *live, double *ms);
 
-/* Work-queue order of cor_trace_batch on this context when every job has the
- * same number of rigidities (no counterpart in the reference; an autotuner's
- * knob): 1 (default) hands out the lowest rigidity of every scan first
- * (longest trajectories first); 0 hands consecutive rigidities of one scan
- * to neighbouring lanes, whose paths start out alike.  The device path takes
- * the order from its flags (COR_FLAG_UNIFORM_GRID).  Results do not depend
- * on it. */
+/* Work-queue order on this context (no counterpart in the reference; an
+ * autotuner's knob).  1 (default): the lowest rigidity of every scan first
+ * (longest trajectories first); 0: scan by scan, consecutive rigidities of one
+ * scan to neighbouring lanes, whose paths start out alike; 2 (streams only;
+ * the batch path takes it as 1): chunks of 32 consecutive rigidities of one
+ * scan, one warp's worth, the chunks in ascending rigidity -- neighbouring
+ * lanes alike and the longest trajectories early.  cor_trace_batch uses it
+ * when every job has the same number of rigidities; the batch device path
+ * takes the order from its flags (COR_FLAG_UNIFORM_GRID); stream segments of
+ * unequal scans (windows) are handed out in ascending rigidity by trajectory
+ * (1) or by chunk (2).  Results do not depend on it. */
 int cor_ctx_set_queue_order(cor_ctx *ctx, int32_t rigidity_major);
 
 /* Replaces the crustal model's coefficient table on this context: G and H as

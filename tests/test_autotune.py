@@ -89,13 +89,15 @@ def test_tune_stream_picks_the_fastest_with_the_same_results():
     chosen."""
     sites = np.zeros(6, ct.SITE_DTYPE)
     sites["r_cutoff"] = np.arange(6) * 0.5
-    times = {(4, 1): 30.0, (4, 0): 31.0, (16, 1): 20.0, (16, 0): 25.0, (64, 1): 10.0, (64, 0): 40.0}
+    cands = autotune.stream_candidates()
+    times = {(16, 0): 30.0, (16, 1): 31.0, (16, 2): 20.0, (4, 2): 25.0, (64, 2): 10.0}
+    assert set(times) == {(c["segments"], c["queue_order"]) for c in cands}
 
     def run_launch(c):
         out = sites.copy()
-        if (c["segments"], c["rigidity_major"]) == (64, 1):
+        if (c["segments"], c["queue_order"]) == (64, 2):
             out["r_cutoff"][2] += 0.01                   # fastest, but wrong
-        return times[(c["segments"], c["rigidity_major"])], out
-    best, results = autotune.tune_stream(run_launch, autotune.stream_candidates())
-    assert best == {"segments": 16, "rigidity_major": 1}
-    assert len(results) == 6 and sum(not r["same_results"] for r in results) == 1
+        return times[(c["segments"], c["queue_order"])], out
+    best, results = autotune.tune_stream(run_launch, cands)
+    assert best == {"segments": 16, "queue_order": 2}
+    assert len(results) == len(cands) and sum(not r["same_results"] for r in results) == 1

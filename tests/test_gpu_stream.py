@@ -249,3 +249,21 @@ def test_window_scan_reacts_to_scan_events(ctx):
         (sites, redone, traced, _), = window.trace_windows_stream(s, [(jobs, p, i_lo, i_hi)])
     assert np.array_equal(sites.view(np.uint8), want_sites.view(np.uint8))
     assert np.array_equal(redone, want_redone) and redone[0] and redone[1]
+
+
+@pytest.mark.parametrize("order", [0, 1, 2])
+def test_stream_queue_orders_give_the_same_results(ctx, order):
+    """Scan by scan, rigidity-major, and warp-wide chunks in ascending
+    rigidity (uniform grids and windows alike) move time only: every result
+    equals cor_trace_batch's bit for bit (IGRF-14)."""
+    p = ct.internal_setup("igrf14", [2020, 1, 1, 1, 0, 0, 0])
+    batches = _batches()
+    c2 = ct.Context(0)
+    try:
+        c2.set_queue_order(order)
+        with ct.Stream(c2, ct.model_set(ct.INTERNAL_SH), slots=4, idle_limit_s=30.0) as s:
+            got = [s.wait(s.submit(b, p), WAIT_MS) for b in batches]
+    finally:
+        c2.close()
+    for b, g in zip(batches, got):
+        _same(g[0], ctx.trace_batch(b, p), records=False)
