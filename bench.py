@@ -498,13 +498,16 @@ def run_profile_case(args) -> dict:
     dev = int(os.environ.get("LOCAL_RANK", "0"))
     torch.cuda.set_device(dev)
     p = params()
-    sites = grid_sites()[::len(grid_sites()) // PROFILE_SITES][:PROFILE_SITES]
+    n_sites, step_limit = args.profile_sites, args.profile_step_limit
+    sites = grid_sites()[::len(grid_sites()) // n_sites][:n_sites]
     jobs = make_jobs(sites)
     ctx = ct.Context(dev)
+    tune = tuning()
+    ctx.set_queue_order(int(tune.get("stream_queue_order", tune["rigidity_major"])))
     ms = []
     if args.profile_stream:
         parts = [jobs[k::4] for k in range(4)]
-        s = ct.Stream(ctx, models(), step_limit=PROFILE_STEP_LIMIT, launch_on_drain=1,
+        s = ct.Stream(ctx, models(), step_limit=step_limit, launch_on_drain=1,
                       **stream_settings(len(parts[0]), len(parts[0]) * N_RIG))
         base = s.upload_params(p)
         bufs = device_segments(torch, dev, [(j, None) for j in parts], base)
@@ -528,7 +531,7 @@ def run_profile_case(args) -> dict:
             e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
             e0.record(st)
             rc = ctx.lib.cor_trace_batch_device(ctx.h, dj.data_ptr(), dt.data_ptr(), len(jobs), do.data_ptr(), n,
-                                                models(), PROFILE_STEP_LIMIT, 0.01, ct.DEF_HM0_P,
+                                                models(), step_limit, 0.01, ct.DEF_HM0_P,
                                                 sites_d.data_ptr(), status.data_ptr(), None, cnt.data_ptr(),
                                                 ct.FLAG_UNIFORM_GRID, C.c_void_p(st.cuda_stream))
             ctx._check(rc, "cor_trace_batch_device")
@@ -538,7 +541,7 @@ def run_profile_case(args) -> dict:
         v = cnt.cpu().numpy()
         c = dict(zip(("accepted_steps", "trials", "trajectories", "watchdog", "kernel_launches"), v.tolist()))
     ctx.close()
-    return {"profile_case": f"{len(sites)} sites x {N_RIG} rigidities, step limit {PROFILE_STEP_LIMIT}",
+    return {"profile_case": f"{len(sites)} sites x {N_RIG} rigidities, step limit {step_limit}",
             "path": "stream" if args.profile_stream else "batch",
             "trajectories": int(c["trajectories"]), "accepted_steps": int(c["accepted_steps"]),
             "trials": int(c["trials"]), "call_ms": ms}
@@ -591,6 +594,8 @@ def main():
                     "(train_window.py output); skipped when the file is absent")
     ap.add_argument("--profile-case", action="store_true",
                     help="run only the small profiling case of the scan kernel (prints its own JSON, not a bench line)")
+    ap.add_argument("--profile-sites", type=int, default=PROFILE_SITES)
+    ap.add_argument("--profile-step-limit", type=int, default=PROFILE_STEP_LIMIT)
     ap.add_argument("--profile-stream", action="store_true",
                     help="with --profile-case: through a scan stream launched with everything staged")
     args = ap.parse_args()
