@@ -547,6 +547,39 @@ def run_profile_case(args) -> dict:
             "trials": int(c["trials"]), "call_ms": ms}
 
 
+def run_chaos_case(args) -> dict:
+    """The CHAOS-7.16 crustal field (degree 185, the warp-cooperative sum) with
+    IGRF-14 through cor_field_batch on seeded points 1-3 R_E, timed end to end
+    (host buffers), against the oracle's restatement of the reference's
+    chaos_geo on a few of the same points on one host core.  Not a bench
+    line; it measures the high-degree field on its own."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import pyoracle
+    rng = np.random.default_rng(185)
+    n = args.chaos_points
+    u = rng.normal(size=(n, 3))
+    u /= np.linalg.norm(u, axis=1)[:, None]
+    pts = u * (ct.DEF_RE * rng.uniform(1.0, 3.0, n))[:, None]
+    p = ct.internal_setup("igrf14", [2020, 1, 1, 1, 0, 0, 0])
+    m = ct.model_set(ct.INTERNAL_SH, ct.EXTERNAL_NONE, ct.CRUSTAL_CHAOS)
+    ctx = ct.Context(0)
+    ctx.field_batch(pts[:1024], p, models=m)                # uploads the table, loads the kernel
+    best = 1e30
+    for _ in range(3):
+        t = time.perf_counter()
+        got = ctx.field_batch(pts, p, models=m)
+        best = min(best, time.perf_counter() - t)
+    ctx.close()
+    k = 64
+    t = time.perf_counter()
+    want = pyoracle.calculate_field(pts[:k], p, models=m)
+    cpu = (time.perf_counter() - t) / k
+    rel = np.linalg.norm(got[:k] - want, axis=1) / np.linalg.norm(want, axis=1)
+    return {"chaos_case": f"IGRF-14 + CHAOS-7.16 (n <= 185) at {n} seeded points, 1-3 R_E",
+            "gpu_us_per_point": best / n * 1e6, "gpu_points_per_s": n / best,
+            "cpu_oracle_us_per_point_one_core": cpu * 1e6, "max_rel_diff_vs_oracle": float(rel.max())}
+
+
 def run_reference(args, rank: int) -> dict | None:
     """CPU reference arm: the oracle port on all host threads, one bounded
     sample per step (CPU_SAMPLE_SITES sites of that step's batch)."""
@@ -594,6 +627,9 @@ def main():
                     "(train_window.py output); skipped when the file is absent")
     ap.add_argument("--profile-case", action="store_true",
                     help="run only the small profiling case of the scan kernel (prints its own JSON, not a bench line)")
+    ap.add_argument("--chaos-case", action="store_true",
+                    help="time the CHAOS-7.16 crustal field alone (prints its own JSON, not a bench line)")
+    ap.add_argument("--chaos-points", type=int, default=1 << 20)
     ap.add_argument("--profile-sites", type=int, default=PROFILE_SITES)
     ap.add_argument("--profile-step-limit", type=int, default=PROFILE_STEP_LIMIT)
     ap.add_argument("--profile-stream", action="store_true",
@@ -607,7 +643,9 @@ def main():
         backend = "gloo" if args.impl == "reference" else "nccl"
         tdist.init_process_group(backend)
         dist = tdist
-    if args.profile_case:
+    if args.chaos_case:
+        out = run_chaos_case(args) if rank == 0 else None
+    elif args.profile_case:
         out = run_profile_case(args) if rank == 0 else None
     elif args.impl == "reference":
         out = run_reference(args, rank)
