@@ -46,10 +46,10 @@ N_RIG = 2000
 METRIC = "site cutoffs/s on 1 GB300: plain scan vs learned window at |\u0394Rc|\u22640.01 GV"
 UNIT = "site cutoffs/s"
 WINDOW_FILE = os.path.join(ROOT, "cor-model_gb300", "window_t96.npz")
-# DRAM bytes (read + write) per trajectory of the scan kernel, from the ncu
-# capture of the profiling case (profiles/trace_kernel_igrf_t96_profile_case.md:
-# 1.61 MB + 0.19 MB over the 64,000 trajectories of its generation-0 launch)
-DRAM_BYTES_PER_TRAJ = (1.613312e6 + 0.185856e6) / 64000
+# DRAM bytes (read + write) per trajectory of the stream kernel, from the ncu
+# capture of its bulk profiling case (profiles/stream_kernel_igrf_t96_profile_case.md:
+# 1.70 MB + 0.24 MB over the 256,000 trajectories of the launch)
+DRAM_BYTES_PER_TRAJ = (1.704448e6 + 0.237056e6) / 256000
 TUNING_FILE = os.path.join(ROOT, "cor-model_gb300", "tuning.json")
 
 
@@ -463,7 +463,7 @@ def run_ours(args, rank: int, world: int, dist) -> dict | None:
                      "division_sqrt_cost_measured": [round(float(fn_flops[9]), 1), round(float(fn_flops[10]), 1)],
                      "traffic": DRAM_BYTES_PER_TRAJ * traj_done / max(1, args.steps * world),
                      "traffic_unit": "bytes per step (one batch), scaled by trajectories from the ncu capture of "
-                                     "the profiling case",
+                                     "the stream kernel's bulk profiling case (128 sites, 256,000 trajectories)",
                      "work_model": wm.get("source") + "; + - * / sqrt = 1 op, each transcendental at its cost "
                                    "measured on this GPU (cor_probe_fp64_functions, FMA-pipe flops per call)",
                      "flops_per_step_fixed_weight": wm["flops_per_step"],
