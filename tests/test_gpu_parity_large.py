@@ -90,15 +90,22 @@ def _jobs(g, sites):
 @pytest.mark.parametrize("name", ["t96", "ts05", "storm", "config1"])
 def test_scan_large_sets_against_reference(ctx, name):
     """1,000 T96 and 800 TS05 site-directions (nine arrival directions), 240
-    at four storm conditions, and 64 sites on the bench's own 0.01 GV grid."""
+    at four storm conditions, and 64 sites on the bench's own 0.01 GV grid,
+    traced through the scan stream (whose results are cor_trace_batch's,
+    tests/test_gpu_stream.py)."""
     g = golden("scan_large.json")[name]
     runs = golden("nudge_sensitivity.json")["scans_large"][name]["runs"]
     models = ct.model_set(ct.INTERNAL_SH, EXT[g["external"]])
     n = int(round((g["rk"] - g["rig"]) / g["del"])) + 1
     rows = []
-    for c in g["conditions"]:
-        p = ct.internal_setup(g["model"], c["time"], parmod=c["parmod"])
-        res = ctx.trace_batch(_jobs(g, c["sites"]), p, models=models)
+    # every condition of the set as one segment of a scan stream: one launch
+    # for the set, so the sets' long trajectories overlap instead of each
+    # condition's call waiting for its own
+    with ct.Stream(ctx, models, slots=8, idle_limit_s=300.0) as st:
+        tickets = [st.submit(_jobs(g, c["sites"]), ct.internal_setup(g["model"], c["time"], parmod=c["parmod"]))
+                   for c in g["conditions"]]
+        results = [st.wait(t, -1)[0] for t in tickets]
+    for c, res in zip(g["conditions"], results):
         for j, s in enumerate(c["sites"]):
             rows.append((_allowed_from_hex(s["allowed_hex"], n), s["cutoff"],
                          res.status[res.offsets[j]:res.offsets[j + 1]], res.sites[j]))
