@@ -116,14 +116,17 @@ def test_scan_large_sets_against_reference(ctx, name):
 
 def test_scan_storm_against_reference(ctx):
     """TS05 at 4 seeded storm conditions, 6 site-directions each (vertical and
-    30 deg zenith), 0.1 GV steps: the smaller storm set made by the reference."""
+    30 deg zenith), 0.1 GV steps: the smaller storm set made by the reference,
+    its four conditions as four segments of one scan-stream launch."""
     g = golden("scan_storm.json")
     nudge = golden("nudge_sensitivity.json")["scans"]["scan_storm.json"]
     models = ct.model_set(ct.INTERNAL_SH, ct.EXTERNAL_TS05)
     rows = []
-    for c in g["conditions"]:
-        p = ct.internal_setup(g["model"], c["time"], parmod=c["parmod"])
-        res = ctx.trace_batch(_jobs(g, c["sites"]), p, models=models)
+    with ct.Stream(ctx, models, slots=8, idle_limit_s=300.0) as st:
+        tickets = [st.submit(_jobs(g, c["sites"]), ct.internal_setup(g["model"], c["time"], parmod=c["parmod"]))
+                   for c in g["conditions"]]
+        results = [st.wait(t, -1)[0] for t in tickets]
+    for c, res in zip(g["conditions"], results):
         for j, s in enumerate(c["sites"]):
             st = res.status[res.offsets[j]:res.offsets[j + 1]]
             ref = np.zeros(len(st), bool)
