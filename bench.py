@@ -61,6 +61,7 @@ def tuning() -> dict:
         out = {k: t[k] for k in ("inflight", "park_below", "max_generations", "min_park")}
         if "stream" in t:
             out["stream_queue_order"] = t["stream"]["queue_order"]
+            out["stream_sort_lanes"] = t["stream"].get("sort_lanes", 1)
         return out | {"rigidity_major": t.get("rigidity_major", 1), "source": "autotune"}
     return {"inflight": 3, "park_below": 16, "max_generations": 48, "min_park": 256, "rigidity_major": 1,
             "source": "defaults"}
@@ -253,9 +254,16 @@ def cpu_baseline(n_batches: int) -> dict:
 
 
 # ---- the GPU arm -------------------------------------------------------------
+SORT_LANES = None  # --sort-lanes; None: the tuning file's choice (default 1)
+
+
+def sort_lanes() -> int:
+    return int(SORT_LANES if SORT_LANES is not None else tuning().get("stream_sort_lanes", 1))
+
+
 def stream_settings(n_jobs: int, n_traj: int) -> dict:
     return {"slots": 8, "max_jobs": max(1, n_jobs), "max_trajectories": max(1, n_traj), "max_params": 1,
-            "fixed_params": 4, "pool_params": 64, "idle_limit_s": 120.0}
+            "fixed_params": 4, "pool_params": 64, "idle_limit_s": 120.0, "sort_lanes": sort_lanes()}
 
 
 def run_device_segments(s, segs) -> list:
@@ -445,7 +453,7 @@ def run_ours(args, rank: int, world: int, dist) -> dict | None:
         "data": "synthetic grid of sites (the configuration's own sites; no dataset)",
         "config": {"workload": WORKLOAD, "sites_per_step": sites_done // max(1, args.steps * world),
                    "trajectories_per_step": traj_done // max(1, args.steps * world),
-                   "batches": args.batches, "tuning": tune,
+                   "batches": args.batches, "tuning": tune | {"stream_sort_lanes": sort_lanes()},
                    "execution": "one persistent scan-stream launch per timed run: every step's batch is a segment "
                                 "published to the resident kernel, whose lanes refill from the next segment as "
                                 "trajectories end",
@@ -542,7 +550,7 @@ def run_profile_case(args) -> dict:
         c = dict(zip(("accepted_steps", "trials", "trajectories", "watchdog", "kernel_launches"), v.tolist()))
     ctx.close()
     return {"profile_case": f"{len(sites)} sites x {N_RIG} rigidities, step limit {step_limit}",
-            "path": "stream" if args.profile_stream else "batch",
+            "path": "stream" if args.profile_stream else "batch", "sort_lanes": sort_lanes(),
             "trajectories": int(c["trajectories"]), "accepted_steps": int(c["accepted_steps"]),
             "trials": int(c["trials"]), "call_ms": ms}
 
@@ -634,7 +642,12 @@ def main():
     ap.add_argument("--profile-step-limit", type=int, default=PROFILE_STEP_LIMIT)
     ap.add_argument("--profile-stream", action="store_true",
                     help="with --profile-case: through a scan stream launched with everything staged")
+    ap.add_argument("--sort-lanes", type=int, choices=(0, 1), default=None,
+                    help="regroup each block's trajectories by field band before every field evaluation "
+                         "(default: the tuning file's choice, else 1)")
     args = ap.parse_args()
+    global SORT_LANES
+    SORT_LANES = args.sort_lanes
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
     dist = None

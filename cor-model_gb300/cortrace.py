@@ -86,7 +86,8 @@ class StreamConfig(C.Structure):
     _fields_ = [("slots", C.c_int32), ("max_jobs", C.c_int32), ("max_trajectories", C.c_int64),
                 ("max_params", C.c_int32), ("want_records", C.c_int32), ("reserve_sms", C.c_int32),
                 ("fixed_params", C.c_int32), ("pool_params", C.c_int32), ("segments_per_launch", C.c_int32),
-                ("idle_limit_s", C.c_double), ("launch_on_drain", C.c_int32), ("scan_events", C.c_int32)]
+                ("idle_limit_s", C.c_double), ("launch_on_drain", C.c_int32), ("scan_events", C.c_int32),
+                ("sort_lanes", C.c_int32)]
 
 
 class BatchResult(C.Structure):

@@ -1071,6 +1071,7 @@ extern "C" void cor_stream_config_default(cor_stream_config* c) {
     c->idle_limit_s = 60.;
     c->launch_on_drain = 0;
     c->scan_events = 0;
+    c->sort_lanes = 1;
 }
 
 static void stream_free(cor_stream* s) {
@@ -1117,7 +1118,8 @@ extern "C" int cor_stream_create(cor_ctx* ctx, cor_model_set models, uint64_t st
         cfg.fixed_params < 0 || cfg.pool_params < cfg.max_params || cfg.segments_per_launch < 1 ||
         cfg.reserve_sms < 0 || cfg.reserve_sms >= ctx->sms || !(cfg.idle_limit_s > 0.) ||
         cfg.idle_limit_s > 86400. || (cfg.want_records != 0 && cfg.want_records != 1) ||
-        (cfg.launch_on_drain != 0 && cfg.launch_on_drain != 1) || (cfg.scan_events != 0 && cfg.scan_events != 1))
+        (cfg.launch_on_drain != 0 && cfg.launch_on_drain != 1) || (cfg.scan_events != 0 && cfg.scan_events != 1) ||
+        (cfg.sort_lanes != 0 && cfg.sort_lanes != 1))
         return fail(ctx, COR_ERR_INVALID, "stream configuration out of range");
     const ModelOps* ops = find_ops(models);
     if (!ops) return fail(ctx, COR_ERR_UNSUPPORTED, "model set not available");
@@ -1223,6 +1225,7 @@ extern "C" int cor_stream_create(cor_ctx* ctx, cor_model_set models, uint64_t st
         sa.idle_limit_ns = (unsigned long long)(cfg.idle_limit_s * 1e9);
         sa.seg_cap = cfg.segments_per_launch;
         sa.n_params = cfg.fixed_params + cfg.pool_params;
+        sa.sort_lanes = cfg.sort_lanes;
     } while (0);
     if (rc != COR_OK) {
         stream_free(s);

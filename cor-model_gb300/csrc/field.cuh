@@ -92,4 +92,30 @@ __device__ __forceinline__ Vec3 calculate_field(const bool want, const Vec3 gsm_
     return want ? gsm_to_geo(tot, p) : tot;
 }
 
+// Which branches of the field code a GSM position (metres) takes, as a sort
+// key: lanes with equal keys run the same call sites of the expensive
+// sub-models, so a warp of them issues each sub-model once.  The key only
+// places lanes and never enters a result, so a position it misjudges costs
+// time, not bits.  With T96 the leading part is the band of the Region-2
+// field (r2_birk's xksi bands, lib/t96/t96.c:1265-1314), whose outer, sheet
+// and inner fields dominate the divergent work; then, for every model set,
+// the radius in whole R_E (the internal field's degree and T96/TS05's inner
+// structures change with it) and |z|/r in twelfths (latitude bands).
+template <class MS>
+__device__ __forceinline__ unsigned field_band(const Vec3 gsm_pos, const DevParams* __restrict__ dp) {
+    constexpr double kInvRe = 1.0 / kRe;
+    const double x = gsm_pos.x * kInvRe, y = gsm_pos.y * kInvRe, z = gsm_pos.z * kInvRe;
+    const double r = sqrt(x * x + y * y + z * z);
+    const unsigned ri = r < 31.0 ? (unsigned)r : 31u;
+    const double zr = r > 0.0 ? fabs(z) / r : 0.0;
+    const unsigned lat = zr < 1.0 ? (unsigned)(zr * 12.0) : 12u;
+    unsigned band = 0;
+    if constexpr (MS::external == COR_EXTERNAL_T96) {
+        const double xa = dp->t96.xappa;
+        const double xks = t96_xksi(x * xa, y * xa, z * xa);
+        band = xks < -0.045 ? 0u : xks < -0.015 ? 1u : xks < 0.015 ? 2u : xks < 0.045 ? 3u : 4u;
+    }
+    return (band << 9) | (ri << 4) | lat;
+}
+
 }  // namespace cor

@@ -14,10 +14,17 @@
         return cudaGetLastError();                                                                         \
     }                                                                                                      \
     static cudaError_t socc_##NAME(int* n) {                                                               \
-        return cudaOccupancyMaxActiveBlocksPerMultiprocessor(n, stream_kernel<MS_##NAME>, kTraceThreads, 0);         \
+        cudaError_t e = cudaFuncSetAttribute(stream_kernel<MS_##NAME>,                                     \
+                                             cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kStreamDynSmem); \
+        if (e != cudaSuccess) return e;                                                                    \
+        return cudaOccupancyMaxActiveBlocksPerMultiprocessor(n, stream_kernel<MS_##NAME>, kTraceThreads,   \
+                                                             kStreamDynSmem);                              \
     }                                                                                                      \
     static cudaError_t stream_##NAME(const StreamArgs& a, unsigned blocks, cudaStream_t s) {               \
-        stream_kernel<MS_##NAME><<<blocks, kTraceThreads, 0, s>>>(a);                                               \
+        cudaError_t e = cudaFuncSetAttribute(stream_kernel<MS_##NAME>,                                     \
+                                             cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kStreamDynSmem); \
+        if (e != cudaSuccess) return e;                                                                    \
+        stream_kernel<MS_##NAME><<<blocks, kTraceThreads, kStreamDynSmem, s>>>(a);                         \
         return cudaGetLastError();                                                                         \
     }                                                                                                      \
     static cudaError_t field_##NAME(const DevParams* p, int np, const int32_t* idx, const double* pos,     \

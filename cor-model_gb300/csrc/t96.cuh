@@ -533,10 +533,16 @@ static __device__ __noinline__ Vec3 t96_birk1shld(const double x, const double y
     return {bx, by, bz};
 }
 
-// birk1tot_02 (:619-807): the Region-1 field with its blend zones and shield.
-static __device__ __noinline__ Vec3 t96_birk1_blend(const double x, const double y, const double z, const double r,
-                                               const double r3, const double cpas, const double spas, const double t1,
-                                               const double t2, const bool south) {
+// The blend bands of birk1tot_02 (north :690-744, south :746-799): the two edge
+// points of the field line, where the two bases are evaluated, and the
+// distance-weighted mix of the two edge fields.
+struct B1Edges {
+    double x1, y1, z1, x2, y2, z2;
+};
+
+__device__ __forceinline__ B1Edges t96_birk1_edges(const double r, const double r3, const double cpas,
+                                                   const double spas, const double t1, const double t2,
+                                                   const bool south) {
     const double sqr = sqrt(r);
     const double s1 = ol_sin(t1);
     const double st01 = sqr / ol_pow(r3 + 1.0 / (s1 * s1 * s1 * s1 * s1 * s1) - 1.0, 0.1666666667);
@@ -547,18 +553,26 @@ static __device__ __noinline__ Vec3 t96_birk1_blend(const double x, const double
         ct01 = -ct01;
         ct02 = -ct02;
     }
-    const double x1 = r * st01 * cpas, y1 = r * st01 * spas, z1 = r * ct01;
-    const double x2 = r * st02 * cpas, y2 = r * st02 * spas, z2 = r * ct02;
-    const Vec3 b1 = south ? t96_r1_condip(x1, y1, z1) : t96_r1_loops(x1, y1, z1);
-    const Vec3 b2 = south ? t96_r1_loops(x2, y2, z2) : t96_r1_condip(x2, y2, z2);
-    const double dx2 = x2 - x1, dy2 = y2 - y1, dz2 = z2 - z1;
+    return {r * st01 * cpas, r * st01 * spas, r * ct01, r * st02 * cpas, r * st02 * spas, r * ct02};
+}
+
+__device__ __forceinline__ Vec3 t96_birk1_mix(const double x, const double y, const double z, const B1Edges& e,
+                                              const Vec3 b1, const Vec3 b2) {
+    const double dx2 = e.x2 - e.x1, dy2 = e.y2 - e.y1, dz2 = e.z2 - e.z1;
     const double ss = sqrt(dx2 * dx2 + dy2 * dy2 + dz2 * dz2);
-    const double dx = x - x1, dy = y - y1, dz = z - z1;
+    const double dx = x - e.x1, dy = y - e.y1, dz = z - e.z1;
     const double ds = sqrt(dx * dx + dy * dy + dz * dz);
     const double frac = ds / ss;
     return {b1.x * (1.0 - frac) + b2.x * frac, b1.y * (1.0 - frac) + b2.y * frac, b1.z * (1.0 - frac) + b2.z * frac};
 }
 
+// birk1tot_02, :619-807.  Every point needs the loops basis at most once and
+// the conical basis at most once: below and above the band one of them at
+// the point itself, inside the band both, one at each edge point (loops at
+// the poleward edge in the north, at the equatorward edge in the south).  So
+// each basis has a single call site, reached by every lane of the warp that
+// needs it: a warp whose lanes lie in different bands evaluates each basis
+// once instead of once per band.
 static __device__ __noinline__ Vec3 t96_birk1tot(const double x, const double y, const double z) {
     const double tnoonn = 12.0 * 0.01745329;
     const double tnoons = 3.141592654 - tnoonn;
@@ -576,25 +590,38 @@ static __device__ __noinline__ Vec3 t96_birk1tot(const double x, const double y,
     const double tr1n = tnoonn + dtet, tr1s = tnoons - dtet;
     const double t01n = tr1n - 0.034906, t01s = tr1s - 0.034906;
     const double t02s = tr1s + 0.034906, t02n = tr1n + 0.034906;
-    Vec3 b = {0.0, 0.0, 0.0};
-    if (tet0 < t01n || tet0 > t02s) {
-        const Vec3 t = t96_r1_loops(x, y, z);
-        b.x += t.x;
-        b.y += t.y;
-        b.z += t.z;
-    }
-    if (tet0 > t02n && tet0 < t01s) {
-        const Vec3 t = t96_r1_condip(x, y, z);
-        b.x += t.x;
-        b.y += t.y;
-        b.z += t.z;
-    }
-    if ((tet0 >= t01n && tet0 <= t02n) || (tet0 >= t01s && tet0 <= t02s)) {
+    const bool loops_here = tet0 < t01n || tet0 > t02s;
+    const bool condip_here = tet0 > t02n && tet0 < t01s;
+    const bool band = (tet0 >= t01n && tet0 <= t02n) || (tet0 >= t01s && tet0 <= t02s);
+    const bool south = tet0 >= t01s;
+    double pl[3] = {x, y, z}, pc[3] = {x, y, z};
+    B1Edges e = {0.0, 0.0, 0.0, 0.0, 0.0, 0.0};
+    if (band) {
         double spas, cpas;
         ol_sincos(pas, &spas, &cpas);
-        const bool south = tet0 >= t01s;
-        b = t96_birk1_blend(x, y, z, r, r3, cpas, spas, south ? t01s : t01n, south ? t02s : t02n, south);
+        e = t96_birk1_edges(r, r3, cpas, spas, south ? t01s : t01n, south ? t02s : t02n, south);
+        pl[0] = south ? e.x2 : e.x1;
+        pl[1] = south ? e.y2 : e.y1;
+        pl[2] = south ? e.z2 : e.z1;
+        pc[0] = south ? e.x1 : e.x2;
+        pc[1] = south ? e.y1 : e.y2;
+        pc[2] = south ? e.z1 : e.z2;
     }
+    Vec3 tl = {0.0, 0.0, 0.0}, tc = {0.0, 0.0, 0.0};
+    if (loops_here || band) tl = t96_r1_loops(pl[0], pl[1], pl[2]);
+    if (condip_here || band) tc = t96_r1_condip(pc[0], pc[1], pc[2]);
+    Vec3 b = {0.0, 0.0, 0.0};
+    if (loops_here) {
+        b.x += tl.x;
+        b.y += tl.y;
+        b.z += tl.z;
+    }
+    if (condip_here) {
+        b.x += tc.x;
+        b.y += tc.y;
+        b.z += tc.z;
+    }
+    if (band) b = t96_birk1_mix(x, y, z, e, south ? tc : tl, south ? tl : tc);
     const Vec3 s = t96_birk1shld(x, y, z);
     return {b.x + s.x, b.y + s.y, b.z + s.z};
 }
@@ -917,34 +944,30 @@ static __device__ __noinline__ Vec3 t96_r2sheet(const double x, const double y, 
     return {bx, by, acc};
 }
 
-// r2_birk, :1265-1314
+// r2_birk, :1265-1314.  The five bands of xksi mix the outer, sheet and
+// inner fields; each has a single call site, so a warp whose lanes lie in
+// different bands evaluates each of them once.
 static __device__ __noinline__ Vec3 t96_r2birk(const double x, const double y, const double z) {
     const double dl = 0.03, dl1 = 0.015;
     const double xks = t96_xksi(x, y, z);
-    if (xks < -(dl + dl1)) {
-        const Vec3 q = t96_r2outer(x, y, z);
-        return {q.x * -0.02, q.y * -0.02, q.z * -0.02};
-    }
-    if (xks < -dl + dl1) {
-        const Vec3 q1 = t96_r2outer(x, y, z);
-        const Vec3 q2 = t96_r2sheet(x, y, z, xks);
+    const int band = xks < -(dl + dl1) ? 0 : xks < -dl + dl1 ? 1 : xks < dl - dl1 ? 2 : xks < dl + dl1 ? 3 : 4;
+    Vec3 qo = {0.0, 0.0, 0.0}, qs = {0.0, 0.0, 0.0}, qi = {0.0, 0.0, 0.0};
+    if (band <= 1) qo = t96_r2outer(x, y, z);
+    if (band >= 1 && band <= 3) qs = t96_r2sheet(x, y, z, xks);
+    if (band >= 3) qi = t96_r2inner(x, y, z);
+    if (band == 0) return {qo.x * -0.02, qo.y * -0.02, qo.z * -0.02};
+    if (band == 1) {
         const double f2 = -0.02 * t96_tksi(xks, -dl, dl1);
         const double f1 = -0.02 - f2;
-        return {q1.x * f1 + q2.x * f2, q1.y * f1 + q2.y * f2, q1.z * f1 + q2.z * f2};
+        return {qo.x * f1 + qs.x * f2, qo.y * f1 + qs.y * f2, qo.z * f1 + qs.z * f2};
     }
-    if (xks < dl - dl1) {
-        const Vec3 q = t96_r2sheet(x, y, z, xks);
-        return {q.x * -0.02, q.y * -0.02, q.z * -0.02};
-    }
-    if (xks < dl + dl1) {
-        const Vec3 q1 = t96_r2inner(x, y, z);
-        const Vec3 q2 = t96_r2sheet(x, y, z, xks);
+    if (band == 2) return {qs.x * -0.02, qs.y * -0.02, qs.z * -0.02};
+    if (band == 3) {
         const double f1 = -0.02 * t96_tksi(xks, dl, dl1);
         const double f2 = -0.02 - f1;
-        return {q1.x * f1 + q2.x * f2, q1.y * f1 + q2.y * f2, q1.z * f1 + q2.z * f2};
+        return {qi.x * f1 + qs.x * f2, qi.y * f1 + qs.y * f2, qi.z * f1 + qs.z * f2};
     }
-    const Vec3 q = t96_r2inner(x, y, z);
-    return {-q.x * 0.02, -q.y * 0.02, -q.z * 0.02};
+    return {-qi.x * 0.02, -qi.y * 0.02, -qi.z * 0.02};
 }
 
 // dipole_t96, :1645-1656 (its x component keeps the reference's form)

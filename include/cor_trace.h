@@ -27,7 +27,7 @@
 extern "C" {
 #endif
 
-#define COR_TRACE_ABI_VERSION 2
+#define COR_TRACE_ABI_VERSION 3
 
 /* Number of Gauss coefficients of the degree-13 internal models
  * (INTERNAL_COEFS_SIZE, lib/internal/coefs/coefs.h:6). */
@@ -361,6 +361,9 @@ typedef struct {
                                   never waits on the host (at most `slots` segments per launch; default 0) */
     int32_t scan_events;       /* 1: each cor_stream_submit scan's result is also written to mapped host
                                   memory as soon as it is reduced (cor_stream_poll_scans; default 0)     */
+    int32_t sort_lanes;        /* 1: before each field evaluation a block regroups its trajectories by the
+                                  branches of the field code their positions take, so a warp's lanes run
+                                  the same sub-models (results are unchanged; default 1); 0: never      */
 } cor_stream_config;
 
 void cor_stream_config_default(cor_stream_config *cfg);

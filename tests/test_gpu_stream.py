@@ -267,3 +267,28 @@ def test_stream_queue_orders_give_the_same_results(ctx, order):
         c2.close()
     for b, g in zip(batches, got):
         _same(g[0], ctx.trace_batch(b, p), records=False)
+
+
+@pytest.mark.parametrize("external", [ct.EXTERNAL_NONE, ct.EXTERNAL_T96])
+def test_lane_regrouping_moves_time_only(ctx, external):
+    """Regrouping a block's trajectories by field band before every field
+    evaluation (sort_lanes, the default) moves trajectories between threads
+    but not their arithmetic: flags, cutoffs, final records and counters equal
+    the unsorted stream's bit for bit (IGRF-14 alone, and with T96, whose key
+    also evaluates the Region-2 band)."""
+    if external == ct.EXTERNAL_T96:
+        g = golden("scan_t96.json")
+        p = ct.internal_setup("igrf14", g["time"], parmod=[6.5, -150.0, 8.0, -12.0])
+        batches = [_jobs([(s["lat"], s["lon"]) for s in g["sites"][:12]], rig=0.1, rk=20.0, dele=0.1)]
+    else:
+        p = ct.internal_setup("igrf14", [2020, 1, 1, 1, 0, 0, 0])
+        batches = _batches()
+    models = ct.model_set(ct.INTERNAL_SH, external)
+    out = {}
+    for sort in (0, 1):
+        with ct.Stream(ctx, models, slots=4, want_records=1, sort_lanes=sort, idle_limit_s=120.0) as s:
+            tickets = [s.submit(b, p, want_records=True) for b in batches]
+            out[sort] = [s.wait(t, WAIT_MS) for t in tickets]
+    for a, b in zip(out[0], out[1]):
+        assert a is not None and b is not None
+        _same(b[0], a[0])
