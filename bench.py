@@ -512,6 +512,7 @@ def run_profile_case(args) -> dict:
     ctx = ct.Context(dev)
     tune = tuning()
     ctx.set_queue_order(int(tune.get("stream_queue_order", tune["rigidity_major"])))
+    ctx.set_lane_sort(bool(sort_lanes()))
     ms = []
     if args.profile_stream:
         parts = [jobs[k::4] for k in range(4)]

@@ -101,6 +101,7 @@ EXPORTS = [
     "cor_internal_setup", "cor_gsm_setup", "cor_probe_fp64_peak", "cor_probe_fp64_functions",
     "cor_upload_crustal",
     "cor_trace_batch_device_noalloc", "cor_ctx_set_regroup", "cor_trace_steps", "cor_ctx_set_queue_order",
+    "cor_ctx_set_lane_sort",
     "cor_ctx_generation_log", "cor_stream_config_default", "cor_stream_create", "cor_stream_submit",
     "cor_stream_upload_params", "cor_stream_submit_device", "cor_stream_wait", "cor_stream_drain",
     "cor_stream_poll_scans",
@@ -134,6 +135,7 @@ def load(path: str = LIB_PATH) -> C.CDLL:
     lib.cor_upload_crustal.argtypes = [vp, vp, vp, i32]
     lib.cor_ctx_set_regroup.argtypes = [vp, i32, i32, i64]
     lib.cor_ctx_set_queue_order.argtypes = [vp, i32]
+    lib.cor_ctx_set_lane_sort.argtypes = [vp, i32]
     lib.cor_ctx_generation_log.argtypes = [vp, i32, vp, vp]
     lib.cor_ctx_generation_log.restype = i32
     lib.cor_trace_steps.argtypes = [vp, C.POINTER(BatchReq), C.POINTER(BatchResult), vp, C.c_uint32]
@@ -306,6 +308,11 @@ class Context:
         rigidity (2, streams)."""
         mode = int(rigidity_major) if not isinstance(rigidity_major, bool) else (1 if rigidity_major else 0)
         self._check(self.lib.cor_ctx_set_queue_order(self.h, mode), "cor_ctx_set_queue_order")
+
+    def set_lane_sort(self, on: bool = True) -> None:
+        """cor_ctx_set_lane_sort: regroup each block's trajectories by field
+        band before every field evaluation (the default) or never."""
+        self._check(self.lib.cor_ctx_set_lane_sort(self.h, 1 if on else 0), "cor_ctx_set_lane_sort")
 
     def upload_crustal(self, g: np.ndarray, h: np.ndarray, nmax: int) -> None:
         """cor_upload_crustal: packed lower-triangle G, H (index n(n+1)/2 + m)."""

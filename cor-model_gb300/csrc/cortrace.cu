@@ -59,6 +59,7 @@ struct cor_ctx {
     int crust_nmax = 0;
     int crust_n_first = 0;
     int rig_major = 1;                    // queue order for uniform grids (cor_ctx_set_queue_order)
+    int sort_lanes = 1;                   // regroup lanes by field band (cor_ctx_set_lane_sort)
     int park_below = 16;                  // regroup settings (cor_ctx_set_regroup)
     int max_generations = 48;
     uint64_t min_park = 256;
@@ -442,6 +443,13 @@ extern "C" int32_t cor_ctx_generation_log(const cor_ctx* ctx, int32_t cap, uint6
     return n;
 }
 
+extern "C" int cor_ctx_set_lane_sort(cor_ctx* ctx, int32_t on) {
+    if (!ctx) return COR_ERR_INVALID;
+    if (on != 0 && on != 1) return fail(ctx, COR_ERR_INVALID, "lane sort must be 0 or 1");
+    ctx->sort_lanes = on;
+    return COR_OK;
+}
+
 extern "C" int cor_ctx_set_queue_order(cor_ctx* ctx, int32_t rigidity_major) {
     if (!ctx) return COR_ERR_INVALID;
     if (rigidity_major < 0 || rigidity_major > 2) return fail(ctx, COR_ERR_INVALID, "queue order must be 0, 1 or 2");
@@ -505,6 +513,7 @@ extern "C" int cor_trace_batch_device(cor_ctx* ctx, const cor_scan_job* jobs_dev
     CUDA_TRY(ctx, cudaSetDevice(ctx->device));
     TraceArgs a;
     memset(&a, 0, sizeof a);
+    a.sort_lanes = ctx->sort_lanes;
     a.step_records = ctx->step_dev;
     a.step_cap = ctx->step_cap;
     a.jobs = jobs_dev;
@@ -912,6 +921,7 @@ extern "C" int cor_trace_batch_device_noalloc(cor_ctx* ctx, const cor_scan_job* 
 
     TraceArgs a;
     memset(&a, 0, sizeof a);
+    a.sort_lanes = ctx->sort_lanes;
     a.jobs = jobs_dev;
     a.trig = reinterpret_cast<const JobTrig*>(trig_dev);
     a.offsets = offsets_dev;
@@ -1225,7 +1235,7 @@ extern "C" int cor_stream_create(cor_ctx* ctx, cor_model_set models, uint64_t st
         sa.idle_limit_ns = (unsigned long long)(cfg.idle_limit_s * 1e9);
         sa.seg_cap = cfg.segments_per_launch;
         sa.n_params = cfg.fixed_params + cfg.pool_params;
-        sa.sort_lanes = cfg.sort_lanes;
+        sa.a.sort_lanes = cfg.sort_lanes;
     } while (0);
     if (rc != COR_OK) {
         stream_free(s);

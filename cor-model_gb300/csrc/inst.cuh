@@ -7,24 +7,31 @@
     namespace cor {                                                                                        \
     using MS_##NAME = ModelSet<I, E, C>;                                                                   \
     static cudaError_t occ_##NAME(int* n) {                                                                \
-        return cudaOccupancyMaxActiveBlocksPerMultiprocessor(n, trace_kernel<MS_##NAME>, kTraceThreads, 0);          \
+        cudaError_t e = cudaFuncSetAttribute(trace_kernel<MS_##NAME>,                                      \
+                                             cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kRegroupSmem); \
+        if (e != cudaSuccess) return e;                                                                    \
+        return cudaOccupancyMaxActiveBlocksPerMultiprocessor(n, trace_kernel<MS_##NAME>, kTraceThreads,    \
+                                                             kRegroupSmem);                                \
     }                                                                                                      \
     static cudaError_t gen_##NAME(const TraceArgs& a, unsigned blocks, cudaStream_t s) {                   \
-        trace_kernel<MS_##NAME><<<blocks, kTraceThreads, 0, s>>>(a);                                                 \
+        cudaError_t e = cudaFuncSetAttribute(trace_kernel<MS_##NAME>,                                      \
+                                             cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kRegroupSmem); \
+        if (e != cudaSuccess) return e;                                                                    \
+        trace_kernel<MS_##NAME><<<blocks, kTraceThreads, kRegroupSmem, s>>>(a);                            \
         return cudaGetLastError();                                                                         \
     }                                                                                                      \
     static cudaError_t socc_##NAME(int* n) {                                                               \
         cudaError_t e = cudaFuncSetAttribute(stream_kernel<MS_##NAME>,                                     \
-                                             cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kStreamDynSmem); \
+                                             cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kRegroupSmem); \
         if (e != cudaSuccess) return e;                                                                    \
         return cudaOccupancyMaxActiveBlocksPerMultiprocessor(n, stream_kernel<MS_##NAME>, kTraceThreads,   \
-                                                             kStreamDynSmem);                              \
+                                                             kRegroupSmem);                              \
     }                                                                                                      \
     static cudaError_t stream_##NAME(const StreamArgs& a, unsigned blocks, cudaStream_t s) {               \
         cudaError_t e = cudaFuncSetAttribute(stream_kernel<MS_##NAME>,                                     \
-                                             cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kStreamDynSmem); \
+                                             cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kRegroupSmem); \
         if (e != cudaSuccess) return e;                                                                    \
-        stream_kernel<MS_##NAME><<<blocks, kTraceThreads, kStreamDynSmem, s>>>(a);                         \
+        stream_kernel<MS_##NAME><<<blocks, kTraceThreads, kRegroupSmem, s>>>(a);                         \
         return cudaGetLastError();                                                                         \
     }                                                                                                      \
     static cudaError_t field_##NAME(const DevParams* p, int np, const int32_t* idx, const double* pos,     \

@@ -81,7 +81,6 @@ struct StreamArgs {
     unsigned long long idle_limit_ns;  // a block with no live lane gives up after waiting this long
     long long seg_cap;             // entries of seg_end
     int32_t n_params;              // blocks in the parameter pool (a job's param_index is checked against it)
-    int32_t sort_lanes;            // 1: regroup the block's trajectories by field band before each field pass
 };
 
 // Bits of the mapped error word.
@@ -173,102 +172,6 @@ __device__ __forceinline__ bool stream_finish(const StreamArgs& sa, unsigned slo
                                     __ldcg(reinterpret_cast<const unsigned long long*>(off) + j));
     const unsigned before = atomicAdd(ldcg_ptr(&sg->job_done) + j, 1u);
     return before + 1 == n_j;
-}
-
-// A trajectory in flight as it moves between threads of a block: the lane
-// state, the two job fields the steps read (zn, nk1), and its segment.
-struct LaneMove {
-    Vec3 pos, vel, field, gsm;
-    double b, v, time, alength, rig, zn;
-    const DevParams* par;
-    unsigned long long traj, seq;
-    uint32_t step, trials;
-    int32_t nk0, job_index, nk1;
-    uint32_t slot;
-};
-static_assert(sizeof(LaneMove) == 192, "LaneMove layout");
-
-// Dynamic shared memory of the stream kernel (regroup_lanes' scratch).
-struct RegroupScratch {
-    LaneMove mv[kTraceThreads];
-    unsigned key[kTraceThreads];
-    unsigned short at[kTraceThreads];   // the threads that hold a trajectory, in thread order
-    unsigned warp_live[kTraceThreads / 32];
-};
-constexpr size_t kStreamDynSmem = sizeof(RegroupScratch);
-
-// Block-wide: the threads that hold a trajectory (has) trade trajectories so
-// that, taken in thread order, their keys ascend (ties keep thread order).
-// The set of threads that hold one does not change: a thread waiting on a
-// claimed queue index, or with nothing to do, keeps its place.  Every lane
-// runs the same arithmetic wherever it sits, so a trajectory's results do not
-// depend on the thread it ends on.  All threads of the block call this.
-__device__ __forceinline__ void regroup_lanes(RegroupScratch& sc, const bool has, const unsigned key, Lane& L,
-                                              cor_scan_job& my_job, unsigned& slot, unsigned long long& seq,
-                                              const int tid) {
-    const int lane = tid & 31, warp = tid >> 5;
-    sc.key[tid] = has ? key : 0xffffffffu;
-    const unsigned live = __ballot_sync(0xffffffffu, has);
-    if (lane == 0) sc.warp_live[warp] = __popc(live);
-    __syncthreads();
-    int pos = __popc(live & ((1u << lane) - 1u));
-    for (int w = 0; w < warp; w++) pos += (int)sc.warp_live[w];
-    if (has) sc.at[pos] = (unsigned short)tid;
-    int rank = 0;
-    if (has) {
-        // keys of threads without a trajectory are above every real key
-        for (int j = 0; j < kTraceThreads; j++) {
-            const unsigned kj = sc.key[j];
-            rank += (kj < key || (kj == key && j < tid)) ? 1 : 0;
-        }
-    }
-    __syncthreads();
-    if (has) {
-        LaneMove& m = sc.mv[sc.at[rank]];
-        m.pos = L.pos;
-        m.vel = L.vel;
-        m.field = L.field;
-        m.gsm = L.gsm;
-        m.b = L.b;
-        m.v = L.v;
-        m.time = L.time;
-        m.alength = L.alength;
-        m.rig = L.rig;
-        m.zn = L.job->zn;
-        m.par = L.par;
-        m.traj = L.traj;
-        m.seq = seq;
-        m.step = L.step;
-        m.trials = L.trials;
-        m.nk0 = L.nk0;
-        m.job_index = L.job_index;
-        m.nk1 = L.job->nk1;
-        m.slot = slot;
-    }
-    __syncthreads();
-    if (has) {
-        const LaneMove& m = sc.mv[tid];
-        L.pos = m.pos;
-        L.vel = m.vel;
-        L.field = m.field;
-        L.gsm = m.gsm;
-        L.b = m.b;
-        L.v = m.v;
-        L.time = m.time;
-        L.alength = m.alength;
-        L.rig = m.rig;
-        L.par = m.par;
-        L.traj = m.traj;
-        L.step = m.step;
-        L.trials = m.trials;
-        L.nk0 = m.nk0;
-        L.job_index = m.job_index;
-        my_job.zn = m.zn;
-        my_job.nk1 = m.nk1;
-        L.job = &my_job;
-        seq = m.seq;
-        slot = m.slot;
-    }
 }
 
 template <class MS>
@@ -474,11 +377,11 @@ __global__ void __launch_bounds__(kTraceThreads, 1) stream_kernel(const StreamAr
             continue;
         }
         if (tid == 0) idle_since = 0;
-        if (sa.sort_lanes) {
+        if (a.sort_lanes) {
             // every thread that holds a trajectory needs its field now (it has
             // just started, or just accepted a step): group them by band
             const unsigned key = has ? field_band<MS>(L.gsm, L.par) : 0u;
-            regroup_lanes(sc, has, key, L, s_job[tid], slot, seq, tid);
+            regroup_lanes<true>(sc, has, key, L, &s_job[tid], slot, seq, tid);
         }
         if constexpr (MS::crustal != 0) {
             // the crustal sum is evaluated by the whole (converged) warp

@@ -86,6 +86,9 @@ struct TraceArgs {
     // over more SMs, a warp or two each, instead of packing them into a few
     // blocks whose warps would share one SM's FP64 pipe
     uint32_t active_threads;
+    // 1: before each field evaluation the block regroups the trajectories
+    // that need one by field_band (regroup_lanes); 0: never
+    int sort_lanes;
 };
 
 __device__ __forceinline__ int find_job(const uint64_t* __restrict__ off, int n_jobs, uint64_t t) {
@@ -317,6 +320,116 @@ __device__ __forceinline__ void warp_add_u64(unsigned long long* dst, unsigned l
 constexpr int kTraceThreads = 256;
 constexpr int kTraceWarps = kTraceThreads / 32;
 
+// A trajectory in flight as it moves between threads of a block: the lane
+// state, its scan (the stream kernel keeps a per-thread copy of the scan's
+// job, so there the two fields the steps read, zn and nk1, move instead of
+// the pointer), and, in the stream kernel, its segment.
+struct LaneMove {
+    Vec3 pos, vel, field, gsm;
+    double b, v, time, alength, rig, zn;
+    const DevParams* par;
+    const cor_scan_job* job;
+    unsigned long long traj, seq;
+    uint32_t step, trials;
+    int32_t nk0, job_index, nk1;
+    uint32_t slot;
+};
+static_assert(sizeof(LaneMove) == 200, "LaneMove layout");
+
+// Dynamic shared memory of the trace and stream kernels (regroup_lanes).
+struct RegroupScratch {
+    LaneMove mv[kTraceThreads];
+    unsigned key[kTraceThreads];
+    unsigned short at[kTraceThreads];   // the threads that take part, in thread order
+    unsigned warp_live[kTraceWarps];
+};
+constexpr size_t kRegroupSmem = sizeof(RegroupScratch);
+
+// Block-wide: the threads that take part (part: they hold a trajectory whose
+// field is evaluated next) trade trajectories so that, taken in thread order,
+// their keys ascend (ties keep thread order).  The set of threads that take
+// part does not change: a thread without a trajectory, or with one that
+// waits for nothing this pass, keeps its place.  Every lane runs the same
+// arithmetic wherever it sits, so a trajectory's results do not depend on
+// the thread it ends on.  JobCopy: L.job points at the thread's own copy of
+// the scan's job (my_job), which then takes the arriving trajectory's zn and
+// nk1.  All threads of the block call this.
+template <bool JobCopy>
+__device__ __forceinline__ void regroup_lanes(RegroupScratch& sc, const bool part, const unsigned key, Lane& L,
+                                              cor_scan_job* my_job, unsigned& slot, unsigned long long& seq,
+                                              const int tid) {
+    const int lane = tid & 31, warp = tid >> 5;
+    sc.key[tid] = part ? key : 0xffffffffu;
+    const unsigned live = __ballot_sync(0xffffffffu, part);
+    if (lane == 0) sc.warp_live[warp] = __popc(live);
+    __syncthreads();
+    int pos = __popc(live & ((1u << lane) - 1u));
+    for (int w = 0; w < warp; w++) pos += (int)sc.warp_live[w];
+    if (part) sc.at[pos] = (unsigned short)tid;
+    int rank = 0;
+    if (part) {
+        // keys of the threads that do not take part are above every real key
+        for (int j = 0; j < kTraceThreads; j++) {
+            const unsigned kj = sc.key[j];
+            rank += (kj < key || (kj == key && j < tid)) ? 1 : 0;
+        }
+    }
+    __syncthreads();
+    if (part) {
+        LaneMove& m = sc.mv[sc.at[rank]];
+        m.pos = L.pos;
+        m.vel = L.vel;
+        m.field = L.field;
+        m.gsm = L.gsm;
+        m.b = L.b;
+        m.v = L.v;
+        m.time = L.time;
+        m.alength = L.alength;
+        m.rig = L.rig;
+        m.par = L.par;
+        m.job = L.job;
+        if constexpr (JobCopy) {
+            m.zn = L.job->zn;
+            m.nk1 = L.job->nk1;
+        }
+        m.traj = L.traj;
+        m.seq = seq;
+        m.step = L.step;
+        m.trials = L.trials;
+        m.nk0 = L.nk0;
+        m.job_index = L.job_index;
+        m.slot = slot;
+    }
+    __syncthreads();
+    if (part) {
+        const LaneMove& m = sc.mv[tid];
+        L.pos = m.pos;
+        L.vel = m.vel;
+        L.field = m.field;
+        L.gsm = m.gsm;
+        L.b = m.b;
+        L.v = m.v;
+        L.time = m.time;
+        L.alength = m.alength;
+        L.rig = m.rig;
+        L.par = m.par;
+        L.traj = m.traj;
+        L.step = m.step;
+        L.trials = m.trials;
+        L.nk0 = m.nk0;
+        L.job_index = m.job_index;
+        if constexpr (JobCopy) {
+            my_job->zn = m.zn;
+            my_job->nk1 = m.nk1;
+            L.job = my_job;
+        } else {
+            L.job = m.job;
+        }
+        seq = m.seq;
+        slot = m.slot;
+    }
+}
+
 // One generation of the scan.  Every thread of a block stays in the loop
 // until the block leaves it as a whole: the exit and park decisions are
 // block-wide (__syncthreads_count / _or), which also lines the block's warps
@@ -330,6 +443,8 @@ constexpr int kTraceWarps = kTraceThreads / 32;
 // which restores them densely (the regroup step).
 template <class MS>
 __global__ void __launch_bounds__(kTraceThreads, 1) trace_kernel(const TraceArgs a) {
+    extern __shared__ __align__(16) unsigned char s_dyn[];
+    RegroupScratch& sc = *reinterpret_cast<RegroupScratch*>(s_dyn);
     Lane L;
     bool has = false, done = threadIdx.x >= a.active_threads;
     unsigned long long n_steps = 0, n_trials = 0, n_traj = 0, n_wd = 0;
@@ -404,6 +519,13 @@ __global__ void __launch_bounds__(kTraceThreads, 1) trace_kernel(const TraceArgs
                 if (lane == 0) atomicAdd(&a.gen->parked_warps, 1u);
                 break;
             }
+        }
+        if (a.sort_lanes) {
+            // the lanes whose field is evaluated now, grouped by band
+            const unsigned key = need_field ? field_band<MS>(L.gsm, L.par) : 0u;
+            unsigned no_slot = 0;
+            unsigned long long no_seq = 0;
+            regroup_lanes<false>(sc, need_field, key, L, nullptr, no_slot, no_seq, (int)threadIdx.x);
         }
         if constexpr (MS::crustal != 0) {
             // the crustal sum is evaluated by the whole (converged) warp

@@ -254,6 +254,16 @@ int32_t cor_ctx_generation_log(const cor_ctx *ctx, int32_t cap, uint64_t *live, 
  * (1) or by chunk (2).  Results do not depend on it. */
 int cor_ctx_set_queue_order(cor_ctx *ctx, int32_t rigidity_major);
 
+/* 1 (the default): before each field evaluation, every block of the scan
+ * kernel of cor_trace_batch, cor_trace_batch_device(_noalloc) and
+ * cor_trace_steps regroups its trajectories by the branches of the field
+ * code their positions take, so that a warp's lanes run the same sub-models;
+ * 0: never.  Results do not depend on it (a stream takes the same choice from
+ * cor_stream_config.sort_lanes).  Other values give COR_ERR_INVALID.  No
+ * counterpart in the reference (its OpenMP threads run one trajectory each,
+ * src/trajectory.c:11). */
+int cor_ctx_set_lane_sort(cor_ctx *ctx, int32_t on);
+
 /* Replaces the crustal model's coefficient table on this context: G and H as
  * packed lower triangles (index n*(n+1)/2 + m, degrees n = 0 .. nmax-1), the
  * layout of lib/chaos/coefs/chaos_7_16.h read by chaos_geo

@@ -24,6 +24,8 @@
 #define __forceinline__ inline __attribute__((always_inline))
 #define __noinline__ __attribute__((noinline))
 #define __restrict__ __restrict
+#define __shared__
+#define __align__(n) __attribute__((aligned(n)))
 #define __launch_bounds__(...)
 
 template <class T>
@@ -92,5 +94,6 @@ static inline int __popc(unsigned) { abort(); }
 static inline void __syncwarp(unsigned = 0xffffffffu) { abort(); }
 static inline int __syncthreads_count(int) { abort(); }
 static inline int __syncthreads_or(int) { abort(); }
+static inline void __syncthreads() { abort(); }
 template <class T>
 static inline T atomicAdd(T*, T) { abort(); }

@@ -274,8 +274,9 @@ def test_lane_regrouping_moves_time_only(ctx, external):
     """Regrouping a block's trajectories by field band before every field
     evaluation (sort_lanes, the default) moves trajectories between threads
     but not their arithmetic: flags, cutoffs, final records and counters equal
-    the unsorted stream's bit for bit (IGRF-14 alone, and with T96, whose key
-    also evaluates the Region-2 band)."""
+    the unsorted run's bit for bit, through the stream and through
+    cor_trace_batch (IGRF-14 alone, and with T96, whose key also evaluates
+    the Region-2 band)."""
     if external == ct.EXTERNAL_T96:
         g = golden("scan_t96.json")
         p = ct.internal_setup("igrf14", g["time"], parmod=[6.5, -150.0, 8.0, -12.0])
@@ -292,3 +293,14 @@ def test_lane_regrouping_moves_time_only(ctx, external):
     for a, b in zip(out[0], out[1]):
         assert a is not None and b is not None
         _same(b[0], a[0])
+    # the batch kernel (cor_trace_batch, its generations and parking) likewise
+    batch = {}
+    for sort in (0, 1):
+        c = ct.Context(0)
+        try:
+            c.set_lane_sort(bool(sort))
+            batch[sort] = [c.trace_batch(b, p, models=models, want_records=True) for b in batches]
+        finally:
+            c.close()
+    for a, b in zip(batch[0], batch[1]):
+        _same(b, a)
