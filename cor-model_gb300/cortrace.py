@@ -161,7 +161,14 @@ def load(path: str = LIB_PATH) -> C.CDLL:
 
 
 def _ptr(a: np.ndarray | None) -> int | None:
-    return None if a is None else a.ctypes.data
+    """Address of a C-contiguous array for the C ABI, which reads whole rows
+    from it: a strided view would hand C the wrong elements (or memory past
+    the array), so it is refused."""
+    if a is None:
+        return None
+    if not a.flags.c_contiguous:
+        raise ValueError("the C ABI needs a contiguous array (np.ascontiguousarray)")
+    return a.ctypes.data
 
 
 class CorError(RuntimeError):
@@ -174,7 +181,7 @@ def internal_setup(version: str, time7, parmod=None) -> np.ndarray:
     """internal_recalc for model `version` at time {iy, mes, ide, id, ih, min, is}."""
     lib = load()
     p = np.zeros(1, PARAMS_DTYPE)
-    t = np.asarray(time7, dtype=np.int32)
+    t = np.ascontiguousarray(time7, dtype=np.int32)
     rc = lib.cor_internal_setup(version.encode(), _ptr(t), _ptr(p))
     if rc != COR_OK:
         raise CorError(rc, f"internal set-up of {version} at {list(time7)}")
@@ -185,6 +192,7 @@ def internal_setup(version: str, time7, parmod=None) -> np.ndarray:
 
 def batch_offsets(jobs: np.ndarray) -> tuple[int, np.ndarray]:
     lib = load()
+    jobs = np.ascontiguousarray(jobs, JOB_DTYPE)
     off = np.zeros(len(jobs) + 1, np.uint64)
     n = C.c_uint64(0)
     rc = lib.cor_batch_count(_ptr(jobs), len(jobs), C.byref(n), _ptr(off))
@@ -195,6 +203,7 @@ def batch_offsets(jobs: np.ndarray) -> tuple[int, np.ndarray]:
 
 def prepare_trig(jobs: np.ndarray) -> np.ndarray:
     lib = load()
+    jobs = np.ascontiguousarray(jobs, JOB_DTYPE)
     out = np.zeros(len(jobs), TRIG_DTYPE)
     rc = lib.cor_prepare_trig(_ptr(jobs), len(jobs), _ptr(out))
     if rc != COR_OK:

@@ -102,7 +102,7 @@ class Network:
     def forward(self, x):
         """x: torch CUDA float32 (n, 19) -> (n, 2)."""
         assert x.dim() == 2 and x.shape[1] == N_IN, x.shape
-        x = x.contiguous()
+        x = x.to(device=self.device, dtype=self.torch.float32).contiguous()
         y = self.torch.empty((x.shape[0], N_OUT), dtype=self.torch.float32, device=x.device)
         self._check(self.lib.cor_mlp_forward(self.h, x.data_ptr(), x.shape[0], y.data_ptr(), self._stream()),
                     "forward")
@@ -110,7 +110,8 @@ class Network:
 
     def train_step(self, x, t, lr: float, weight_decay: float = 1e-4) -> float:
         assert x.shape[1] == N_IN and t.shape[1] == N_OUT and x.shape[0] == t.shape[0]
-        x, t = x.contiguous(), t.contiguous()
+        x = x.to(device=self.device, dtype=self.torch.float32).contiguous()
+        t = t.to(device=self.device, dtype=self.torch.float32).contiguous()
         self._check(self.lib.cor_mlp_train_step(self.h, x.data_ptr(), t.data_ptr(), x.shape[0], lr, weight_decay,
                                                 self.loss.data_ptr(), None, self._stream()), "train_step")
         return float(self.loss.item())
@@ -118,7 +119,8 @@ class Network:
     def gradient(self, x, t):
         """(loss, gradient in the parameter layout) without an update."""
         assert x.shape[1] == N_IN and t.shape[1] == N_OUT and x.shape[0] == t.shape[0]
-        x, t = x.contiguous(), t.contiguous()
+        x = x.to(device=self.device, dtype=self.torch.float32).contiguous()
+        t = t.to(device=self.device, dtype=self.torch.float32).contiguous()
         g = self.torch.zeros(N_PARAMS, dtype=self.torch.float32, device=x.device)
         self._check(self.lib.cor_mlp_gradient(self.h, x.data_ptr(), t.data_ptr(), x.shape[0], self.loss.data_ptr(),
                                               g.data_ptr(), self._stream()), "gradient")

@@ -99,3 +99,20 @@ def test_regroup_and_steps_reject_null_context():
     lib = ct.load()
     assert lib.cor_ctx_set_regroup(None, 16, 48, 256) == -1
     assert lib.cor_trace_steps(None, None, None, None, 0) == -1
+
+
+def test_binding_takes_strided_job_views_by_value():
+    """The host helpers read whole job rows from the address they get: a
+    strided or reversed view is copied to a contiguous array first, so every
+    row is the one the caller meant, and a raw strided pointer is refused."""
+    jobs = np.concatenate([ct.make_job(float(lat), float(lon), rig=1.0, rk=3.0 + lat / 90.0, dele=0.5)
+                           for lat in (-60, -20, 0, 30, 70) for lon in (10, 200)])
+    for view in (jobs[1::3], jobs[::-1], jobs[::2]):
+        assert not view.flags.c_contiguous
+        copy = view.copy()
+        assert np.array_equal(ct.prepare_trig(view).view(np.uint8), ct.prepare_trig(copy).view(np.uint8))
+        n_view, off_view = ct.batch_offsets(view)
+        n_copy, off_copy = ct.batch_offsets(copy)
+        assert n_view == n_copy and np.array_equal(off_view, off_copy)
+    with pytest.raises(ValueError):
+        ct._ptr(jobs[::2])
