@@ -108,6 +108,7 @@ EXPORTS = [
     "cor_stream_close",
 ]
 NOALLOC_MAX_TRAJ = 1048576  # COR_NOALLOC_MAX_TRAJ
+ABI_VERSION = 3  # COR_TRACE_ABI_VERSION: the structure layouts above
 
 _lib = None
 
@@ -126,6 +127,9 @@ def load(path: str = LIB_PATH) -> C.CDLL:
     lib.cor_last_error_string.argtypes = [vp]
     lib.cor_last_error_string.restype = C.c_char_p
     lib.cor_abi_version.restype = C.c_int
+    if lib.cor_abi_version() != ABI_VERSION:
+        raise RuntimeError(f"{path} has ABI version {lib.cor_abi_version()}, this binding needs {ABI_VERSION}: "
+                           "rebuild it with __graft_entry__.build()")
     lib.cor_batch_count.argtypes = [vp, i32, C.POINTER(u64), vp]
     lib.cor_prepare_trig.argtypes = [vp, i32, vp]
     lib.cor_trace_batch.argtypes = [vp, C.POINTER(BatchReq), C.POINTER(BatchResult)]

@@ -33,7 +33,7 @@ def test_library_exports_every_declared_function():
 
 
 def test_abi_version():
-    assert ct.load().cor_abi_version() == 3
+    assert ct.load().cor_abi_version() == ct.ABI_VERSION == 3
 
 
 def test_batch_count_matches_reference_grid():
