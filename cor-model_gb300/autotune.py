@@ -131,14 +131,17 @@ def tune(ctxs, batches, p, models, cands, log=None):
     return {k: best[k] for k in KNOBS}, results
 
 
-STREAM_KNOBS = ("segments", "queue_order")
+STREAM_KNOBS = ("segments", "queue_order", "sort_lanes")
 
 
 def stream_candidates():
     """The sample as 16 interleaved segments under each queue order (0 scan
     by scan, 1 rigidity-major, 2 warp-wide chunks of one scan in ascending
-    rigidity), and as 4 and 64 segments under the chunked order."""
-    return [{"segments": n, "queue_order": o} for n, o in ((16, 0), (16, 1), (16, 2), (4, 2), (64, 2))]
+    rigidity), and as 4 and 64 segments under the chunked order, all with the
+    blocks regrouping their lanes by field band; and 16 chunked segments
+    without the regrouping."""
+    return [{"segments": n, "queue_order": o, "sort_lanes": s}
+            for n, o, s in ((16, 0, 1), (16, 1, 1), (16, 2, 1), (4, 2, 1), (64, 2, 1), (16, 2, 0))]
 
 
 def tune_stream(run_launch, cands, log=None):
@@ -166,7 +169,8 @@ def stream_launcher(ctx, grid_jobs, p, models):
         ctx.set_queue_order(int(c["queue_order"]))
         parts = [grid_jobs[k::c["segments"]] for k in range(c["segments"])]
         st = ct.Stream(ctx, models, slots=max(8, c["segments"]), max_jobs=max(len(x) for x in parts),
-                       max_trajectories=max(len(x) for x in parts) * 2000, max_params=1, idle_limit_s=300.0)
+                       max_trajectories=max(len(x) for x in parts) * 2000, max_params=1, idle_limit_s=300.0,
+                       sort_lanes=int(c.get("sort_lanes", 1)))
         try:
             tickets = [st.submit(x, p, want_status=False) for x in parts]
             got = [st.wait(t, -1)[0] for t in tickets]
@@ -194,7 +198,7 @@ def main():
         jobs = np.concatenate([ct.make_job(la, lo, rig=0.01, rk=20.0, dele=0.01) for la, lo in grid])
         ctx = ct.Context(0)
         run_launch = stream_launcher(ctx, jobs, p, models)
-        run_launch({"segments": 4, "queue_order": 1})               # load the kernels, warm the clocks
+        run_launch({"segments": 4, "queue_order": 1, "sort_lanes": 1})  # load the kernels, warm the clocks
         best, results = tune_stream(run_launch, stream_candidates(), log=lambda r: print(json.dumps(r), flush=True))
         ctx.close()
         prev = {}

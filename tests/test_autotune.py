@@ -90,14 +90,16 @@ def test_tune_stream_picks_the_fastest_with_the_same_results():
     sites = np.zeros(6, ct.SITE_DTYPE)
     sites["r_cutoff"] = np.arange(6) * 0.5
     cands = autotune.stream_candidates()
-    times = {(16, 0): 30.0, (16, 1): 31.0, (16, 2): 20.0, (4, 2): 25.0, (64, 2): 10.0}
-    assert set(times) == {(c["segments"], c["queue_order"]) for c in cands}
+    times = {(16, 0, 1): 30.0, (16, 1, 1): 31.0, (16, 2, 1): 20.0, (4, 2, 1): 25.0, (64, 2, 1): 10.0,
+             (16, 2, 0): 22.0}
+    key = lambda c: (c["segments"], c["queue_order"], c["sort_lanes"])
+    assert set(times) == {key(c) for c in cands}
 
     def run_launch(c):
         out = sites.copy()
-        if (c["segments"], c["queue_order"]) == (64, 2):
+        if key(c) == (64, 2, 1):
             out["r_cutoff"][2] += 0.01                   # fastest, but wrong
-        return times[(c["segments"], c["queue_order"])], out
+        return times[key(c)], out
     best, results = autotune.tune_stream(run_launch, cands)
-    assert best == {"segments": 16, "queue_order": 2}
+    assert best == {"segments": 16, "queue_order": 2, "sort_lanes": 1}
     assert len(results) == len(cands) and sum(not r["same_results"] for r in results) == 1
