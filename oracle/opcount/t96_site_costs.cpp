@@ -41,6 +41,7 @@ enum Col {
     kR2Outer, kR2Sheet, kR2Inner,
     kR2Birk, kBirk1Tot,
     kRadius,    // |x| in R_E
+    kRingcurr, kShlcar, kTaildisk, kTail87,  // the parts of tailrc96 (one shield: all three cost alike)
     kCols
 };
 }  // namespace
@@ -145,6 +146,16 @@ int main(int argc, char** argv) {
         out[kBirk1Tot] = COST(t_birk1tot(xx, yy, zz, b));
         out[kRadius] = std::sqrt(s[3 * i] * s[3 * i] + s[3 * i + 1] * s[3 * i + 1] + s[3 * i + 2] * s[3 * i + 2]) /
                        6.3712e+06;
+        {
+            // a shield's cost does not depend on its coefficient values
+            flop_t coef[24];
+            for (int k = 0; k < 24; k++) coef[k] = 1.0 + 0.1 * k;
+            flop_t hx, hz;
+            out[kRingcurr] = COST(t_ringcurr(xx, yy, zz, b));
+            out[kShlcar] = COST(t_shlcar3x3(coef, xx, yy, zz, b));
+            out[kTaildisk] = COST(t_taildisk(xx, yy, zz, b));
+            out[kTail87] = COST(t_tail87(xx, zz, &hx, &hz));
+        }
         fwrite(out, sizeof(double), kCols, o);
     }
     fclose(o);

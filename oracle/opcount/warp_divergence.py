@@ -25,7 +25,9 @@ is evaluated, weighted by step.  This script
          (csrc/field.cuh) before the warps are formed (the scan stream's
          sort_lanes).
 Lanes per operation = the lanes' own work / the warp's issued work x 32; the
-field evaluation only (the step logic around it is left out).
+field evaluation only (the step logic around it is left out).  It also sizes
+splitting a lone long trajectory's field evaluation over the SM's four FP64
+pipes (tail_split).
 
 usage: python oracle/opcount/warp_divergence.py [n_trajectories]
 """
@@ -52,7 +54,8 @@ N_POSITIONS = 120000
 RE = 6.3712e6
 # column indices of t96_site_costs' output
 (WHOLE, SIGMA, CYL, TAIL, B2S, IC, B1S, B1PRE, B1BAND, LX, CX, BLEND, LE1, CE1, LE2, CE2, XKSI, R2BAND, OUTER,
- SHEET, INNER, R2BIRK, B1TOT, RADIUS, NCOLS) = range(25)
+ SHEET, INNER, R2BIRK, B1TOT, RADIUS, RINGCURR, SHLCAR, TAILDISK, TAIL87, NCOLS) = range(29)
+LONG = 5000   # accepted steps: the trajectories that make a run's tail
 
 
 def build() -> str:
@@ -71,14 +74,17 @@ def _trajectory(args):
     return pyoracle.trace_steps(job, p, models=ct.model_set(ct.INTERNAL_SH, ct.EXTERNAL_T96))["gsm"].copy()
 
 
-def sample_positions(n_traj: int, seed: int = 5) -> np.ndarray:
+def sample_positions(n_traj: int, seed: int = 5) -> tuple[np.ndarray, np.ndarray]:
+    """-> (positions, the accepted steps of the trajectory each belongs to)."""
     rng = np.random.default_rng(seed)
     sites = [(float(a), float(b)) for a in range(-90, 91, 5) for b in range(0, 360, 5)]
     picks = [(*sites[rng.integers(len(sites))], round(0.01 * int(rng.integers(1, 2001)), 2)) for _ in range(n_traj)]
     with mp.get_context("spawn").Pool(min(16, os.cpu_count() or 1)) as pool:
-        pts = np.concatenate(pool.map(_trajectory, picks, chunksize=1))
+        runs = pool.map(_trajectory, picks, chunksize=1)
+    pts = np.concatenate(runs)
+    length = np.repeat([len(r) for r in runs], [len(r) for r in runs])
     keep = np.sort(np.random.default_rng(seed + 1).choice(len(pts), min(N_POSITIONS, len(pts)), replace=False))
-    return np.ascontiguousarray(pts[keep])
+    return np.ascontiguousarray(pts[keep]), length[keep]
 
 
 def site_costs(pos: np.ndarray) -> np.ndarray:
@@ -167,9 +173,54 @@ class WarpModel:
         return {"lanes_per_op": 32.0 * lane_work / (32.0 * warp_work), "warp_work": warp_work}
 
 
+def tail_split(c: np.ndarray, igrf: np.ndarray, pipes: int = 4) -> dict:
+    """A lone trajectory's field evaluation split over the SM's FP64 pipes
+    (one warp per pipe, each taking whole independent sub-models), priced on
+    positions of long trajectories: the sub-models' mean costs, and the
+    longest-first assignment's makespan against the serial sum.  Chains that
+    must stay together: birk1tot_02's band decision with the basis it picks
+    (and, in a band, the decision before both bases), r2_birk's xksi with the
+    field it picks."""
+    b1 = c[:, B1BAND].astype(int)
+    r2 = c[:, R2BAND].astype(int)
+    band = b1 >= 2
+    blend_pre = np.where(b1 == 2, c[:, BLEND] - c[:, LE1] - c[:, CE2],
+                         np.where(b1 == 3, c[:, BLEND] - c[:, CE1] - c[:, LE2], 0.0))
+    pre = c[:, B1PRE] + blend_pre            # what both bases wait for (each warp that takes one repeats it)
+    needs_loops, needs_condip = b1 != 1, b1 != 0
+    items = {
+        "internal field": igrf,
+        "cylharm (dipole shield)": c[:, CYL],
+        "ringcurr": c[:, RINGCURR],
+        "ring-current shield": c[:, SHLCAR],
+        "tail sheet (taildisk)": c[:, TAILDISK],
+        "tail shield 2": c[:, SHLCAR],
+        "tail87": c[:, TAIL87],
+        "tail shield 3": c[:, SHLCAR],
+        "birk1 band decision + loops basis": np.where(needs_loops, pre + np.select(
+            [b1 == 0, b1 == 2, b1 == 3], [c[:, LX], c[:, LE1], c[:, LE2]], 0.0), 0.0),
+        "birk1 band decision + conical basis": np.where(needs_condip, pre + np.select(
+            [b1 == 1, b1 == 2, b1 == 3], [c[:, CX], c[:, CE2], c[:, CE1]], 0.0), 0.0),
+        "birk1 shield": c[:, B1S],
+        "birk2 shield": c[:, B2S],
+        "r2 xksi + outer": np.where(r2 <= 1, c[:, XKSI] + c[:, OUTER], 0.0),
+        "r2 xksi + sheet": np.where((r2 >= 1) & (r2 <= 3), c[:, XKSI] + c[:, SHEET], 0.0),
+        "r2 xksi + inner": np.where(r2 >= 3, c[:, XKSI] + c[:, INNER], 0.0),
+        "intercon": c[:, IC],
+    }
+    means = {k: float(v.mean()) for k, v in items.items()}
+    serial = float((c[:, WHOLE] + igrf).mean())   # the unsplit evaluation
+    load = [0.0] * pipes
+    for v in sorted(means.values(), reverse=True):
+        load[load.index(min(load))] += v
+    return {"mean_cost": {k: round(v) for k, v in means.items()}, "serial": round(serial),
+            "band_share": float(band.mean()), "pipes": pipes, "makespan": round(max(load)),
+            "speedup": serial / max(load)}
+
+
 def main(n_traj: int) -> dict:
     build()
-    pos = sample_positions(n_traj)
+    pos, length = sample_positions(n_traj)
     c = site_costs(pos)
     m = WarpModel(c, internal_costs(c[:, RADIUS]))
     key = field_band_key(pos, c[:, R2BAND])
@@ -191,6 +242,8 @@ def main(n_traj: int) -> dict:
                                            "speedup": base["warp_work"] / single["warp_work"]},
         "single_call_sites_sorted_by_field_band": {"lanes_per_op": sorted_["lanes_per_op"],
                                                    "speedup": base["warp_work"] / sorted_["warp_work"]},
+        f"tail_split_over_4_pipes (positions of trajectories >= {LONG} steps)":
+            tail_split(c[length >= LONG], m.igrf[length >= LONG]),
     }
 
 
