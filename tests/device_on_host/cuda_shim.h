@@ -53,10 +53,21 @@ struct ShimWarp {
 };
 static ShimWarp* shim_warp = nullptr;
 
+// Block emulation for the lane regrouping (regroup_lanes, trace.cuh): 256
+// host threads stand for a block's threads; __syncthreads waits on the block
+// barrier and each warp's ballots go through its own ShimWarp.  While
+// shim_block is set it takes the place of shim_warp.
+struct ShimBlock {
+    std::barrier<> bar{256};
+    ShimWarp warps[8];
+};
+static ShimBlock* shim_block = nullptr;
+static inline ShimWarp* shim_my_warp() { return shim_block ? &shim_block->warps[(threadIdx.x >> 5) & 7] : shim_warp; }
+
 template <class T>
 static inline T shim_exchange(T v, int src) {
     static_assert(sizeof(T) <= 8, "exchange of at most 8 bytes");
-    ShimWarp* w = shim_warp;
+    ShimWarp* w = shim_my_warp();
     if (!w) abort();
     uint64_t b = 0;
     memcpy(&b, &v, sizeof(T));
@@ -73,7 +84,7 @@ static inline T __shfl_sync(unsigned, T v, int src, int = 32) { return shim_exch
 template <class T>
 static inline T __shfl_xor_sync(unsigned, T v, int o, int = 32) { return shim_exchange(v, (int)(threadIdx.x & 31) ^ o); }
 static inline unsigned __ballot_sync(unsigned, int p) {
-    ShimWarp* w = shim_warp;
+    ShimWarp* w = shim_my_warp();
     if (!w) abort();
     w->slot[threadIdx.x & 31] = p != 0;
     w->bar.arrive_and_wait();
@@ -90,10 +101,13 @@ static inline int __ffs(unsigned x) { return __builtin_ffs((int)x); }
 // these let the header compile and abort if they are ever called.
 template <class T>
 static inline T __shfl_down_sync(unsigned, T, unsigned, int = 32) { abort(); }
-static inline int __popc(unsigned) { abort(); }
+static inline int __popc(unsigned x) { return __builtin_popcount(x); }
 static inline void __syncwarp(unsigned = 0xffffffffu) { abort(); }
 static inline int __syncthreads_count(int) { abort(); }
 static inline int __syncthreads_or(int) { abort(); }
-static inline void __syncthreads() { abort(); }
+static inline void __syncthreads() {
+    if (!shim_block) abort();
+    shim_block->bar.arrive_and_wait();
+}
 template <class T>
 static inline T atomicAdd(T*, T) { abort(); }

@@ -215,4 +215,52 @@ void host_rk_step(double h, double d, const double* field, double* vel, double* 
     pos[2] = nx.z;
 }
 
+// regroup_lanes (trace.cuh) on one emulated 256-thread block.  Thread t starts
+// with a trajectory tagged t (traj = t, step = 1000 + t, slot = t, seq =
+// 100000 + t, rig = t + 0.5, its job = jobs[t] with zn = t + 1 and nk1 = 7 + t)
+// when part[t] is set, and takes part with key[t].  job_copy selects the
+// stream kernel's form (each thread keeps its own copy of its scan's job) or
+// the batch kernel's (the job pointer moves).  out[t] gets, for the
+// trajectory thread t holds afterwards: traj, step, slot, seq, rig, zn, nk1,
+// and whether its job pointer is the thread's own copy.
+int host_regroup(const unsigned* key, const int32_t* part, int32_t job_copy, double* out) {
+    static cor_scan_job jobs[kTraceThreads], own[kTraceThreads];
+    static RegroupScratch sc;
+    for (int t = 0; t < kTraceThreads; t++) {
+        memset(&jobs[t], 0, sizeof(cor_scan_job));
+        jobs[t].zn = t + 1.0;
+        jobs[t].nk1 = 7 + t;
+        own[t] = jobs[t];
+    }
+    ShimBlock block;
+    shim_block = &block;
+    std::vector<std::thread> threads;
+    for (int t = 0; t < kTraceThreads; t++)
+        threads.emplace_back([&, t] {
+            threadIdx.x = (unsigned)t;
+            Lane L;
+            memset(&L, 0, sizeof L);
+            L.traj = (uint64_t)t;
+            L.step = 1000u + (uint32_t)t;
+            L.rig = t + 0.5;
+            L.job = job_copy ? &own[t] : &jobs[t];
+            unsigned slot = (unsigned)t;
+            unsigned long long seq = 100000ull + (unsigned long long)t;
+            if (job_copy) regroup_lanes<true>(sc, part[t] != 0, key[t], L, &own[t], slot, seq, t);
+            else regroup_lanes<false>(sc, part[t] != 0, key[t], L, nullptr, slot, seq, t);
+            double* o = out + 8 * t;
+            o[0] = (double)L.traj;
+            o[1] = (double)L.step;
+            o[2] = (double)slot;
+            o[3] = (double)seq;
+            o[4] = L.rig;
+            o[5] = L.job->zn;
+            o[6] = (double)L.job->nk1;
+            o[7] = L.job == &own[t] ? 1.0 : 0.0;
+        });
+    for (std::thread& th : threads) th.join();
+    shim_block = nullptr;
+    return 0;
+}
+
 }  // extern "C"

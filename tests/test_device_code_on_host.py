@@ -53,6 +53,7 @@ def _build(out_dir, defines=()) -> C.CDLL:
     lib.host_calculate_field_crustal.argtypes = [C.c_int, C.c_int, vp, vp, vp, C.c_int32, vp, C.c_int64, vp]
     lib.host_trace.argtypes = [C.c_int, C.c_int, vp, vp, C.c_int32, vp, C.c_uint64, vp, C.c_int32, C.c_uint64,
                                C.c_double, C.c_double, vp, vp]
+    lib.host_regroup.argtypes = [vp, vp, C.c_int32, vp]
     lib.host_tables()
     return lib
 
@@ -262,3 +263,38 @@ def test_crustal_model_set_composes_bit_for_bit(builds):
         got = np.zeros_like(pts)
         assert lib.host_calculate_field_crustal(1, ext, _p(p), _p(g), _p(h), nmax, _p(pts), len(pts), _p(got)) == 0
         assert _bits_equal(got, unhex(case["b"]).reshape(-1, 3)).all(), key
+
+
+@pytest.mark.parametrize("job_copy", [0, 1])
+def test_lane_regrouping_permutes_the_block(builds, job_copy):
+    """regroup_lanes on an emulated 256-thread block (256 host threads, a block
+    barrier and per-warp ballots): the threads that take part end up holding
+    exactly their original trajectories, in ascending key order (ties in
+    thread order), each with all of its own fields (step, segment slot and
+    sequence, rigidity, the job's zn and nk1); the others keep theirs.  In the
+    stream kernel's form the job fields land in the thread's own job copy."""
+    lib = builds["default"]
+    rng = np.random.default_rng(11)
+    for trial in range(3):
+        part = (rng.uniform(size=256) < (0.95, 0.5, 0.1)[trial]).astype(np.int32)
+        key = rng.integers(0, 40, size=256).astype(np.uint32)
+        out = np.zeros((256, 8))
+        lib.host_regroup(_p(key), _p(part), job_copy, _p(out))
+        origin = out[:, 0].astype(int)
+        holders = np.nonzero(part)[0]
+        # the threads that took part hold a permutation of their trajectories ...
+        assert sorted(origin[holders]) == sorted(holders)
+        # ... in ascending (key, original thread) order
+        order = sorted(holders, key=lambda t: (int(key[t]), int(t)))
+        assert list(origin[holders]) == order
+        # the others are untouched
+        rest = np.nonzero(part == 0)[0]
+        assert np.array_equal(origin[rest], rest)
+        # every field travelled with its trajectory
+        assert np.array_equal(out[:, 1], 1000 + origin)
+        assert np.array_equal(out[:, 2], origin)
+        assert np.array_equal(out[:, 3], 100000 + origin)
+        assert np.array_equal(out[:, 4], origin + 0.5)
+        assert np.array_equal(out[:, 5], origin + 1.0)
+        assert np.array_equal(out[:, 6], 7 + origin)
+        assert np.array_equal(out[:, 7], np.ones(256) if job_copy else np.zeros(256))
