@@ -47,9 +47,10 @@ METRIC = "site cutoffs/s on 1 GB300: plain scan vs learned window at |\u0394Rc|\
 UNIT = "site cutoffs/s"
 WINDOW_FILE = os.path.join(ROOT, "cor-model_gb300", "window_t96.npz")
 # DRAM bytes (read + write) per trajectory of the stream kernel, from the ncu
-# capture of its bulk profiling case (profiles/stream_kernel_igrf_t96_profile_case.md:
-# 1.70 MB + 0.24 MB over the 256,000 trajectories of the launch)
-DRAM_BYTES_PER_TRAJ = (1.704448e6 + 0.237056e6) / 256000
+# capture of its bulk profiling case with lane regrouping
+# (profiles/stream_kernel_igrf_t96_profile_case.md: 1.55 MB + 0.11 MB over the
+# 256,000 trajectories of the launch)
+DRAM_BYTES_PER_TRAJ = (1.551104e6 + 0.112640e6) / 256000
 TUNING_FILE = os.path.join(ROOT, "cor-model_gb300", "tuning.json")
 
 
